@@ -1,0 +1,237 @@
+/*
+ * xtrack_gb300.h — C-ABI of the GB300-native particle push that replaces
+ * xtrack's generated `track_line` kernel.
+ *
+ * Plain C types only: raw pointers and sizes, no torch or CUDA types apart
+ * from an opaque stream handle passed as `void*` (a cudaStream_t; NULL means
+ * the legacy default stream).
+ *
+ * Reference interfaces replaced (paths inside the xtrack source tree):
+ *   xtrack/tracker.py:546-564      track_line(...) kernel signature
+ *                                  (descriptor tracker.py:793-814)
+ *   xtrack/tracker.py:107-118      TrackerData / ElementRefData build
+ *                                  (tracker_data.py:65-172, 221-255)
+ *   xtrack/base_element.py:130-215 <Elem>_track_particles (per-element kernel)
+ *   xtrack/particles/particles.py:26-83   Particles structure-of-arrays
+ *   xtrack/monitors/particles_monitor.h:12-77  ParticlesMonitor record layout
+ *
+ * Error convention: every entry point returns an int32 status; 0 is success,
+ * negative values are host-detectable errors (XTG_E_*). Physics outcomes
+ * (losses) are reported only through the particles' `state` array, exactly as
+ * in the reference. Nothing here aborts or traps. The message of the last
+ * error on the calling thread is available from xtg_get_last_error().
+ */
+#ifndef XTRACK_GB300_H
+#define XTRACK_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define XTG_ABI_VERSION 1
+
+/* Maximum number of multipole coefficients per array (order <= 20). */
+#define XTG_MAX_KNL 21
+
+/* ---- status codes ------------------------------------------------------ */
+#define XTG_OK               0
+#define XTG_E_NULL          -1   /* a required pointer is NULL               */
+#define XTG_E_VALUE         -2   /* an argument is out of its valid range    */
+#define XTG_E_UNSUPPORTED   -3   /* element feature outside the built set    */
+#define XTG_E_CUDA          -4   /* a CUDA runtime call failed               */
+#define XTG_E_CAPACITY      -5   /* a size exceeds a compiled-in maximum     */
+#define XTG_E_TIMEOUT       -6   /* a bounded device wait gave up            */
+#define XTG_E_NOMEM         -7   /* an allocation failed                     */
+
+/* ---- element classes (reference class names, xtrack/beam_elements/) ---- */
+#define XTG_CLS_MARKER          0   /* marker.py                             */
+#define XTG_CLS_DRIFT           1   /* drift.py, drift.h                     */
+#define XTG_CLS_MULTIPOLE       2   /* multipole.py, multipole.h             */
+#define XTG_CLS_BEND            3   /* bend.py, bend.h                       */
+#define XTG_CLS_QUADRUPOLE      4   /* quadrupole.py, quadrupole.h           */
+#define XTG_CLS_SEXTUPOLE       5   /* sextupole.py, sextupole.h             */
+#define XTG_CLS_OCTUPOLE        6   /* octupole.py, octupole.h               */
+#define XTG_CLS_CAVITY          7   /* cavity.py, cavity.h                   */
+#define XTG_CLS_LIMIT_ELLIPSE   8   /* limit_ellipse.py, limitellipse.h      */
+#define XTG_CLS_LIMIT_RECT      9   /* limit_rect.py, limitrect.h            */
+#define XTG_NUM_CLS            10
+
+/* Slice kind of a record (slice classes of slice_elements_*.py). A slice
+ * record carries its parent's parameters plus its own `weight`. */
+#define XTG_SLICE_NONE    0   /* the element itself                           */
+#define XTG_SLICE_THICK   1   /* ThickSlice<X>  (thick_slice_*.h)             */
+#define XTG_SLICE_THIN    2   /* ThinSlice<X>   (thin_slice_*.h)              */
+#define XTG_SLICE_DRIFT   3   /* DriftSlice<X>  (drift_slice_*.h)             */
+#define XTG_SLICE_ENTRY   4   /* ThinSlice<X>Entry (edge map at entry)        */
+#define XTG_SLICE_EXIT    5   /* ThinSlice<X>Exit  (edge map at exit)         */
+
+/* Track flags bit positions (xtrack/track_flags.py:5-12). */
+#define XTG_FLAG_BACKTRACK               0
+#define XTG_FLAG_KILL_CAVITY_KICK        2
+#define XTG_FLAG_IGNORE_GLOBAL_APERTURE  3
+#define XTG_FLAG_IGNORE_LOCAL_APERTURE   4
+
+/*
+ * One lattice element as the reference stores it (the `_xofields` of each
+ * class, with slice parents resolved into the record). Fields a class does
+ * not have are ignored. Arrays hold `order+1` (knl/ksl) and `order_rel+1`
+ * (knl_rel/ksl_rel) valid entries.
+ */
+typedef struct xtg_element {
+    int32_t cls;                 /* XTG_CLS_*                                 */
+    int32_t slice;               /* XTG_SLICE_*                               */
+    int32_t model;               /* model index (_common.py:20-80)            */
+    int32_t integrator;          /* 0 adaptive,1 teapot,2 yoshida4,3 uniform  */
+    int64_t num_multipole_kicks; /* magnets; Cavity: num_kicks                */
+    int64_t order;               /* len(knl)-1                                */
+    int64_t order_rel;           /* len(knl_rel)-1; -1 when absent            */
+    int32_t isthick;             /* Multipole.isthick                         */
+    int32_t main_is_skew;        /* knl_rel reference component is skew       */
+    int32_t main_order;          /* Multipole.main_order                      */
+    int32_t edge_entry_active;
+    int32_t edge_exit_active;
+    int32_t edge_entry_model;    /* -1 suppressed, 0 linear, 1 full, 2 dipole */
+    int32_t edge_exit_model;
+    int32_t absolute_time;       /* Cavity                                    */
+    double weight;               /* slices; 1 for the element itself          */
+    double length;
+    double h;                    /* Bend curvature angle/length               */
+    double hxl;                  /* Multipole                                 */
+    double k0, k1, k2, k3;
+    double k0s, k1s, k2s, k3s;
+    double inv_factorial_order;  /* 1/order!                                  */
+    double knl[XTG_MAX_KNL];
+    double ksl[XTG_MAX_KNL];
+    double knl_rel[XTG_MAX_KNL];
+    double ksl_rel[XTG_MAX_KNL];
+    double edge_entry_angle, edge_exit_angle;
+    double edge_entry_angle_fdown, edge_exit_angle_fdown;
+    double edge_entry_fint, edge_exit_fint;
+    double edge_entry_hgap, edge_exit_hgap;
+    double voltage, frequency, harmonic, lag, phase;   /* Cavity            */
+    double a_squ, b_squ, a_b_squ;                      /* LimitEllipse      */
+    double min_x, max_x, min_y, max_y;                 /* LimitRect         */
+    /* Misalignment fields (base_element.py:274-282); must all be zero. */
+    double shift_x, shift_y, shift_s;
+    double rot_x_rad, rot_y_rad, rot_s_rad, rot_s_rad_no_frame;
+} xtg_element;
+
+/*
+ * Particles structure-of-arrays (particles.py:26-83). Pointers are device
+ * pointers for xtg_track and host pointers for the CPU oracle; every array has
+ * `capacity` entries. Fields the push does not touch (spin, rng, weight,
+ * pdg_id, parent_particle_id, gamma0) may be NULL.
+ */
+typedef struct xtg_particles {
+    int64_t capacity;
+    double q0, mass0, t_sim;
+    double *p0c, *gamma0, *beta0;
+    double *s, *zeta, *x, *y, *px, *py;
+    double *ptau, *delta, *rpp, *rvv;
+    double *chi, *charge_ratio, *weight;
+    double *ax, *ay;
+    int64_t *pdg_id, *particle_id, *at_element, *at_turn, *state;
+    int64_t *parent_particle_id;
+} xtg_particles;
+
+/*
+ * Turn-by-turn ParticlesMonitor (particles_monitor.h:12-77). Records have
+ * `n_records = (stop-start) * (part_id_end-part_id_start) * n_repetitions`
+ * entries in `data`; a record lands at
+ *   n_turns*(particle_id - part_id_start) + at_turn - start_at_turn
+ * (plus the frame offset when n_repetitions > 1). A NULL array in `data`
+ * means that field is not recorded (the reference records all of them).
+ */
+typedef struct xtg_monitor {
+    int64_t start_at_turn, stop_at_turn;
+    int64_t part_id_start, part_id_end;
+    int64_t ebe_mode;
+    int64_t n_repetitions, repetition_period;
+    int64_t n_records;
+    xtg_particles data;
+} xtg_monitor;
+
+/* Compile-time TrackerConfig equivalents (line.py:283-287). */
+typedef struct xtg_config {
+    int32_t use_exact_drifts;     /* XTRACK_USE_EXACT_DRIFTS                 */
+    int32_t cavity_preserve_angle;/* XTRACK_CAVITY_PRESERVE_ANGLE            */
+    int32_t has_global_xy_limit;  /* XTRACK_GLOBAL_XY_LIMIT defined          */
+    int32_t arith;                /* XTG_ARITH_EXACT or XTG_ARITH_FAST       */
+    double global_xy_limit;       /* its value, 1.0 by default               */
+} xtg_config;
+
+/* Arithmetic of the push (xtg_config.arith).
+ * EXACT: the reference's operation order, no fused multiply-add; results
+ *        equal the reference CPU build bit for bit except for the last-ulp
+ *        behaviour of sin/cos/atan2/asin/sinh/cosh.
+ * FAST:  the minimal formulation (one merged complex Horner polynomial per
+ *        kick, fused multiply-adds, merged half drifts); results agree with
+ *        the reference to within its own rounding noise. */
+#define XTG_ARITH_EXACT 0
+#define XTG_ARITH_FAST  1
+
+typedef struct xtg_lattice xtg_lattice;   /* opaque handle */
+
+/* Library / ABI information. */
+int32_t xtg_abi_version(void);
+
+/* Copies the last error message of the calling thread into buf (size n). */
+int32_t xtg_get_last_error(char* buf, int64_t n);
+
+/*
+ * Builds the packed element-parameter table from `n_elements` raw records
+ * and uploads it to the current CUDA device. Replaces TrackerData
+ * construction (tracker_data.py:65-172) and the per-particle model
+ * resolution of track_magnet_particles (track_magnet.h:518-574), which is
+ * hoisted here. Allocates device memory; the handle owns it.
+ */
+int32_t xtg_lattice_create(const xtg_element* elements, int64_t n_elements,
+                           const xtg_config* config, xtg_lattice** out);
+
+/* Frees the device table and the handle. Safe on NULL. */
+int32_t xtg_lattice_destroy(xtg_lattice* lattice);
+
+/* Number of elements and the FP64 FLOPs one particle spends on elements
+ * [ele_start, ele_start+num_ele) in the canonical minimal formulation
+ * (FMA = 2, div/sqrt/sin/cos = 1). Used for roofline accounting. */
+int32_t xtg_lattice_info(const xtg_lattice* lattice, int64_t* n_elements,
+                         int64_t ele_start, int64_t num_ele,
+                         double* flops_per_particle);
+
+/*
+ * The push: replaces track_line (tracker.py:546-750). Tracks particles
+ * [0, capacity) through `num_turns` turns of elements
+ * [ele_start, ele_start+num_ele_track), writing the particles in place.
+ * `monitor` may be NULL (flag_monitor must then be 0). Asynchronous on
+ * `stream`; no allocation on this path.
+ */
+int32_t xtg_track(const xtg_lattice* lattice, const xtg_particles* particles,
+                  int32_t num_turns, int32_t ele_start, int32_t num_ele_track,
+                  int32_t flag_end_turn_actions, int32_t flag_reset_s_at_end_turn,
+                  int32_t flag_monitor, int32_t num_ele_line, double line_length,
+                  const xtg_monitor* monitor, uint64_t track_flags,
+                  void* stream);
+
+/* Launch-shape tuning for xtg_track (block size and compaction period in
+ * turns; 0 keeps the default). Returns the values in effect. */
+int32_t xtg_set_launch_config(xtg_lattice* lattice, int32_t block_size,
+                              int32_t compact_every, int32_t* out_block_size,
+                              int32_t* out_compact_every);
+
+/* Blocks until all work on `stream` is done; returns XTG_E_CUDA on error. */
+int32_t xtg_sync(void* stream);
+
+/* Number of kernel launches xtg_track issued since the library loaded. */
+int64_t xtg_launch_count(void);
+
+/* FP64 peak probe: DFMA throughput of the current device in FLOP/s
+ * (FMA = 2), measured with independent FMA chains over the whole GPU. */
+int32_t xtg_measure_fp64_peak(double* flops_per_s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* XTRACK_GB300_H */

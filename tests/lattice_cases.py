@@ -1,0 +1,104 @@
+"""Small lattices that exercise every element class, model, integrator,
+slice kind and edge configuration of the push (shared by the oracle-pin
+tests and the GPU parity tests)."""
+import math
+
+import numpy as np
+
+import xtrack_gb300 as xt
+
+
+def _errs(rng, n, scale):
+    return list(rng.normal(0, scale, n + 1))
+
+
+def element_zoo(seed=3):
+    """One of every in-scope configuration, strengths small enough that a
+    millimetre beam survives one pass."""
+    rng = np.random.default_rng(seed)
+    els = []
+    names = []
+
+    def add(name, e):
+        names.append(name)
+        els.append(e)
+
+    add("m0", xt.Marker())
+    add("d_adapt", xt.Drift(length=0.7))
+    add("d_exact", xt.Drift(length=0.9, model="exact"))
+    add("mult_thin", xt.Multipole(knl=[1e-5, 2e-3, 0.05, 0.3], ksl=[-2e-6, 1e-4, 0.01],
+                                  knl_rel=_errs(rng, 6, 1e-3), ksl_rel=_errs(rng, 6, 1e-3),
+                                  main_order=1))
+    add("mult_hxl", xt.Multipole(knl=[1e-3], hxl=1e-3, length=0.4))
+    add("mult_thick", xt.Multipole(knl=[0, 1e-3, 0.02], isthick=True, length=0.5,
+                                   num_multipole_kicks=3))
+    angle = 2 * math.pi / 1104
+    for model in ("adaptive", "drift-kick-drift-expanded", "drift-kick-drift-exact",
+                  "rot-kick-rot", "mat-kick-mat", "bend-kick-bend", "rot-kick-rot-low-order",
+                  "rot-kick-rot-high-order"):
+        for integ in ("adaptive", "uniform", "teapot", "yoshida4"):
+            add(f"b.{model}.{integ}", xt.Bend(length=2.0, angle=angle, k1=1e-3,
+                                               knl_rel=_errs(rng, 10, 1e-4),
+                                               ksl_rel=_errs(rng, 10, 1e-4),
+                                               model=model, integrator=integ,
+                                               num_multipole_kicks=(0 if integ == "adaptive" else 5),
+                                               edge_entry_angle=0.01, edge_exit_angle=-0.005,
+                                               edge_entry_hgap=0.02, edge_entry_fint=0.4))
+    add("b_k0", xt.Bend(length=1.5, angle=1e-3, k0=1.2e-3, num_multipole_kicks=2))
+    add("b_noedge", xt.Bend(length=1.0, angle=2e-3, edge_entry_active=False,
+                            edge_exit_model="suppressed"))
+    for model in ("adaptive", "drift-kick-drift-expanded", "drift-kick-drift-exact",
+                  "mat-kick-mat"):
+        for integ in ("adaptive", "uniform", "teapot", "yoshida4"):
+            add(f"q.{model}.{integ}", xt.Quadrupole(length=1.1, k1=0.01, k1s=-2e-3,
+                                                    knl_rel=_errs(rng, 10, 1e-4),
+                                                    ksl_rel=_errs(rng, 10, 1e-4),
+                                                    model=model, integrator=integ,
+                                                    num_multipole_kicks=(0 if integ == "adaptive" else 4)))
+    add("q_skew", xt.Quadrupole(length=0.8, k1s=0.004, main_is_skew=True,
+                                knl_rel=[0, 0, 1e-3], ksl_rel=[0, 1e-3]))
+    add("s", xt.Sextupole(length=0.37, k2=0.1, k2s=0.01, knl_rel=_errs(rng, 8, 1e-4),
+                          num_multipole_kicks=3))
+    add("o", xt.Octupole(length=0.3, k3=2.0, k3s=0.5, num_multipole_kicks=2,
+                         integrator="teapot"))
+    add("cav", xt.Cavity(voltage=3e6, frequency=200e6, lag=175.0))
+    add("cav_h", xt.Cavity(voltage=1e6, harmonic=20, lag=10.0, phase=0.1))
+    add("cav_thick", xt.Cavity(voltage=2e6, frequency=400e6, lag=170.0, length=0.5,
+                               num_kicks=3))
+    add("cav_abs", xt.Cavity(voltage=1e6, frequency=100e6, lag=180.0, absolute_time=1))
+    add("ell", xt.LimitEllipse(a=0.03, b=0.02))
+    add("rect", xt.LimitRect(min_x=-0.03, max_x=0.028, min_y=-0.02, max_y=0.021))
+    return xt.Line(elements=els, element_names=names)
+
+
+def sliced_line(thin=True):
+    """A short ring of thick magnets sliced thin (Teapot) or thick (Uniform)."""
+    angle = 0.01
+    els = [xt.Drift(length=1.0),
+           xt.Bend(length=3.0, angle=angle, k1=2e-3, knl_rel=[0, 1e-4, 1e-3], ksl_rel=[0, 0, 1e-4],
+                   edge_entry_angle=0.002, edge_exit_angle=0.001),
+           xt.Drift(length=0.5),
+           xt.Quadrupole(length=1.0, k1=0.02, knl_rel=[1e-4, 0, 0, 1e-3]),
+           xt.Drift(length=0.5),
+           xt.Sextupole(length=0.4, k2=0.2),
+           xt.Octupole(length=0.3, k3=1.0),
+           xt.Multipole(knl=[0, 5e-3, 0.02], isthick=True, length=0.6),
+           xt.Cavity(voltage=1e6, frequency=400e6, lag=180.0, length=0.4),
+           xt.Drift(length=2.0)]
+    names = ["d0", "mb", "d1", "mq", "d2", "ms", "mo", "mm", "cav", "d3"]
+    line = xt.Line(elements=els, element_names=names)
+    if thin:
+        line.slice_thick_elements([xt.Strategy(slicing=xt.Teapot(4)),
+                                   xt.Strategy(slicing=xt.Uniform(3), element_type=xt.Bend),
+                                   xt.Strategy(slicing=xt.Teapot(2), name="d3")])
+    else:
+        line.slice_thick_elements([xt.Strategy(slicing=xt.Uniform(3, mode="thick")),
+                                   xt.Strategy(slicing=xt.Teapot(2, mode="thick"), element_type=xt.Bend)])
+    return line
+
+
+def small_beam(n, p0c=7e12, seed=0, scale=1.0):
+    rng = np.random.default_rng(seed)
+    return dict(p0c=p0c, x=rng.normal(0, 1e-3 * scale, n), px=rng.normal(0, 1e-5 * scale, n),
+                y=rng.normal(0, 1e-3 * scale, n), py=rng.normal(0, 1e-5 * scale, n),
+                zeta=rng.normal(0, 0.05 * scale, n), delta=rng.normal(0, 1e-4 * scale, n))

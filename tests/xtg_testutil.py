@@ -1,0 +1,107 @@
+"""Helpers shared by the tests: run the same track_line call on the GPU
+(through the C-ABI) and on the CPU oracle, and compare the results."""
+import ctypes
+
+import numpy as np
+
+import pyoracle
+from xtrack_gb300 import _abi
+
+COORDS = ("x", "px", "y", "py", "zeta", "delta", "ptau", "rpp", "rvv", "s")
+INTS = ("state", "at_turn", "at_element", "particle_id")
+
+
+def beam_arrays(particles):
+    return pyoracle.host_arrays(particles.to_numpy())
+
+
+def gpu_track(records, arrs, arith="exact", q0=1.0, mass0=938272088.16, t_sim=0.0,
+              num_turns=1, ele_start=0, num_ele_track=None, flag_end_turn_actions=1,
+              flag_reset_s=1, line_length=0.0, track_flags=0, use_exact_drifts=False,
+              cavity_preserve_angle=False, global_xy_limit=1.0, monitor=None,
+              flag_monitor=0, num_ele_line=None, compact_every=0, block_size=0):
+    """One xtg_track call on cuda:0 over copies of the host arrays ``arrs``.
+    Returns (arrays, monitor_data) as numpy."""
+    import torch
+    lib = _abi.load_library()
+    n = len(records)
+    if num_ele_track is None:
+        num_ele_track = n - ele_start
+    if num_ele_line is None:
+        num_ele_line = n
+    dev = torch.device("cuda:0")
+    t = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in arrs.items()}
+    ps = _abi.particles_struct_from_ptrs(len(arrs["x"]), q0, mass0, t_sim,
+                                         {k: v.data_ptr() for k, v in t.items()})
+    cfg = _abi.XtgConfig()
+    cfg.use_exact_drifts = int(bool(use_exact_drifts))
+    cfg.cavity_preserve_angle = int(bool(cavity_preserve_angle))
+    cfg.has_global_xy_limit = 0 if global_xy_limit is None else 1
+    cfg.global_xy_limit = 0.0 if global_xy_limit is None else float(global_xy_limit)
+    cfg.arith = _abi.ARITH_EXACT if arith == "exact" else _abi.ARITH_FAST
+    h = ctypes.c_void_p()
+    recs = np.ascontiguousarray(records)
+    _abi.check(lib.xtg_lattice_create(recs.ctypes.data_as(ctypes.c_void_p), n, ctypes.byref(cfg),
+                                      ctypes.byref(h)))
+    try:
+        if compact_every or block_size:
+            _abi.check(lib.xtg_set_launch_config(h, block_size, compact_every, None, None))
+        mst = None
+        mdata = None
+        if monitor is not None:
+            mdata = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev)
+                     for k, v in monitor["data"].items()}
+            mst = _abi.XtgMonitor()
+            for k in ("start_at_turn", "stop_at_turn", "part_id_start", "part_id_end",
+                      "ebe_mode", "n_repetitions", "repetition_period", "n_records"):
+                setattr(mst, k, int(monitor[k]))
+            mst.data = _abi.particles_struct_from_ptrs(monitor["n_records"], 0., 0., 0.,
+                                                       {k: v.data_ptr() for k, v in mdata.items()})
+        _abi.check(lib.xtg_track(h, ctypes.byref(ps), num_turns, ele_start, num_ele_track,
+                                 flag_end_turn_actions, flag_reset_s, flag_monitor, num_ele_line,
+                                 line_length, ctypes.byref(mst) if mst is not None else None,
+                                 int(track_flags), None))
+        _abi.check(lib.xtg_sync(None))
+    finally:
+        lib.xtg_lattice_destroy(h)
+    out = {k: v.cpu().numpy() for k, v in t.items()}
+    mon = {k: v.cpu().numpy() for k, v in mdata.items()} if mdata is not None else None
+    return out, mon
+
+
+def make_monitor(start, stop, pid_range, fields=("x", "px", "y", "py", "zeta", "delta", "s",
+                                                 "at_turn", "at_element", "state", "particle_id"),
+                 n_repetitions=1, repetition_period=-1, ebe_mode=0):
+    n_rec = (stop - start) * (pid_range[1] - pid_range[0]) * n_repetitions
+    data = {}
+    for f in fields:
+        dt = np.int64 if f in pyoracle.INT_FIELDS else np.float64
+        data[f] = np.zeros(n_rec, dtype=dt)
+    return dict(start_at_turn=start, stop_at_turn=stop, part_id_start=pid_range[0],
+                part_id_end=pid_range[1], ebe_mode=ebe_mode, n_repetitions=n_repetitions,
+                repetition_period=repetition_period, n_records=n_rec, data=data)
+
+
+def rel_err(a, b, field):
+    """max |a-b| / max(|b|) over the array (scale-relative error)."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    scale = np.max(np.abs(b)) if b.size else 1.0
+    if scale == 0:
+        scale = 1.0
+    return float(np.max(np.abs(a - b)) / scale) if b.size else 0.0
+
+
+def compare(got, ref, coord_tol, fields=COORDS, mask=None):
+    """Asserts integer fields bit-exact and coordinates within coord_tol
+    (scale-relative). Returns {field: (rel_err, n_bitexact)}."""
+    report = {}
+    sel = slice(None) if mask is None else mask
+    for f in INTS:
+        if f in ref:
+            assert np.array_equal(got[f][sel], ref[f][sel]), f"{f} differs"
+    for f in fields:
+        e = rel_err(got[f][sel], ref[f][sel], f)
+        report[f] = (e, int(np.sum(got[f][sel] == ref[f][sel])))
+        assert e <= coord_tol, f"{f}: relative error {e:.3e} > {coord_tol:.1e}"
+    return report

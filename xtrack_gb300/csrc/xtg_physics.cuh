@@ -1,0 +1,592 @@
+// Device-side element physics of the push, one particle per thread.
+//
+// Two arithmetic modes share this file (template parameter kExact):
+//   kExact = true : the reference's operation order. The translation unit is
+//                   compiled with -fmad=false so no product is fused into an
+//                   addition; with the per-element constants precomputed by
+//                   the host packer in the same order, results equal the
+//                   reference's CPU results bit for bit (libm aside).
+//   kExact = false: the minimal formulation — one merged complex Horner
+//                   polynomial per kick and explicit fma() — for throughput.
+// Citations are to xtrack/beam_elements/elements_src/ unless noted.
+#pragma once
+#include <stdint.h>
+
+#include "xtg_table.h"
+
+namespace xtg {
+
+#define XTG_DEV __device__ __forceinline__
+// Element maps that the common lattices do not use per kick are kept out of
+// line so that they cost no registers in the hot loop.
+#define XTG_COLD __device__ __noinline__
+
+constexpr double kCLightD = 299792458.0;
+constexpr double kPiD = 3.1415926535897932384626433832795028841971693993751;
+
+// Register-resident state of one particle (the LocalParticle of the
+// reference, particles.py:96-112, restricted to what the push changes or
+// reads). rv0v = 1/rvv and opd = 1 + delta are cached: the reference
+// recomputes them in every drift and kick with the same IEEE operations, so
+// caching them does not change any result.
+struct PState {
+    double x, px, y, py, zeta, delta, ptau, rpp, rvv, s;
+    double rv0v, opd;
+    double chi, charge_ratio, beta0, p0c;
+    double ax, ay;
+    int64_t state, at_element, at_turn;
+};
+
+XTG_DEV void refresh_energy_cache(PState& p) {
+    p.rv0v = 1. / p.rvv;
+    p.opd = 1. + p.delta;
+}
+
+// ---------------------------------------------------------------------------
+// Drifts
+// ---------------------------------------------------------------------------
+
+// track_drift.h:10-23
+template <bool kExact>
+XTG_DEV void drift_expanded(PState& p, double length) {
+    if (kExact) {
+        double const xp = p.px * p.rpp;
+        double const yp = p.py * p.rpp;
+        double const dzeta = 1 - p.rv0v * (1. + (xp * xp + yp * yp) * 0.5);
+        p.x = p.x + xp * length;
+        p.y = p.y + yp * length;
+        p.s = p.s + length;
+        p.zeta = p.zeta + length * dzeta;
+    } else {
+        double const xp = p.px * p.rpp;
+        double const yp = p.py * p.rpp;
+        double const t = fma(xp, xp, yp * yp);
+        double const dzeta = fma(-p.rv0v, fma(t, 0.5, 1.0), 1.0);
+        p.x = fma(xp, length, p.x);
+        p.y = fma(yp, length, p.y);
+        p.s = p.s + length;
+        p.zeta = fma(length, dzeta, p.zeta);
+    }
+}
+
+// track_drift.h:26-42
+template <bool kExact>
+XTG_DEV void drift_exact(PState& p, double length) {
+    double const px = p.px, py = p.py;
+    double const opd = p.opd;
+    if (kExact) {
+        double const one_over_pz = 1. / sqrt(opd * opd - px * px - py * py);
+        double const dzeta = 1 - p.rv0v * opd * one_over_pz;
+        p.x = p.x + px * one_over_pz * length;
+        p.y = p.y + py * one_over_pz * length;
+        p.zeta = p.zeta + dzeta * length;
+        p.s = p.s + length;
+    } else {
+        double const pz2 = fma(-py, py, fma(-px, px, opd * opd));
+        double const one_over_pz = 1. / sqrt(pz2);
+        double const dzeta = fma(-p.rv0v * opd, one_over_pz, 1.0);
+        double const fl = one_over_pz * length;
+        p.x = fma(px, fl, p.x);
+        p.y = fma(py, fl, p.y);
+        p.zeta = fma(dzeta, length, p.zeta);
+        p.s = p.s + length;
+    }
+}
+
+// track_magnet_drift.h:44-87
+XTG_DEV void drift_polar(PState& p, double length, double h) {
+    double const x = p.x, y = p.y, px = p.px, py = p.py;
+    double const s = length;
+    double const opd = p.delta + 1.0;
+    double const pz = sqrt((opd) * (opd) - (px) * (px) - (py) * (py));
+    double const rho = 1 / h;
+    double const ca = cos(h * s);
+    double const sa = sin(h * s);
+    double const sa2 = sin(0.5 * h * s);
+    double const _pz = 1 / pz;
+    double const pxt = px * _pz;
+    double const _ptt = 1 / (ca - sa * pxt);
+    double const pst = (x + rho) * sa * _pz * _ptt;
+    double const new_x = (x + rho * (2 * sa2 * sa2 + sa * pxt)) * _ptt;
+    double const new_px = ca * px + sa * pz;
+    double const new_y = y + pst * py;
+    double const delta_ell = opd * (x + rho) * sa / ca / pz / (1 - px * sa / ca / pz);
+    p.x = new_x;
+    p.px = new_px;
+    p.y = new_y;
+    p.zeta = p.zeta + (length - delta_ell / p.rvv);
+    p.s = p.s + s;
+}
+
+// track_magnet_drift.h:90-213
+XTG_DEV void drift_cf_expanded(PState& p, double length, double k0_, double k1_, double h) {
+    double const x = p.x, y = p.y, px = p.px, py = p.py;
+    double const dp1 = p.delta + 1;
+    double const chi = p.chi;
+    double const k0 = chi * k0_ / dp1;
+    double const k1 = chi * k1_ / dp1;
+    double const Kx = k0 * h + k1;
+    double const Ky = -k1;
+    double Sx, Sy, Cx, Cy;
+    if (Kx > 0.0) {
+        double sq = sqrt(Kx);
+        Sx = sin(sq * length) / sq;
+        Cx = cos(sq * length);
+    } else if (Kx < 0.0) {
+        double sq = sqrt(-Kx);
+        Sx = sinh(sq * length) / sq;
+        Cx = cosh(sq * length);
+    } else {
+        Sx = length;
+        Cx = 1.0;
+    }
+    if (Ky > 0.0) {
+        double sq = sqrt(Ky);
+        Sy = sin(sq * length) / sq;
+        Cy = cos(sq * length);
+    } else if (Ky < 0.0) {
+        double sq = sqrt(-Ky);
+        Sy = sinh(sq * length) / sq;
+        Cy = cosh(sq * length);
+    } else {
+        Sy = length;
+        Cy = 1.0;
+    }
+    double const xp = px / dp1;
+    double const yp = py / dp1;
+    double const A = -Kx * x - k0 + h;
+    double const B = xp;
+    double const C = -Ky * y;
+    double const D = yp;
+    double x_ = x * Cx + xp * Sx;
+    double const y_ = y * Cy + yp * Sy;
+    double const px_ = (A * Sx + B * Cx) * dp1;
+    double const py_ = (C * Sy + D * Cy) * dp1;
+    if (Kx != 0.0) x_ = x_ + (k0 - h) * (Cx - 1.0) / Kx;
+    else x_ = x_ - (k0 - h) * 0.5 * ((length) * (length));
+    double length_ = length;
+    if (Kx != 0.0) {
+        length_ -= (h * ((Cx - 1.0) * xp + Sx * A + length * (k0 - h))) / Kx;
+        length_ += 0.5 * (-(((A) * (A)) * Cx * Sx) / (2.0 * Kx) + (((B) * (B)) * Cx * Sx) / 2.0 +
+                          (((A) * (A)) * length) / (2.0 * Kx) + (((B) * (B)) * length) / 2.0 -
+                          (A * B * ((Cx) * (Cx))) / Kx + (A * B) / Kx);
+    } else {
+        length_ += h * length * (3.0 * length * xp + 6.0 * x - (k0 - h) * ((length) * (length))) / 6.0;
+        length_ += 0.5 * (((B) * (B))) * length;
+    }
+    if (Ky != 0.0) {
+        length_ += 0.5 * (-(((C) * (C)) * Cy * Sy) / (2.0 * Ky) + (((D) * (D)) * Cy * Sy) / 2.0 +
+                          (((C) * (C)) * length) / (2.0 * Ky) + (((D) * (D)) * length) / 2.0 -
+                          (C * D * ((Cy) * (Cy))) / Ky + (C * D) / Ky);
+    } else {
+        length_ += 0.5 * ((D) * (D)) * length;
+    }
+    double const dzeta = length - length_ / p.rvv;
+    p.x = x_;
+    p.px = px_;
+    p.y = y_;
+    p.py = py_;
+    p.zeta = p.zeta + dzeta;
+    p.s = p.s + length;
+}
+
+// track_magnet_drift.h:348-393
+XTG_DEV void drift_straight_exact_bend(PState& p, double length, double k0) {
+    double const k0_chi = k0 * p.chi;
+    if (fabs(k0_chi) < 1e-8) {
+        drift_exact<true>(p, length);
+        return;
+    }
+    double const x = p.x, y = p.y, px = p.px, py = p.py;
+    double const s = length;
+    double const opd = p.delta + 1.0;
+    double const A = 1.0 / sqrt((opd) * (opd) - (py) * (py));
+    double const pz = sqrt((opd) * (opd) - (px) * (px) - (py) * (py));
+    double const new_px = px - k0_chi * s;
+    double const new_x = x + (sqrt((opd) * (opd) - (new_px) * (new_px) - (py) * (py)) - pz) / k0_chi;
+    double const D = asin(A * px) - asin(A * new_px);
+    double const new_y = y + (py / k0_chi) * D;
+    double const delta_ell = (opd / k0_chi) * D;
+    p.x = new_x;
+    p.px = new_px;
+    p.y = new_y;
+    p.zeta = p.zeta + (length - delta_ell / p.rvv);
+    p.s = p.s + s;
+}
+
+// track_magnet_drift.h:271-345
+XTG_DEV void drift_curved_exact_bend(PState& p, double length, double k0, double h) {
+    double const k0_chi = k0 * p.chi;
+    if (fabs(k0_chi) < 1e-8) {
+        drift_polar(p, length, h);
+        return;
+    }
+    double const x0 = p.x, y0 = p.y, px0 = p.px, py = p.py;
+    double const s = length;
+    double const opd = p.delta + 1.0;
+    double const hs = h * s;
+    double const sin_hs = sin(hs);
+    double const cos_hs = cos(hs);
+    double const sin_hs_2 = sin(hs / 2);
+    double const pz0 = sqrt((opd) * (opd) - (px0) * (px0) - (py) * (py));
+    double const C = pz0 - k0_chi * ((1.0 / h) + x0);
+    double const pxs = px0 * cos_hs + C * sin_hs;
+    double const pzs = sqrt((opd) * (opd) - (pxs) * (pxs) - (py) * (py));
+    double const delta_pz = (px0 - pxs) * (px0 + pxs) / (pz0 + pzs);
+    double const delta_D = -2 * C * ((sin_hs_2) * (sin_hs_2)) - px0 * sin_hs;
+    double const delta_x = (delta_pz - delta_D) / k0_chi;
+    double const delta_px = -2 * px0 * ((sin_hs_2) * (sin_hs_2)) + C * sin_hs;
+    double const N_a = px0 * delta_pz - pz0 * delta_px;
+    double const D_a = pz0 * pzs + px0 * pxs;
+    double const delta_a = atan2(N_a, D_a);
+    double const integ = (hs + delta_a) / k0_chi;
+    double const new_y = y0 + py * integ;
+    double const delta_ell = opd * integ;
+    p.x = p.x + delta_x;
+    p.px = pxs;
+    p.y = new_y;
+    p.zeta = p.zeta + (length - delta_ell / p.rvv);
+    p.s = p.s + s;
+}
+
+XTG_COLD PState magnet_drift_curved(PState p, double length, int drift_model, double k0, double k1,
+                                    double h);
+
+// track_magnet_drift.h:469-555 (model 6, solenoid, is rejected on the host)
+template <bool kExact>
+XTG_DEV void magnet_drift(PState& p, double length, int drift_model, double k0, double k1,
+                          double h) {
+    if (drift_model == -1) return;
+    if (length == 0.0) return;
+    if (drift_model == 0) {
+        drift_expanded<kExact>(p, length);
+        return;
+    }
+    if (drift_model == 1) {
+        drift_exact<kExact>(p, length);
+        return;
+    }
+    p = magnet_drift_curved(p, length, drift_model, k0, k1, h);
+}
+
+// Drift models 2-8 of track_magnet_drift.h:469-555. Out of line and by
+// value, so that the caller's particle state stays in registers.
+XTG_COLD PState magnet_drift_curved(PState p, double length, int drift_model, double k0, double k1,
+                                    double h) {
+    switch (drift_model) {
+    case 2: drift_polar(p, length, h); break;
+    case 3: drift_cf_expanded(p, length, k0, k1, h); break;
+    case 4: drift_curved_exact_bend(p, length, k0, h); break;
+    case 5: drift_straight_exact_bend(p, length, k0); break;
+    case 7:
+        drift_polar(p, 0.6756035959798289 * length, h);
+        p.px = p.px - 1.3512071919596578 * k0 * p.chi * length;
+        drift_polar(p, -0.17560359597982889 * length, h);
+        p.px = p.px - (-1.7024143839193155) * k0 * p.chi * length;
+        drift_polar(p, -0.17560359597982889 * length, h);
+        p.px = p.px - 1.3512071919596578 * k0 * p.chi * length;
+        drift_polar(p, 0.6756035959798289 * length, h);
+        break;
+    case 8:
+        drift_polar(p, 3.922568052387799819591407413100e-01 * length, h);
+        p.px = p.px - 7.845136104775599639182814826199e-01 * k0 * p.chi * length;
+        drift_polar(p, 5.100434119184584780271052295575e-01 * length, h);
+        p.px = p.px - 2.355732133593569921359289764951e-01 * k0 * p.chi * length;
+        drift_polar(p, -4.710533854097565531482416645304e-01 * length, h);
+        p.px = p.px - (-1.177679984178870098432412305556e+00) * k0 * p.chi * length;
+        drift_polar(p, 6.875316825251809316199569366290e-02 * length, h);
+        p.px = p.px - 1.315186320683906284756403692882e+00 * k0 * p.chi * length;
+        drift_polar(p, 6.875316825251809316199569366290e-02 * length, h);
+        p.px = p.px - (-1.177679984178870098432412305556e+00) * k0 * p.chi * length;
+        drift_polar(p, -4.710533854097565531482416645304e-01 * length, h);
+        p.px = p.px - 2.355732133593569921359289764951e-01 * k0 * p.chi * length;
+        drift_polar(p, 5.100434119184584780271052295575e-01 * length, h);
+        p.px = p.px - 7.845136104775599639182814826199e-01 * k0 * p.chi * length;
+        drift_polar(p, 3.922568052387799819591407413100e-01 * length, h);
+        break;
+    default: break;
+    }
+    return p;
+}
+
+// ---------------------------------------------------------------------------
+// Kicks
+// ---------------------------------------------------------------------------
+
+// One kick_simple pass in the reference arithmetic (track_magnet_kick.h:
+// 182-260). `co` holds quintuples (A, B, knl, ksl, invf) from `top` down.
+XTG_DEV void exact_pass(PState& p, const double* __restrict__ co, int top, double factor,
+                        double kick_weight, double x, double y) {
+    double dpx_mul, dpy_mul;
+    if (p.chi == 1.0) {
+        dpx_mul = co[0];
+        dpy_mul = co[1];
+        for (int i = top; i > 0; i--) {
+            co += 5;
+            double const zre = dpx_mul * x - dpy_mul * y;
+            double const zim = dpx_mul * y + dpy_mul * x;
+            dpx_mul = co[0] + zre;
+            dpy_mul = co[1] + zim;
+        }
+    } else {
+        double const chi = p.chi;
+        dpx_mul = chi * co[2] * factor * co[4];
+        dpy_mul = chi * co[3] * factor * co[4];
+        for (int i = top; i > 0; i--) {
+            co += 5;
+            double const zre = dpx_mul * x - dpy_mul * y;
+            double const zim = dpx_mul * y + dpy_mul * x;
+            double const this_knl = chi * co[2] * factor;
+            double const this_ksl = chi * co[3] * factor;
+            dpx_mul = this_knl * co[4] + zre;
+            dpy_mul = this_ksl * co[4] + zim;
+        }
+    }
+    dpx_mul = -dpx_mul;
+    p.px = p.px + kick_weight * dpx_mul;
+    p.py = p.py + kick_weight * dpy_mul;
+}
+
+// track_magnet_kick.h:23-144 for kick-weight slot k of a magnet record.
+template <bool kExact>
+XTG_DEV void magnet_kick(PState& p, const MagnetRec& r, const double* __restrict__ coefs, int k) {
+    double const x = p.x, y = p.y;
+    if (kExact) {
+        double const kw = r.kw[k];
+#pragma unroll 1
+        for (int q = 0; q < 3; q++) {
+            if (r.pass[q].top >= 0)
+                exact_pass(p, coefs + r.pass[q].coef, r.pass[q].top, r.pass[q].factor, kw, x, y);
+        }
+        int const curv = r.curv_terms;
+        if (curv) {
+            double dpx = 0.0, dpy = 0.0, dzeta = 0.0;
+            double const chi = p.chi;
+            double C0, C1;
+            if (chi == 1.0) {
+                C0 = r.C0[k];
+                C1 = r.C1[k];
+            } else {
+                C0 = -chi * r.Q0 * kw * r.htot;
+                C1 = r.htot * chi * r.Q1 * kw;
+            }
+            if (curv & 1) {
+                double const hl = r.hl[k];
+                dpx = dpx + hl * p.opd;
+                dzeta = dzeta + -p.rv0v * hl * x;
+            }
+            if (curv & 2) dpx = dpx + C0 * x;
+            if (curv & 4) {
+                dpx = dpx + C1 * (-x * x + 0.5 * y * y);
+                dpy = dpy + C1 * x * y;
+            }
+            p.px = p.px + dpx;
+            p.py = p.py + dpy;
+            p.zeta = p.zeta + dzeta;
+        }
+    } else {
+        // merged polynomial sum_i (cn_i + i cs_i) z^i, z = x + i y
+        double pr = 0.0, pi = 0.0;
+        int const top = r.fast_top;
+        if (top >= 0) {
+            const double* __restrict__ c = coefs + r.fast_coef;
+            pr = c[0];
+            pi = c[1];
+            for (int i = top; i > 0; i--) {
+                c += 2;
+                double const nr = fma(pr, x, fma(-pi, y, c[0]));
+                double const ni = fma(pr, y, fma(pi, x, c[1]));
+                pr = nr;
+                pi = ni;
+            }
+        }
+        double const cs = p.chi * r.fast_scale[k];
+        double dpx = -cs * pr;
+        double dpy = cs * pi;
+        int const curv = r.curv_terms;
+        if (curv) {
+            double const chi = p.chi;
+            if (curv & 1) {
+                double const hl = r.hl[k];
+                dpx = fma(hl, p.opd, dpx);
+                p.zeta = fma(-p.rv0v * hl, x, p.zeta);
+            }
+            if (curv & 2) dpx = fma(chi * r.C0[k], x, dpx);
+            if (curv & 4) {
+                double const c1 = chi * r.C1[k];
+                dpx = fma(c1, fma(-x, x, 0.5 * y * y), dpx);
+                dpy = fma(c1 * x, y, dpy);
+            }
+        }
+        p.px = p.px + dpx;
+        p.py = p.py + dpy;
+    }
+}
+
+// track_magnet_edge.h:16-80 with the linear model (track_dipole_edge_linear.h)
+XTG_DEV void magnet_edge(PState& p, int kind, bool is_exit, double r21, double r43) {
+    if (kind == EDGE_NONE) return;
+    if (is_exit) {
+        p.ax = 0.;
+        p.ay = 0.;
+    } else {
+        p.ax = (-0.5 * 0.0) * (p.y - 0.);
+        p.ay = (0.5 * 0.0) * (p.x - 0.);
+    }
+    if (kind == EDGE_LINEAR) {
+        double const x = p.x, y = p.y, chi = p.chi;
+        p.px = p.px + chi * r21 * x;
+        p.py = p.py + chi * r43 * y;
+    }
+}
+
+// track_magnet.h:25-285 (body) after the host-side resolution.
+template <bool kExact>
+XTG_DEV void magnet_body(PState& p, const MagnetRec& r, const double* __restrict__ coefs) {
+    int const dm = r.drift_model;
+    double const k0d = r.k0_drift, k1d = r.k1_drift, hd = r.h_drift;
+    if (r.only_drift) {
+        magnet_drift<kExact>(p, r.length, dm, k0d, k1d, hd);
+        return;
+    }
+    int const n = r.n_kicks;
+    if (r.integrator == INT_UNIFORM) {
+        if (kExact || (dm != 0 && dm != 1)) {
+            for (int i = 0; i < n; i++) {
+                magnet_drift<kExact>(p, r.d_edge, dm, k0d, k1d, hd);
+                magnet_kick<kExact>(p, r, coefs, 0);
+                magnet_drift<kExact>(p, r.d_edge, dm, k0d, k1d, hd);
+            }
+        } else {
+            // adjacent half drifts of straight drift maps compose exactly
+            magnet_drift<false>(p, r.d_edge, dm, 0, 0, 0);
+            for (int i = 0; i < n - 1; i++) {
+                magnet_kick<false>(p, r, coefs, 0);
+                magnet_drift<false>(p, r.d_fast_inside, dm, 0, 0, 0);
+            }
+            magnet_kick<false>(p, r, coefs, 0);
+            magnet_drift<false>(p, r.d_edge, dm, 0, 0, 0);
+        }
+    } else if (r.integrator == INT_TEAPOT) {
+        magnet_drift<kExact>(p, r.d_edge, dm, k0d, k1d, hd);
+        for (int i = 0; i < n - 1; i++) {
+            magnet_kick<kExact>(p, r, coefs, 0);
+            magnet_drift<kExact>(p, r.d_inside, dm, k0d, k1d, hd);
+        }
+        magnet_kick<kExact>(p, r, coefs, 0);
+        magnet_drift<kExact>(p, r.d_edge, dm, k0d, k1d, hd);
+    } else if (r.integrator == INT_YOSHIDA4) {
+        for (int s = 0; s < n; s++) {
+            magnet_drift<kExact>(p, r.d_yoshida[0], dm, k0d, k1d, hd);
+            magnet_kick<kExact>(p, r, coefs, 0);
+            magnet_drift<kExact>(p, r.d_yoshida[1], dm, k0d, k1d, hd);
+            magnet_kick<kExact>(p, r, coefs, 1);
+            magnet_drift<kExact>(p, r.d_yoshida[2], dm, k0d, k1d, hd);
+            magnet_kick<kExact>(p, r, coefs, 2);
+            magnet_drift<kExact>(p, r.d_yoshida[3], dm, k0d, k1d, hd);
+            magnet_kick<kExact>(p, r, coefs, 3);
+            magnet_drift<kExact>(p, r.d_yoshida[3], dm, k0d, k1d, hd);
+            magnet_kick<kExact>(p, r, coefs, 2);
+            magnet_drift<kExact>(p, r.d_yoshida[2], dm, k0d, k1d, hd);
+            magnet_kick<kExact>(p, r, coefs, 1);
+            magnet_drift<kExact>(p, r.d_yoshida[1], dm, k0d, k1d, hd);
+            magnet_kick<kExact>(p, r, coefs, 0);
+            magnet_drift<kExact>(p, r.d_yoshida[0], dm, k0d, k1d, hd);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// RF
+// ---------------------------------------------------------------------------
+
+// local_particle_custom_api.h:20-33, 195-217
+XTG_DEV void add_to_energy(PState& p, double delta_energy, bool pz_only) {
+    double ptau = p.ptau;
+    double const mass_ratio = p.charge_ratio / p.chi;
+    ptau = ptau + delta_energy / p.p0c / mass_ratio;
+    double const old_rpp = p.rpp;
+    double const beta0 = p.beta0;
+    double const irpp = sqrt(ptau * ptau + 2 * ptau / beta0 + 1);
+    double const new_rpp = 1. / irpp;
+    double const new_rvv = irpp / (1 + beta0 * ptau);
+    p.delta = irpp - 1;
+    p.rvv = new_rvv;
+    p.ptau = ptau;
+    p.rpp = new_rpp;
+    if (!pz_only) {
+        double const f = old_rpp / new_rpp;
+        p.px = p.px * f;
+        p.py = p.py * f;
+    }
+    refresh_energy_cache(p);
+}
+
+struct RfCtx {
+    double q0, t_sim, line_length;
+    bool kill, preserve_angle;
+};
+
+// track_rf.h:17-167 (order = -1, no transverse voltage)
+XTG_DEV void rf_kick(PState& p, const CavityRec& r, double voltage, const RfCtx& c) {
+    double arg;
+    double const tau = p.zeta / p.beta0;
+    if (r.harmonic == 0.0 && r.absolute_time != 1) {
+        arg = r.phi_const - r.w_freq * tau;
+    } else {
+        double phase0 = 0;
+        double frequency = r.frequency;
+        if (r.harmonic != 0) {
+            double const t_rev0 = c.line_length / (p.beta0 * kCLightD);
+            frequency = frequency + (r.harmonic / t_rev0);
+        }
+        if (r.absolute_time == 1) {
+            phase0 = phase0 + 2 * kPiD * (double)p.at_turn * frequency * c.t_sim;
+        }
+        arg = phase0 + r.lag_rad + r.phase - (2.0 * kPiD) / kCLightD * frequency * tau;
+    }
+    double const q = fabs(c.q0) * p.charge_ratio;
+    double const energy_kick = q * voltage * sin(arg);
+    if (!c.kill) add_to_energy(p, energy_kick + 0.0, !c.preserve_angle);
+}
+
+// track_rf.h:170-290
+template <bool kExact>
+XTG_DEV void cavity(PState& p, const CavityRec& r, const RfCtx& c) {
+    int const dm = r.drift_model;
+    int const n = r.n_kicks;
+    if (r.integrator == INT_UNIFORM) {
+        for (int i = 0; i < n; i++) {
+            magnet_drift<kExact>(p, r.d_edge, dm, 0., 0., 0.);
+            rf_kick(p, r, r.voltage * r.kw[0], c);
+            magnet_drift<kExact>(p, r.d_edge, dm, 0., 0., 0.);
+        }
+    } else if (r.integrator == INT_TEAPOT) {
+        magnet_drift<kExact>(p, r.d_edge, dm, 0., 0., 0.);
+        for (int i = 0; i < n - 1; i++) {
+            rf_kick(p, r, r.voltage * r.kw[0], c);
+            magnet_drift<kExact>(p, r.d_inside, dm, 0., 0., 0.);
+        }
+        rf_kick(p, r, r.voltage * r.kw[0], c);
+        magnet_drift<kExact>(p, r.d_edge, dm, 0., 0., 0.);
+    } else if (r.integrator == INT_YOSHIDA4) {
+        for (int s = 0; s < n; s++) {
+            magnet_drift<kExact>(p, r.d_yoshida[0], dm, 0., 0., 0.);
+            for (int j = 0; j < 7; j++) {
+                int const kj = (j <= 3) ? j : 6 - j;
+                rf_kick(p, r, r.voltage * r.kw[kj], c);
+                int const dj = (j < 3) ? j + 1 : (j == 3 ? 3 : 6 - j);
+                magnet_drift<kExact>(p, r.d_yoshida[dj], dm, 0., 0., 0.);
+            }
+        }
+    }
+}
+
+// Out-of-line entry for the hot loop (one cavity per turn in most rings).
+template <bool kExact>
+XTG_COLD PState cavity_cold(PState p, const CavityRec& r, const RfCtx c) {
+    cavity<kExact>(p, r, c);
+    return p;
+}
+
+}  // namespace xtg

@@ -1,0 +1,137 @@
+// Packed element-parameter table: the device-side form of a lattice.
+//
+// The reference hands its kernel a table of references to per-class element
+// structs (ElementRefData, xtrack/tracker.py:1771-1792) and resolves each
+// magnet's model, integrator, number of kicks and strength splits per
+// particle at run time (xtrack/beam_elements/elements_src/track_magnet.h:
+// 518-574). Here all of that is resolved once on the host: each element
+// becomes one variable-length record of plain doubles/ints that the kernel
+// walks sequentially. Records are 16-byte aligned so a chunk of consecutive
+// records can be copied into shared memory with one bulk copy.
+//
+// Shared by the host packer (xtg_lattice.cpp) and the kernels (xtg_track.cu).
+#pragma once
+#include <stdint.h>
+
+namespace xtg {
+
+enum Op : int32_t {
+    OP_NOP = 0,           // Marker, suppressed edges, zero-effect elements
+    OP_DRIFT = 1,         // Drift / DriftSlice*
+    OP_MAGNET = 2,        // Multipole, Bend, Quadrupole, Sextupole, Octupole
+                          // and their thick/thin/entry/exit slices
+    OP_CAVITY = 3,        // Cavity and its slices
+    OP_LIMIT_ELLIPSE = 4,
+    OP_LIMIT_RECT = 5,
+};
+
+// RecHeader.flags
+enum : int32_t {
+    F_GLOBAL_APER = 1,    // statically thick class: global aperture follows
+};
+
+struct alignas(16) RecHeader {
+    int32_t op;
+    int32_t flags;
+    int32_t nbytes;       // size of the whole record, multiple of 16
+    int32_t reserved;
+};
+
+struct alignas(16) DriftRec {
+    RecHeader h;
+    double length;        // signed (negated for backtracking tables)
+    int32_t exact;        // 1: exact drift map, 0: expanded
+    int32_t reserved;
+};
+
+struct alignas(16) LimitEllipseRec {
+    RecHeader h;
+    double a_squ, b_squ, a_b_squ, reserved;
+};
+
+struct alignas(16) LimitRectRec {
+    RecHeader h;
+    double min_x, max_x, min_y, max_y;
+};
+
+// Integrators (reference numbering, _common.py:40-47)
+enum : int32_t { INT_TEAPOT = 1, INT_YOSHIDA4 = 2, INT_UNIFORM = 3 };
+
+// One kick_simple_single_coordinates pass in the reference's arithmetic
+// (track_magnet_kick.h:182-228). Coefficients live in the record's
+// coefficient area at `coef` doubles from its start, highest order first:
+// for each order i = top..0 the quintuple
+//   A_i = round(round(knl_i*factor)*invf_i)   (value of chi*knl_i*factor*invf_i at chi = 1)
+//   B_i = same with ksl_i
+//   knl_i, ksl_i, invf_i                        (for particles with chi != 1)
+// `top` is the highest order with a non-zero coefficient (-1: skip pass).
+struct ExactPass {
+    int32_t top;
+    int32_t coef;
+    double factor;
+};
+
+enum : int32_t { EDGE_NONE = 0, EDGE_AXAY = 1, EDGE_LINEAR = 2 };
+
+struct alignas(16) MagnetRec {
+    RecHeader h;
+    // --- structure ---
+    int32_t body_active;
+    int32_t integrator;       // INT_*
+    int32_t n_kicks;          // resolved number of kicks (>= 0)
+    int32_t drift_model;      // -1 kick only, 0 expanded, 1 exact, 2 polar,
+                              // 3 expanded combined, 4/5 exact bend, 7/8 yoshida
+    int32_t only_drift;       // body is a single drift of the full length
+    int32_t kick_rot_frame;
+    int32_t edge_entry;       // EDGE_*
+    int32_t edge_exit;
+    int32_t n_kw;             // distinct kick weights (1, or 4 for Yoshida)
+    int32_t curv_terms;       // bit0: rot-frame term, bit1: k0h term, bit2: k1h term
+    int32_t fast_top;         // merged-polynomial top order for the fast path (-1: none)
+    int32_t fast_coef;        // offset of merged coefficients (pairs cn_i, cs_i)
+    // --- drift lengths (as the reference computes them) ---
+    double length;            // core length (weight and backtrack applied)
+    double d_edge;            // TEAPOT edge drift / uniform half drift
+    double d_inside;          // TEAPOT inside drift
+    double d_fast_inside;     // fast path: merged uniform drift (2*d_edge)
+    double d_yoshida[4];      // Yoshida drifts slice_length*d_i
+    double k0_drift, k1_drift, h_drift;
+    // --- kick weights and curvature constants per kick weight ---
+    double kw[4];
+    double hl[4];             // h*L*kw + hxl*kw
+    double C0[4];             // round(round(-Q0*kw)*htot)  (chi = 1)
+    double C1[4];             // round(round(htot*Q1)*kw)   (chi = 1)
+    double fast_scale[4];     // fast path: kick weight relative to kw[0]
+    double htot, Q0, Q1;
+    // --- linear edges ---
+    double entry_r21, entry_r43, exit_r21, exit_r43;
+    // --- exact kick passes: knl, knl_rel, main strengths ---
+    ExactPass pass[3];
+    // coefficient area follows (doubles)
+};
+
+struct alignas(16) CavityRec {
+    RecHeader h;
+    int32_t integrator;
+    int32_t n_kicks;
+    int32_t drift_model;      // -1, 0, 1, 3 (see configure_tracking_model)
+    int32_t absolute_time;
+    double length;            // body_length * weight
+    double voltage;           // voltage * weight (sign flipped when backtracking)
+    double d_edge, d_inside, d_yoshida[4];
+    double kw[4];
+    double frequency;
+    double harmonic;
+    double lag_rad;           // DEG2RAD*lag
+    double phase;
+    double phi_const;         // DEG2RAD*lag + phase (valid when phase0 == 0)
+    double w_freq;            // (2*pi/c)*frequency (valid when harmonic == 0)
+};
+
+// Header of an uploaded table.
+struct TableInfo {
+    int64_t n_elements;
+    int64_t table_bytes;
+};
+
+}  // namespace xtg

@@ -1,0 +1,564 @@
+"""Beam elements of the push, with xtrack's constructors and defaults.
+
+Each class keeps the parameters of its xtrack counterpart
+(xtrack/beam_elements/*.py ``_xofields``) and fills one raw C-ABI record
+(``xtg_element``); the library packs the records into the device table.
+Parameter handling follows the reference:
+  * knl/ksl padding and ``order`` / ``inv_factorial_order``:
+    _common.py:481-546 (``_prepare_multipolar_params``), default order 5
+    for the thick magnets (_common.py:18, 426);
+  * knl_rel/ksl_rel default ``[0]`` and equal-length padding:
+    _common.py:548-557;
+  * Bend ``angle``/``length`` -> ``h``, ``k0='from_h'``: _common.py:619-690;
+  * model / integrator / edge-model names: _common.py:20-80;
+  * LimitEllipse a, b -> a_squ, b_squ, a_b_squ: limit_ellipse.py:45-64.
+"""
+import math
+
+import numpy as np
+
+from . import _abi
+
+DEFAULT_MULTIPOLE_ORDER = 5
+UNLIMITED = 1e10                        # beam_elements/_aperture_common.py:6
+
+MODEL_CURVED = {
+    "adaptive": 0, "full": 1, "bend-kick-bend": 2, "rot-kick-rot": 3,
+    "mat-kick-mat": 4, "drift-kick-drift-exact": 5, "drift-kick-drift-expanded": 6,
+    "rot-kick-rot-low-order": 7, "rot-kick-rot-high-order": 8, "expanded": 4,
+}
+MODEL_STRAIGHT = {k: v for k, v in MODEL_CURVED.items() if v not in (2, 3)}
+MODEL_RF = {k: v for k, v in MODEL_STRAIGHT.items() if v not in (1, 4)}
+MODEL_DRIFT = {"adaptive": 0, "expanded": 1, "exact": 2}
+INTEGRATORS = {"adaptive": 0, "teapot": 1, "yoshida4": 2, "uniform": 3}
+EDGE_MODELS = {"suppressed": -1, "linear": 0, "full": 1, "dipole-only": 2}
+
+
+def _index(table, value, what):
+    if isinstance(value, (int, np.integer)):
+        return int(value)
+    try:
+        return table[value]
+    except KeyError:
+        raise ValueError(f"Invalid {what}: {value}") from None
+
+
+def _name_of(table, index):
+    for k, v in table.items():
+        if v == index and k != "expanded":
+            return k
+    return index
+
+
+class BeamElement:
+    """Base of all elements: holds parameters, fills a C-ABI record."""
+    isthick = False
+    _cls = None
+
+    def _fill(self, rec):
+        raise NotImplementedError
+
+    def to_record(self):
+        rec = np.zeros(1, dtype=_abi.ELEMENT_DTYPE)[0]
+        rec["weight"] = 1.0
+        rec["order_rel"] = -1
+        self._fill(rec)
+        return rec
+
+    def copy(self):
+        import copy
+        return copy.deepcopy(self)
+
+    def __repr__(self):
+        return f"{type(self).__name__}({', '.join(f'{k}={v!r}' for k, v in self._repr_items())})"
+
+    def _repr_items(self):
+        return []
+
+
+class Marker(BeamElement):
+    """Marker (beam_elements/marker.py): no effect, counts as an element."""
+    _cls = _abi.CLS_MARKER
+
+    def _fill(self, rec):
+        rec["cls"] = self._cls
+
+
+class Drift(BeamElement):
+    """Drift (drift.py:14-76). ``model``: 'adaptive' (-> expanded), 'expanded', 'exact'."""
+    isthick = True
+    _cls = _abi.CLS_DRIFT
+
+    def __init__(self, length=0.0, model="adaptive"):
+        self.length = float(length)
+        self.model = model
+
+    @property
+    def model(self):
+        return _name_of(MODEL_DRIFT, self._model)
+
+    @model.setter
+    def model(self, value):
+        self._model = _index(MODEL_DRIFT, value, "drift model")
+
+    def _fill(self, rec):
+        rec["cls"] = self._cls
+        rec["length"] = self.length
+        rec["model"] = self._model
+
+    def _repr_items(self):
+        return [("length", self.length)]
+
+
+def _multipolar(order, knl, ksl, default_order):
+    """_common.py:481-546 (_prepare_multipolar_params)."""
+    order = order if order else default_order
+    order = order or 0
+    lengths = [len(v) for v in (knl, ksl) if v is not None]
+    target_len = max([order + 1] + lengths)
+    out = []
+    for v in (knl, ksl):
+        a = np.zeros(target_len, dtype=np.float64)
+        if v is not None:
+            a[:len(v)] = np.asarray(v, dtype=np.float64)
+        out.append(a)
+    order = target_len - 1
+    return order, out[0], out[1], 1.0 / math.factorial(order)
+
+
+def _rel(knl_rel, ksl_rel):
+    """_common.py:548-557 (_handle_knl_ksl_rel_kwargs)."""
+    knl_rel = [0.0] if knl_rel is None else list(knl_rel)
+    ksl_rel = [0.0] if ksl_rel is None else list(ksl_rel)
+    n = max(len(knl_rel), len(ksl_rel))
+    knl_rel = knl_rel + [0.0] * (n - len(knl_rel))
+    ksl_rel = ksl_rel + [0.0] * (n - len(ksl_rel))
+    return np.asarray(knl_rel, dtype=np.float64), np.asarray(ksl_rel, dtype=np.float64)
+
+
+class _Magnet(BeamElement):
+    """Common part of the magnet classes (knl/ksl, knl_rel/ksl_rel, model,
+    integrator, number of kicks)."""
+    _models = MODEL_STRAIGHT
+
+    def _init_common(self, order, knl, ksl, knl_rel, ksl_rel, model, integrator,
+                     num_multipole_kicks, default_order):
+        self._order, self.knl, self.ksl, self.inv_factorial_order = _multipolar(
+            order, knl, ksl, default_order)
+        self.knl_rel, self.ksl_rel = _rel(knl_rel, ksl_rel)
+        self.model = model
+        self.integrator = integrator
+        self.num_multipole_kicks = int(num_multipole_kicks)
+
+    @property
+    def order(self):
+        return self._order
+
+    @property
+    def model(self):
+        return _name_of(self._models, self._model)
+
+    @model.setter
+    def model(self, value):
+        self._model = _index(self._models, value, "model")
+
+    @property
+    def integrator(self):
+        return _name_of(INTEGRATORS, self._integrator)
+
+    @integrator.setter
+    def integrator(self, value):
+        self._integrator = _index(INTEGRATORS, value, "integrator")
+
+    def _fill_common(self, rec):
+        rec["cls"] = self._cls
+        rec["model"] = self._model
+        rec["integrator"] = self._integrator
+        rec["num_multipole_kicks"] = self.num_multipole_kicks
+        rec["order"] = self._order
+        rec["inv_factorial_order"] = self.inv_factorial_order
+        if self._order + 1 > _abi.XTG_MAX_KNL or len(self.knl_rel) > 20:
+            raise ValueError("multipole order above the supported maximum "
+                             f"(knl up to {_abi.XTG_MAX_KNL - 1}, knl_rel up to 19)")
+        rec["knl"][:self._order + 1] = self.knl
+        rec["ksl"][:self._order + 1] = self.ksl
+        rec["order_rel"] = len(self.knl_rel) - 1
+        rec["knl_rel"][:len(self.knl_rel)] = self.knl_rel
+        rec["ksl_rel"][:len(self.ksl_rel)] = self.ksl_rel
+
+
+class Multipole(_Magnet):
+    """Multipole (multipole.py:26-206). Thin (kick only) unless ``isthick``."""
+    _cls = _abi.CLS_MULTIPOLE
+
+    def __init__(self, knl=None, ksl=None, order=None, hxl=0.0, length=0.0, isthick=False,
+                 knl_rel=None, ksl_rel=None, main_order=0, main_is_skew=False,
+                 num_multipole_kicks=0, model="adaptive", integrator="adaptive"):
+        self._init_common(order, knl, ksl, knl_rel, ksl_rel, model, integrator,
+                          num_multipole_kicks, default_order=0)
+        self.hxl = float(hxl)
+        self.length = float(length)
+        self._isthick = bool(isthick)
+        self.main_order = int(main_order)
+        self.main_is_skew = bool(main_is_skew)
+
+    @property
+    def isthick(self):
+        return self._isthick
+
+    @isthick.setter
+    def isthick(self, value):
+        self._isthick = bool(value)
+
+    def _fill(self, rec):
+        self._fill_common(rec)
+        rec["hxl"] = self.hxl
+        rec["length"] = self.length
+        rec["isthick"] = 1 if self._isthick else 0
+        rec["main_order"] = self.main_order
+        rec["main_is_skew"] = 1 if self.main_is_skew else 0
+
+    def _repr_items(self):
+        return [("knl", self.knl.tolist()), ("ksl", self.ksl.tolist())]
+
+
+class Bend(_Magnet):
+    """Sector bend (bend.py:24-124, fields _common.py:561-690).
+
+    ``k0`` defaults to 'from_h' (k0 = h = angle/length). Edges are active
+    with the linear model by default (only 'linear' and 'suppressed' edge
+    models are built)."""
+    isthick = True
+    _cls = _abi.CLS_BEND
+    _models = MODEL_CURVED
+
+    def __init__(self, length=0.0, angle=0.0, k0="from_h", k1=0.0, k2=0.0, knl=None, ksl=None,
+                 order=None, knl_rel=None, ksl_rel=None, model="adaptive",
+                 integrator="adaptive", num_multipole_kicks=0,
+                 edge_entry_active=True, edge_exit_active=True,
+                 edge_entry_model="linear", edge_exit_model="linear",
+                 edge_entry_angle=0.0, edge_exit_angle=0.0,
+                 edge_entry_angle_fdown=0.0, edge_exit_angle_fdown=0.0,
+                 edge_entry_fint=0.0, edge_exit_fint=0.0,
+                 edge_entry_hgap=0.0, edge_exit_hgap=0.0):
+        self._init_common(order, knl, ksl, knl_rel, ksl_rel, model, integrator,
+                          num_multipole_kicks, default_order=DEFAULT_MULTIPOLE_ORDER)
+        self.k1 = float(k1)
+        self.k2 = float(k2)
+        self._length = float(length)
+        self._angle = float(angle)
+        self._k0_from_h = True
+        self._k0 = 0.0
+        self._update_h()
+        self.k0 = k0
+        self.edge_entry_active = int(bool(edge_entry_active))
+        self.edge_exit_active = int(bool(edge_exit_active))
+        self.edge_entry_model = edge_entry_model
+        self.edge_exit_model = edge_exit_model
+        self.edge_entry_angle = float(edge_entry_angle)
+        self.edge_exit_angle = float(edge_exit_angle)
+        self.edge_entry_angle_fdown = float(edge_entry_angle_fdown)
+        self.edge_exit_angle_fdown = float(edge_exit_angle_fdown)
+        self.edge_entry_fint = float(edge_entry_fint)
+        self.edge_exit_fint = float(edge_exit_fint)
+        self.edge_entry_hgap = float(edge_entry_hgap)
+        self.edge_exit_hgap = float(edge_exit_hgap)
+
+    def _update_h(self):
+        self._h = self._angle / self._length if self._length != 0 else 0.0
+        if self._k0_from_h:
+            self._k0 = self._h
+
+    @property
+    def length(self):
+        return self._length
+
+    @length.setter
+    def length(self, v):
+        self._length = float(v)
+        self._update_h()
+
+    @property
+    def angle(self):
+        return self._angle
+
+    @angle.setter
+    def angle(self, v):
+        self._angle = float(v)
+        self._update_h()
+
+    @property
+    def h(self):
+        return self._h
+
+    @property
+    def k0(self):
+        return "from_h" if self._k0_from_h else self._k0
+
+    @k0.setter
+    def k0(self, value):
+        if isinstance(value, str):
+            if value != "from_h":
+                raise ValueError("k0 can only be set to 'from_h' as a string")
+            self._k0_from_h = True
+            self._k0 = self._h
+        else:
+            self._k0_from_h = False
+            self._k0 = float(value)
+
+    @property
+    def edge_entry_model(self):
+        return _name_of(EDGE_MODELS, self._edge_entry_model)
+
+    @edge_entry_model.setter
+    def edge_entry_model(self, v):
+        self._edge_entry_model = _index(EDGE_MODELS, v, "edge model")
+
+    @property
+    def edge_exit_model(self):
+        return _name_of(EDGE_MODELS, self._edge_exit_model)
+
+    @edge_exit_model.setter
+    def edge_exit_model(self, v):
+        self._edge_exit_model = _index(EDGE_MODELS, v, "edge model")
+
+    def _fill(self, rec):
+        self._fill_common(rec)
+        rec["length"] = self._length
+        rec["h"] = self._h
+        rec["k0"] = self._k0
+        rec["k1"] = self.k1
+        rec["k2"] = self.k2
+        rec["edge_entry_active"] = self.edge_entry_active
+        rec["edge_exit_active"] = self.edge_exit_active
+        rec["edge_entry_model"] = self._edge_entry_model
+        rec["edge_exit_model"] = self._edge_exit_model
+        for f in ("edge_entry_angle", "edge_exit_angle", "edge_entry_angle_fdown",
+                  "edge_exit_angle_fdown", "edge_entry_fint", "edge_exit_fint",
+                  "edge_entry_hgap", "edge_exit_hgap"):
+            rec[f] = getattr(self, f)
+
+    def _repr_items(self):
+        return [("length", self._length), ("angle", self._angle), ("k0", self.k0)]
+
+
+class _StraightMagnet(_Magnet):
+    isthick = True
+    _main = None
+
+    def __init__(self, length=0.0, knl=None, ksl=None, order=None, knl_rel=None, ksl_rel=None,
+                 main_is_skew=False, model="adaptive", integrator="adaptive",
+                 num_multipole_kicks=0, edge_entry_active=False, edge_exit_active=False, **k):
+        self._init_common(order, knl, ksl, knl_rel, ksl_rel, model, integrator,
+                          num_multipole_kicks, default_order=DEFAULT_MULTIPOLE_ORDER)
+        self.length = float(length)
+        self.main_is_skew = bool(main_is_skew)
+        self.edge_entry_active = int(bool(edge_entry_active))
+        self.edge_exit_active = int(bool(edge_exit_active))
+        n, s = self._main
+        setattr(self, n, float(k.pop(n, 0.0)))
+        setattr(self, s, float(k.pop(s, 0.0)))
+        if k:
+            raise NameError(f"Invalid argument(s): {set(k)}")
+
+    def _fill(self, rec):
+        self._fill_common(rec)
+        rec["length"] = self.length
+        rec["main_is_skew"] = 1 if self.main_is_skew else 0
+        rec["edge_entry_active"] = self.edge_entry_active
+        rec["edge_exit_active"] = self.edge_exit_active
+        n, s = self._main
+        rec[n] = getattr(self, n)
+        rec[s] = getattr(self, s)
+
+    def _repr_items(self):
+        n, _ = self._main
+        return [("length", self.length), (n, getattr(self, n))]
+
+
+class Quadrupole(_StraightMagnet):
+    """Quadrupole (quadrupole.py:24-146): k1, k1s; default model mat-kick-mat."""
+    _cls = _abi.CLS_QUADRUPOLE
+    _main = ("k1", "k1s")
+
+
+class Sextupole(_StraightMagnet):
+    """Sextupole (sextupole.py): k2, k2s; default drift-kick-drift-expanded."""
+    _cls = _abi.CLS_SEXTUPOLE
+    _main = ("k2", "k2s")
+
+
+class Octupole(_StraightMagnet):
+    """Octupole (octupole.py): k3, k3s; default drift-kick-drift-expanded."""
+    _cls = _abi.CLS_OCTUPOLE
+    _main = ("k3", "k3s")
+
+
+class Cavity(BeamElement):
+    """Cavity (cavity.py:24-200). ``frequency`` [Hz] or ``harmonic``, ``lag``
+    [deg], ``phase`` [rad], ``voltage`` [V]."""
+    isthick = True
+    _cls = _abi.CLS_CAVITY
+
+    def __init__(self, voltage=0.0, frequency=0.0, lag=0.0, phase=0.0, harmonic=0.0,
+                 length=0.0, absolute_time=0, num_kicks=0, model="adaptive",
+                 integrator="adaptive"):
+        if frequency != 0 and harmonic != 0:
+            raise ValueError("Cannot set non-zero frequency when harmonic is not zero.")
+        self.voltage = float(voltage)
+        self.frequency = float(frequency)
+        self.harmonic = float(harmonic)
+        self.lag = float(lag)
+        self.phase = float(phase)
+        self.length = float(length)
+        self.absolute_time = int(absolute_time)
+        self.num_kicks = int(num_kicks)
+        self.model = model
+        self.integrator = integrator
+
+    @property
+    def model(self):
+        return _name_of(MODEL_RF, self._model)
+
+    @model.setter
+    def model(self, value):
+        self._model = _index(MODEL_RF, value, "model")
+
+    @property
+    def integrator(self):
+        return _name_of(INTEGRATORS, self._integrator)
+
+    @integrator.setter
+    def integrator(self, value):
+        self._integrator = _index(INTEGRATORS, value, "integrator")
+
+    def _fill(self, rec):
+        rec["cls"] = self._cls
+        rec["length"] = self.length
+        rec["voltage"] = self.voltage
+        rec["frequency"] = self.frequency
+        rec["harmonic"] = self.harmonic
+        rec["lag"] = self.lag
+        rec["phase"] = self.phase
+        rec["absolute_time"] = self.absolute_time
+        rec["num_multipole_kicks"] = self.num_kicks
+        rec["model"] = self._model
+        rec["integrator"] = self._integrator
+
+    def _repr_items(self):
+        return [("voltage", self.voltage), ("frequency", self.frequency), ("lag", self.lag)]
+
+
+class LimitEllipse(BeamElement):
+    """Elliptical aperture (limit_ellipse.py:12-94)."""
+    _cls = _abi.CLS_LIMIT_ELLIPSE
+
+    def __init__(self, a=None, b=None, a_squ=None, b_squ=None, a_b_squ=None):
+        if a is None and a_squ is None:
+            a = UNLIMITED
+        if b is None and b_squ is None:
+            b = UNLIMITED
+        if a is not None:
+            a_squ = a * a
+        if b is not None:
+            b_squ = b * b
+        if a_b_squ is None:
+            a_b_squ = a_squ * b_squ
+        if not (a_squ > 0.0 and b_squ > 0.0):
+            raise ValueError("a_squ and b_squ have to be positive definite")
+        self.a_squ = float(a_squ)
+        self.b_squ = float(b_squ)
+        self.a_b_squ = float(a_b_squ)
+
+    @property
+    def a(self):
+        return math.sqrt(self.a_squ)
+
+    @property
+    def b(self):
+        return math.sqrt(self.b_squ)
+
+    def _fill(self, rec):
+        rec["cls"] = self._cls
+        rec["a_squ"] = self.a_squ
+        rec["b_squ"] = self.b_squ
+        rec["a_b_squ"] = self.a_b_squ
+
+    def _repr_items(self):
+        return [("a", self.a), ("b", self.b)]
+
+
+class LimitRect(BeamElement):
+    """Rectangular aperture (limit_rect.py)."""
+    _cls = _abi.CLS_LIMIT_RECT
+
+    def __init__(self, min_x=-UNLIMITED, max_x=UNLIMITED, min_y=-UNLIMITED, max_y=UNLIMITED):
+        self.min_x = float(min_x)
+        self.max_x = float(max_x)
+        self.min_y = float(min_y)
+        self.max_y = float(max_y)
+
+    def _fill(self, rec):
+        rec["cls"] = self._cls
+        for f in ("min_x", "max_x", "min_y", "max_y"):
+            rec[f] = getattr(self, f)
+
+    def _repr_items(self):
+        return [("min_x", self.min_x), ("max_x", self.max_x),
+                ("min_y", self.min_y), ("max_y", self.max_y)]
+
+
+# ---------------------------------------------------------------------------
+# Slices (slice_elements_thick.py, slice_elements_thin.py,
+# slice_elements_drift.py, slice_elements_edge.py): a slice refers to its
+# parent and adds its own weight; the record carries the parent's
+# parameters with the slice kind and weight.
+# ---------------------------------------------------------------------------
+class _Slice(BeamElement):
+    _kind = _abi.SLICE_NONE
+
+    def __init__(self, _parent, weight=1.0, parent_name=None):
+        self._parent = _parent
+        self.weight = float(weight)
+        self.parent_name = parent_name
+
+    @property
+    def isthick(self):
+        return self._kind in (_abi.SLICE_THICK, _abi.SLICE_DRIFT)
+
+    def _fill(self, rec):
+        self._parent._fill(rec)
+        rec["slice"] = self._kind
+        rec["weight"] = self.weight
+
+    def _repr_items(self):
+        return [("parent", self.parent_name), ("weight", self.weight)]
+
+
+def _make_slice_classes():
+    out = {}
+    kinds = {"ThickSlice": _abi.SLICE_THICK, "ThinSlice": _abi.SLICE_THIN,
+             "DriftSlice": _abi.SLICE_DRIFT}
+    for parent in ("Bend", "Quadrupole", "Sextupole", "Octupole", "Multipole", "Cavity"):
+        for prefix, kind in kinds.items():
+            name = prefix + parent
+            out[name] = type(name, (_Slice,), {"_kind": kind})
+        if parent not in ("Multipole", "Cavity"):
+            out[f"ThinSlice{parent}Entry"] = type(f"ThinSlice{parent}Entry", (_Slice,),
+                                                  {"_kind": _abi.SLICE_ENTRY})
+            out[f"ThinSlice{parent}Exit"] = type(f"ThinSlice{parent}Exit", (_Slice,),
+                                                 {"_kind": _abi.SLICE_EXIT})
+    return out
+
+
+_SLICE_CLASSES = _make_slice_classes()
+globals().update(_SLICE_CLASSES)
+
+
+def slice_class(parent, prefix, suffix=""):
+    """Slice class named <prefix><ParentClass><suffix> (e.g. ThickSliceBend)."""
+    return _SLICE_CLASSES.get(prefix + type(parent).__name__ + suffix)
+
+
+__all__ = ["Marker", "Drift", "Multipole", "Bend", "Quadrupole", "Sextupole", "Octupole",
+           "Cavity", "LimitEllipse", "LimitRect", "BeamElement", "slice_class"] + sorted(_SLICE_CLASSES)
