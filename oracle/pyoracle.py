@@ -20,6 +20,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_LIB = os.path.join(HERE, "libxtg_oracle.so")
+ORACLE_FMA_LIB = os.path.join(HERE, "libxtg_oracle_fma.so")
 REF_LIBS = {
     "default": os.path.join(HERE, "_ref", "libxtref.so"),
     "exact_drifts": os.path.join(HERE, "_ref", "libxtref_exact.so"),
@@ -61,7 +62,7 @@ class _Config(ctypes.Structure):
 
 def ensure_built(with_ref=True):
     """Builds the oracle libraries if they are missing."""
-    need = not os.path.exists(ORACLE_LIB)
+    need = not os.path.exists(ORACLE_LIB) or not os.path.exists(ORACLE_FMA_LIB)
     if with_ref:
         need = need or not os.path.exists(REF_LIBS["default"])
     if need:
@@ -139,8 +140,12 @@ def track(records, arrs, q0=1.0, mass0=938272088.16, t_sim=0.0, num_turns=1, ele
           num_threads=0, num_ele_line=None, which="oracle"):
     """Runs one track_line call in place on host arrays ``arrs``.
 
-    which='oracle' -> C restatement; which='ref' -> reference-compiled code
-    (monitor and OpenMP mode only on the oracle)."""
+    which='oracle'     -> C restatement (no contraction: the reference's CPU
+                          arithmetic);
+    which='oracle_fma' -> the same source compiled with fused multiply-adds
+                          (the reference's arithmetic as its CUDA build
+                          rounds it);
+    which='ref'        -> reference-compiled code (no monitor, no OpenMP mode)."""
     records = np.ascontiguousarray(records)
     n = len(records)
     if num_ele_track is None:
@@ -149,9 +154,9 @@ def track(records, arrs, q0=1.0, mass0=938272088.16, t_sim=0.0, num_turns=1, ele
         num_ele_line = n
     cfg = _config(use_exact_drifts, cavity_preserve_angle, global_xy_limit)
     ps = _pstruct(arrs, q0, mass0, t_sim)
-    if which == "oracle":
+    if which in ("oracle", "oracle_fma"):
         ensure_built(with_ref=False)
-        lib = _load(ORACLE_LIB, "oracle")
+        lib = _load(ORACLE_LIB if which == "oracle" else ORACLE_FMA_LIB, "oracle")
         mst = None
         if monitor is not None:
             mst = _Monitor()

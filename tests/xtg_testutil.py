@@ -105,3 +105,28 @@ def compare(got, ref, coord_tol, fields=COORDS, mask=None):
         report[f] = (e, int(np.sum(got[f][sel] == ref[f][sel])))
         assert e <= coord_tol, f"{f}: relative error {e:.3e} > {coord_tol:.1e}"
     return report
+
+
+def fma_spread(records, arrs, fields=COORDS, **kw):
+    """Per-field scale-relative distance between the oracle compiled without
+    and with fused multiply-adds after the same call: the reference's own
+    rounding noise for this case. Returns ({field: spread}, mask of particles
+    alive in both runs)."""
+    a = {k: v.copy() for k, v in arrs.items()}
+    b = {k: v.copy() for k, v in arrs.items()}
+    pyoracle.track(records, a, which="oracle", **kw)
+    pyoracle.track(records, b, which="oracle_fma", **kw)
+    ok = (a["state"] > 0) & (b["state"] > 0)
+    return {f: rel_err(b[f][ok], a[f][ok], f) for f in fields}, ok
+
+
+def compare_within_spread(got, ref, spread, mask, factor=3.0, floor=1e-15, fields=COORDS):
+    """Coordinates of ``got`` within ``factor`` x the reference's own FMA
+    spread of ``ref`` (scale-relative, per field)."""
+    out = {}
+    for f in fields:
+        e = rel_err(got[f][mask], ref[f][mask], f)
+        lim = factor * spread[f] + floor
+        out[f] = (e, lim)
+        assert e <= lim, f"{f}: {e:.3e} > {factor} x reference FMA spread {spread[f]:.3e}"
+    return out
