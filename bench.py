@@ -254,6 +254,25 @@ def run_gpu(args):
                         "peak_source": "in-run DFMA probe (FP64 pipe, FMA = 2)",
                         "flops_per_particle_turn": flops_pt, "traffic": _traffic()},
            "clocks": clk.summary()}
+    if not args.no_alt:
+        # the other arithmetic mode on the same beam, same step count
+        alt = "exact" if args.arith == "fast" else "fast"
+        t_alt = line.build_tracker(device=dev, arith=alt)
+        for _ in range(args.warmup):
+            t_alt._track(beam, num_turns=1)
+        torch.cuda.synchronize(dev)
+        a0 = torch.cuda.Event(enable_timing=True)
+        a1 = torch.cuda.Event(enable_timing=True)
+        a0.record(stream)
+        for _ in range(args.steps):
+            t_alt._track(beam, num_turns=1)
+        a1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms_alt = a0.elapsed_time(a1)
+        v_alt = float(n) * args.steps * world / (ms_alt * 1e-3)
+        out[alt] = {"value": v_alt, "unit": UNIT, "ms_per_step": ms_alt / args.steps,
+                    "roofline_frac": flops_pt * n / (ms_alt * 1e-3 / args.steps) / fp64_peak}
+        line.tracker = tracker
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(line)
     if rank == 0:
@@ -280,7 +299,9 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--arith", default="exact", choices=["exact", "fast"])
+    ap.add_argument("--arith", default="fast", choices=["exact", "fast"])
+    ap.add_argument("--no-alt", action="store_true",
+                    help="skip the timing of the other arithmetic mode")
     ap.add_argument("--particles", type=int, default=1_000_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

@@ -101,9 +101,9 @@ def _load(path, kind):
     return lib
 
 
-def _pstruct(arrs, q0, mass0, t_sim):
+def _pstruct(arrs, q0, mass0, t_sim, capacity=None):
     st = _Particles()
-    st.capacity = len(arrs["x"])
+    st.capacity = len(arrs["x"]) if capacity is None else int(capacity)
     st.q0, st.mass0, st.t_sim = q0, mass0, t_sim
     for f in DOUBLE_FIELDS:
         a = arrs.get(f)
@@ -163,7 +163,7 @@ def track(records, arrs, q0=1.0, mass0=938272088.16, t_sim=0.0, num_turns=1, ele
             for k in ("start_at_turn", "stop_at_turn", "part_id_start", "part_id_end", "ebe_mode",
                       "n_repetitions", "repetition_period", "n_records"):
                 setattr(mst, k, int(monitor[k]))
-            mst.data = _pstruct(monitor["data"], 0.0, 0.0, 0.0)
+            mst.data = _pstruct(monitor["data"], 0.0, 0.0, 0.0, capacity=monitor["n_records"])
         st = lib.xto_track(records.ctypes.data, n, ctypes.byref(cfg), ctypes.byref(ps),
                            num_turns, ele_start, num_ele_track, flag_end_turn_actions,
                            flag_reset_s, flag_monitor, num_ele_line, line_length,

@@ -13,6 +13,7 @@
 #include "xtg_oracle.h"
 
 #include <math.h>
+#include <stddef.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -1462,6 +1463,19 @@ static void xto_track_chunk_openmp(const xto_args* a, int64_t ipart, int64_t end
             }
         }
     }
+}
+
+/* sizeof of the C-ABI structs as this compiler lays them out, for the
+ * layout test of the ctypes mirror: element, particles, monitor, config. */
+int32_t xto_abi_sizes(int64_t* out) {
+    out[0] = (int64_t)sizeof(xtg_element);
+    out[1] = (int64_t)sizeof(xtg_particles);
+    out[2] = (int64_t)sizeof(xtg_monitor);
+    out[3] = (int64_t)sizeof(xtg_config);
+    out[4] = (int64_t)offsetof(xtg_element, knl);
+    out[5] = (int64_t)offsetof(xtg_element, shift_x);
+    out[6] = (int64_t)offsetof(xtg_monitor, data);
+    return 4;
 }
 
 int32_t xto_max_threads(void) {

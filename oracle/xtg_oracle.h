@@ -42,6 +42,11 @@ int32_t xto_track(const xtg_element* elements, int64_t n_elements,
                   const xtg_monitor* monitor, uint64_t track_flags,
                   int32_t mode, int32_t num_threads);
 
+/* sizeof / offsetof of the C-ABI structs (layout check of foreign mirrors):
+ * out[0..6] = element, particles, monitor, config sizes; offsets of
+ * element.knl, element.shift_x, monitor.data. */
+int32_t xto_abi_sizes(int64_t* out);
+
 /* Threads the OpenMP runtime would use (1 when built without OpenMP). */
 int32_t xto_max_threads(void);
 

@@ -765,11 +765,19 @@ int32_t pack_lattice(const xtg_element* els, int64_t n, const xtg_config& cfg,
 }
 
 // Canonical minimal FP64 operation count of one element for one particle
-// (FMA = 2 FLOPs; add, mul = 1; div, sqrt, sin, cos = 1).
+// (FMA = 2 FLOPs; add, mul = 1; div, sqrt, sin, cos = 1):
+//   expanded drift 16: xp, yp (2 mul), t = xp^2+yp^2 (mul+fma), 1+t/2 (fma),
+//                      1-rv0v*w (fma), x, y, zeta (3 fma), s (add);
+//   exact drift 18:    pz^2 (mul + 2 fma), sqrt, 1/pz (div), 1-rv0v*opd/pz
+//                      (mul+fma), px/pz*L (mul), x, y, zeta (3 fma), s (add);
+//   kick of merged order N: 4N fma (complex Horner) + 2 fma (apply, chi);
+//   curvature: rot-frame 5 (fma, mul+fma), k0*h 3 (mul+fma),
+//              k1*h 10 (3 mul, 2 fma for w, fma, mul+fma);
+//   cavity 25 (tau, phase, sin, energy kick, ptau/delta/rpp/rvv update).
 double canonical_flops(const unsigned char* rec) {
     const RecHeader* h = reinterpret_cast<const RecHeader*>(rec);
-    const double drift_exp = 15.0;     // 2 mul, 4 fma, 1 add, 1 add (s)
-    const double drift_exact = 17.0;
+    const double drift_exp = 16.0;
+    const double drift_exact = 18.0;
     switch (h->op) {
     case OP_DRIFT: {
         const DriftRec* r = reinterpret_cast<const DriftRec*>(rec);
@@ -780,7 +788,7 @@ double canonical_flops(const unsigned char* rec) {
     case OP_LIMIT_RECT:
         return 0.0;
     case OP_CAVITY:
-        return 30.0;
+        return 25.0;
     case OP_MAGNET: {
         const MagnetRec* r = reinterpret_cast<const MagnetRec*>(rec);
         double f = 0;
@@ -791,8 +799,8 @@ double canonical_flops(const unsigned char* rec) {
         if (r->only_drift) return f + (r->drift_model < 0 ? 0 : dr);
         // kick: merged complex Horner, 4 FMA per order, plus 2 FMA to apply
         double kick = 8.0 * (r->fast_top > 0 ? r->fast_top : 0) + 4.0;
-        if (r->curv_terms & 1) kick += 6;   // hl*(1+delta), rv0v*hl*x
-        if (r->curv_terms & 2) kick += 4;
+        if (r->curv_terms & 1) kick += 5;   // hl*(1+delta), rv0v*hl*x
+        if (r->curv_terms & 2) kick += 3;
         if (r->curv_terms & 4) kick += 10;
         int64_t n_kicks = r->n_kicks;
         int64_t n_drifts = 0;

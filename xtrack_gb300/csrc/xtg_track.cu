@@ -353,11 +353,13 @@ int32_t xtg_lattice_create(const xtg_element* elements, int64_t n_elements, cons
     std::unique_ptr<xtg_lattice> L(new xtg_lattice());
     L->elements.assign(elements, elements + n_elements);
     L->config = *config;
-    XTG_CUDA_CHECK(cudaGetDevice(&L->device));
+    // validate and pack before touching the device, so that an unsupported
+    // element is reported as such on any host
     PackedLattice pl;
     std::string err;
     int32_t st = pack_lattice(L->elements.data(), n_elements, L->config, false, &pl, &err);
     if (st != XTG_OK) return set_error(st, "%s", err.c_str());
+    XTG_CUDA_CHECK(cudaGetDevice(&L->device));
     st = upload_table(pl, &L->fwd);
     if (st != XTG_OK) {
         free_table(&L->fwd);
