@@ -169,6 +169,7 @@ def run_gpu(args):
     n = args.particles
     beam = workloads.gaussian_beam(n, p0c, seed=100 + rank, device=dev)
     tracker = line.build_tracker(device=dev, arith=args.arith)
+    tuning = tracker.set_tuning(**_tuning_args(args))
     lib = _abi.load_library()
     n_el = len(line.element_names)
     flops_pt = tracker.flops_per_particle()
@@ -204,12 +205,20 @@ def run_gpu(args):
         t = torch.tensor([ms], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
+    # particle-turns survived: particles alive after the last timed step
+    # times the steps (a lower bound: particles lost inside the timed
+    # region are not counted for the turns they did survive)
     n_alive1 = int((beam.state > 0).sum().item())
-    particle_turns = float(n) * args.steps * world
+    alive_all = float(n_alive1)
+    if world > 1:
+        t = torch.tensor([alive_all], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(t)
+        alive_all = float(t.item())
+    particle_turns = alive_all * args.steps
     value = particle_turns / (ms * 1e-3)
     ms_per_step = ms / args.steps
     kernel_s = ms * 1e-3 / args.steps
-    achieved = flops_pt * n / kernel_s
+    achieved = flops_pt * n_alive1 / kernel_s
 
     # e2e through the C-ABI with pinned host buffers
     fields = _abi.PARTICLE_DOUBLE_FIELDS + _abi.PARTICLE_INT_FIELDS
@@ -235,7 +244,7 @@ def run_gpu(args):
         e2e_step()
     torch.cuda.synchronize(dev)
     e2e_s = time.perf_counter() - t0
-    e2e_value = float(n) * e2e_steps * world / e2e_s
+    e2e_value = alive_all * e2e_steps / e2e_s
 
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
@@ -245,7 +254,8 @@ def run_gpu(args):
                                   "1e6 protons 7 TeV, 1 turn per step",
                       "particles_per_gpu": n, "elements": n_el, "turns_per_step": 1,
                       "l2": "inputs larger than L2 (152 MB of particle arrays), no flush",
-                      "alive_before": n_alive0, "alive_after": n_alive1},
+                      "alive_before": n_alive0, "alive_after": n_alive1,
+                      "tuning": tuning},
            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                    "d2h_bytes_per_step": h2d},
            "gpu_launches": int(launches),
@@ -258,6 +268,7 @@ def run_gpu(args):
         # the other arithmetic mode on the same beam, same step count
         alt = "exact" if args.arith == "fast" else "fast"
         t_alt = line.build_tracker(device=dev, arith=alt)
+        t_alt.set_tuning(**_tuning_args(args))
         for _ in range(args.warmup):
             t_alt._track(beam, num_turns=1)
         torch.cuda.synchronize(dev)
@@ -269,9 +280,9 @@ def run_gpu(args):
         a1.record(stream)
         torch.cuda.synchronize(dev)
         ms_alt = a0.elapsed_time(a1)
-        v_alt = float(n) * args.steps * world / (ms_alt * 1e-3)
+        v_alt = alive_all * args.steps / (ms_alt * 1e-3)
         out[alt] = {"value": v_alt, "unit": UNIT, "ms_per_step": ms_alt / args.steps,
-                    "roofline_frac": flops_pt * n / (ms_alt * 1e-3 / args.steps) / fp64_peak}
+                    "roofline_frac": flops_pt * n_alive1 / (ms_alt * 1e-3 / args.steps) / fp64_peak}
         line.tracker = tracker
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(line)
@@ -279,6 +290,115 @@ def run_gpu(args):
         print(json.dumps(out))
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def _tuning_args(args):
+    kw = {}
+    for k in ("block_size", "compact_every", "chunk_bytes", "use_graph"):
+        v = getattr(args, k)
+        if v is not None:
+            kw[k] = v
+    return kw
+
+
+def run_da_screen(args):
+    """DA-scan time, surrogate-screened vs plain: a scaled-down learned
+    screening study on the thick ring. Seeds of the ring are scanned on a
+    polar grid (11 angles x 2 momentum offsets x amplitudes up to 20 sigma)
+    with all seeds in one persistent launch; a survival MLP is trained on
+    the training seeds' outcomes with the library's kernels, then the test
+    seeds are scanned twice: plainly (every particle tracked) and screened
+    (only 0.05 < P(survive) < 0.95 plus a 2 % audit tracked). value = plain
+    time / screened time; the DA error (sigma) and the audit's
+    misclassification rate judge the screened result against the plain one."""
+    import torch
+    from xtrack_gb300 import scan as sc
+    from xtrack_gb300 import surrogate as sg
+    from xtrack_gb300 import workloads
+    from xtrack_gb300.batch import BatchTracker
+
+    rank, world, local = _dist()
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    turns = args.da_turns
+    rng = np.random.default_rng(7)
+
+    def counts(n):
+        return rng.integers(args.da_particles // 2, args.da_particles * 3 // 2 + 1, size=n)
+
+    def features(scan):
+        d = scan.deltas[scan.delta_index]
+        return np.concatenate([sg.coord_features(scan.r, scan.theta, d),
+                               scan.seed_features[scan.lattice_index]], axis=1)
+
+    train_lines = [workloads.thick_ring(seed=100 + s) for s in range(args.da_train_seeds)]
+    test_lines = [workloads.thick_ring(seed=200 + s) for s in range(args.da_test_seeds)]
+    t0 = time.perf_counter()
+    s_train = sc.build_scan(train_lines, counts(len(train_lines)), device=dev,
+                            features=sg.seed_features)
+    s_test = sc.build_scan(test_lines, counts(len(test_lines)), device=dev,
+                           features=sg.seed_features)
+    t_setup = time.perf_counter() - t0
+    bt_train = BatchTracker(train_lines, device=dev, arith=args.arith)
+    bt_test = BatchTracker(test_lines, device=dev, arith=args.arith)
+    for bt in (bt_train, bt_test):
+        bt.set_tuning(compact_every=max(1, turns // 10))
+
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    st, at, _ = sc.run_scan(bt_train, s_train, turns, device=dev)
+    t_train_scan = time.perf_counter() - t0
+    surv, lt = sg.targets(st, at, turns)
+    net = sg.SurvivalMLP(seed=0, device=dev)
+    t0 = time.perf_counter()
+    hist = net.fit(features(s_train), surv, lt, epochs=args.da_epochs, batch=2048, lr=2e-3)
+    torch.cuda.synchronize(dev)
+    t_fit = time.perf_counter() - t0
+
+    # plain scan of the test seeds
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    st_p, at_p, _ = sc.run_scan(bt_test, s_test, turns, device=dev)
+    t_plain = time.perf_counter() - t0
+    surv_plain = sg.targets(st_p, at_p, turns)[0] > 0
+
+    # screened scan
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    p, _ = net.predict(features(s_test))
+    track, audit = sg.screen(p, 0.05, 0.95, 0.02, seed=1)
+    st_s, at_s, _ = sc.run_scan(bt_test, s_test, turns, select=track, device=dev)
+    torch.cuda.synchronize(dev)
+    t_screen = time.perf_counter() - t0
+    surv_tracked = sg.targets(st_s, at_s, turns)[0] > 0
+    surv_screen = sg.screened_outcome(p, track, surv_tracked)
+
+    n_seeds = len(test_lines)
+    da_plain = sc.da_table(s_test, surv_plain, n_seeds)
+    da_screen = sc.da_table(s_test, surv_screen, n_seeds)
+    da_err = float(np.max(np.abs(da_screen - da_plain)))
+    aud_idx = np.nonzero(audit)[0]
+    mis = float(np.mean((p[aud_idx] >= 0.5) != surv_plain[aud_idx])) if aud_idx.size else None
+    all_mis = float(np.mean((p >= 0.5) != surv_plain))
+    grid_step = float(np.max(np.diff(np.unique(s_test.r))))
+    out = {"metric": "DA-scan time, surrogate vs plain", "value": t_plain / t_screen,
+           "unit": "x (plain time / screened time)", "higher_is_better": True, "n_gpus": 1,
+           "dtype": "f64 tracking, bf16/f32 network", "data": "synthetic",
+           "config": {"workload": "thick LHC-like ring seeds (6993 elements), polar grid "
+                                  "0-20 sigma x 11 angles x delta in {0, 2.7e-4}",
+                      "turns": turns, "train_seeds": len(train_lines),
+                      "test_seeds": n_seeds, "train_particles": int(s_train.n),
+                      "test_particles": int(s_test.n), "radial_step_sigma": grid_step,
+                      "arith": args.arith},
+           "plain_s": t_plain, "screened_s": t_screen, "tracked_fraction": float(track.mean()),
+           "audit_fraction": float(audit.mean()), "da_error_sigma": da_err,
+           "da_plain_mean_sigma": float(da_plain.mean()),
+           "audit_misclassification": mis, "misclassification_all": all_mis,
+           "train_scan_s": t_train_scan, "fit_s": t_fit, "fit_loss": [hist[0], hist[-1]],
+           "setup_s": t_setup}
+    print(json.dumps(out))
 
 
 def _traffic():
@@ -304,8 +424,21 @@ def main():
                     help="skip the timing of the other arithmetic mode")
     ap.add_argument("--particles", type=int, default=1_000_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--block-size", dest="block_size", type=int, default=None)
+    ap.add_argument("--compact-every", dest="compact_every", type=int, default=None)
+    ap.add_argument("--chunk-bytes", dest="chunk_bytes", type=int, default=None)
+    ap.add_argument("--use-graph", dest="use_graph", type=int, default=None)
+    ap.add_argument("--workload", default="thick_ring", choices=["thick_ring", "da_screen"])
+    ap.add_argument("--da-turns", dest="da_turns", type=int, default=300)
+    ap.add_argument("--da-particles", dest="da_particles", type=int, default=20000,
+                    help="mean particles per seed (uniform in [n/2, 3n/2])")
+    ap.add_argument("--da-train-seeds", dest="da_train_seeds", type=int, default=6)
+    ap.add_argument("--da-test-seeds", dest="da_test_seeds", type=int, default=4)
+    ap.add_argument("--da-epochs", dest="da_epochs", type=int, default=6)
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.workload == "da_screen":
+        run_da_screen(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)

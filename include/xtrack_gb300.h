@@ -205,7 +205,9 @@ int32_t xtg_lattice_info(const xtg_lattice* lattice, int64_t* n_elements,
  * [0, capacity) through `num_turns` turns of elements
  * [ele_start, ele_start+num_ele_track), writing the particles in place.
  * `monitor` may be NULL (flag_monitor must then be 0). Asynchronous on
- * `stream`; no allocation on this path.
+ * `stream`. The lattice owns the scratch of the push (active-particle index
+ * list, work queue); it is allocated on the first call and when the particle
+ * capacity grows, so steady-state calls allocate nothing.
  */
 int32_t xtg_track(const xtg_lattice* lattice, const xtg_particles* particles,
                   int32_t num_turns, int32_t ele_start, int32_t num_ele_track,
@@ -214,21 +216,114 @@ int32_t xtg_track(const xtg_lattice* lattice, const xtg_particles* particles,
                   const xtg_monitor* monitor, uint64_t track_flags,
                   void* stream);
 
-/* Launch-shape tuning for xtg_track (block size and compaction period in
- * turns; 0 keeps the default). Returns the values in effect. */
-int32_t xtg_set_launch_config(xtg_lattice* lattice, int32_t block_size,
-                              int32_t compact_every, int32_t* out_block_size,
-                              int32_t* out_compact_every);
+/* Launch tuning of the push. Results do not depend on it. */
+typedef struct xtg_tuning {
+    int32_t block_size;      /* threads per block: 64, 128 or 256            */
+    int32_t compact_every;   /* turns between lost-particle compactions;
+                                0: only at the start of each call            */
+    int32_t chunk_bytes;     /* shared-memory chunk of the element table
+                                (double-buffered bulk copies), multiple of
+                                16, at most 115712; raised to the largest
+                                element record when smaller. A tracked range
+                                of at most 2*chunk_bytes is copied once and
+                                stays resident. 0: read the table from
+                                global memory                                */
+    int32_t use_graph;       /* replay the compaction + tracking rounds of a
+                                call from a captured CUDA graph              */
+} xtg_tuning;
+
+int32_t xtg_get_tuning(const xtg_lattice* lattice, xtg_tuning* out);
+int32_t xtg_set_tuning(xtg_lattice* lattice, const xtg_tuning* tuning);
+
+/* Device-side status of the calls on this lattice (or batch) since the last
+ * status read: XTG_OK, XTG_E_TIMEOUT when a bounded wait inside a kernel gave
+ * up, XTG_E_VALUE when a particle named a lattice outside the batch (that
+ * particle is not tracked). Synchronizes the device and clears the status. */
+int32_t xtg_device_status(const xtg_lattice* lattice);
+
+/*
+ * Batched push of several lattices that share one element sequence (error
+ * seeds of one ring): one persistent launch tracks every particle through
+ * the lattice named by its entry in `lattice_index` (device int32 array of
+ * `capacity` entries). The batch keeps its own copy of the packed tables;
+ * the lattices may be destroyed afterwards. All lattices must have the same
+ * number of elements and the same xtg_config.
+ */
+typedef struct xtg_batch xtg_batch;
+
+int32_t xtg_batch_create(const xtg_lattice* const* lattices, int32_t n_lattices,
+                         xtg_batch** out);
+int32_t xtg_batch_destroy(xtg_batch* batch);
+int32_t xtg_batch_get_tuning(const xtg_batch* batch, xtg_tuning* out);
+int32_t xtg_batch_set_tuning(xtg_batch* batch, const xtg_tuning* tuning);
+int32_t xtg_batch_device_status(const xtg_batch* batch);
+int32_t xtg_track_batch(xtg_batch* batch, const xtg_particles* particles,
+                        const int32_t* lattice_index, int32_t num_turns,
+                        int32_t ele_start, int32_t num_ele_track,
+                        int32_t flag_end_turn_actions,
+                        int32_t flag_reset_s_at_end_turn, int32_t flag_monitor,
+                        int32_t num_ele_line, double line_length,
+                        const xtg_monitor* monitor, uint64_t track_flags,
+                        void* stream);
 
 /* Blocks until all work on `stream` is done; returns XTG_E_CUDA on error. */
 int32_t xtg_sync(void* stream);
 
-/* Number of kernel launches xtg_track issued since the library loaded. */
+/* Number of kernel launches the library issued since it loaded. */
 int64_t xtg_launch_count(void);
 
 /* FP64 peak probe: DFMA throughput of the current device in FLOP/s
  * (FMA = 2), measured with independent FMA chains over the whole GPU. */
 int32_t xtg_measure_fp64_peak(double* flops_per_s);
+
+/*
+ * Survival surrogate kernels (no reference counterpart: the reference has
+ * no learned component). A multilayer perceptron with BF16 weights and
+ * activations and FP32 accumulation screens dynamic-aperture scans. All
+ * pointers are device pointers; bf16 arrays are passed as void*. All calls
+ * are asynchronous on `stream`.
+ */
+#define XTG_MLP_ACT_NONE 0
+#define XTG_MLP_ACT_GELU 1
+
+/* Tensor-core contraction R[m, n] = sum_k A(m, k) B(n, k), with A(m, k) at
+ * A[m*a_sm + k*a_sk] and B(n, k) at B[n*b_sn + k*b_sk] (bf16, any strides),
+ * FP32 accumulation. Epilogue: z = R + bias[n] (bias may be NULL);
+ * Z[m*z_ld + n] = z (fp32, optional); Y[m*y_ld + n] = act(z) (bf16,
+ * optional); C[m*c_ld + n] = z, or += z with c_accumulate (fp32, optional). */
+int32_t xtg_mlp_gemm(const void* A, int64_t a_sm, int64_t a_sk, const void* B,
+                     int64_t b_sn, int64_t b_sk, int32_t M, int32_t N, int32_t K,
+                     const float* bias, int32_t act, float* Z, int64_t z_ld,
+                     void* Y, int64_t y_ld, float* C, int64_t c_ld,
+                     int32_t c_accumulate, void* stream);
+
+/* dZ = dY * act'(Z) over n elements; fp32 (dZ) and/or bf16 (dZ16) output. */
+int32_t xtg_mlp_act_backward(const float* dY, const float* Z, int64_t n, int32_t act,
+                             float* dZ, void* dZ16, void* stream);
+
+/* out[n] (+)= sum_m X[m*ld + n], fp32, fixed summation order. */
+int32_t xtg_mlp_colsum(const float* X, int64_t M, int32_t N, int64_t ld, float* out,
+                       int32_t accumulate, void* stream);
+
+/* Loss of the two network outputs per sample (out[m*2+0]: logit of
+ * P(survive), out[m*2+1]: normalised log loss turn): binary cross-entropy
+ * plus w_turn * squared error on the loss turn of lost samples. Writes
+ * dLoss/dout / M (fp32 and bf16) and the per-sample loss. */
+int32_t xtg_mlp_loss(const float* out, const float* survive, const float* logturn,
+                     int64_t M, float w_turn, float* dout, void* dout16, float* loss,
+                     void* stream);
+
+/* One Adam step (bias-corrected, decoupled weight decay) on fp32 master
+ * weights w; refreshes the bf16 copy w16 when not NULL. step >= 1. */
+int32_t xtg_mlp_adam(float* w, void* w16, const float* grad, float* m1, float* m2,
+                     int64_t n, float lr, float beta1, float beta2, float eps,
+                     float weight_decay, int64_t step, void* stream);
+
+/* y = bf16(x) over n elements. */
+int32_t xtg_mlp_to_bf16(const float* x, int64_t n, void* y, void* stream);
+
+/* Message of the last failed xtg_mlp_* call of this thread. */
+int32_t xtg_mlp_get_last_error(char* buf, int64_t n);
 
 #ifdef __cplusplus
 }

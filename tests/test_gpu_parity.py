@@ -26,6 +26,8 @@ Tolerances (scale-relative: max|gpu - oracle| / max|oracle| per field):
     inside the spread.
 state, at_turn and at_element are compared bit for bit.
 """
+import math
+
 import numpy as np
 import pytest
 
@@ -199,14 +201,78 @@ def test_monitor_repetitions_and_ebe():
             assert np.max(np.abs(mgot[f] - v)) / scale <= 1e-14, f
 
 
-@pytest.mark.parametrize("compact_every,block", [(1, 0), (7, 128), (0, 64)])
-def test_launch_shapes_do_not_change_results(compact_every, block):
+# (compact_every, block_size, chunk_bytes, use_graph): global-memory table,
+# one resident bulk copy, streamed double-buffered chunks (chunks far smaller
+# than the ring), frequent compaction, graph replay of the rounds
+LAUNCH_SHAPES = [
+    (1, 256, 0, 0), (7, 128, 49152, 0), (0, 64, 49152, 0), (3, 256, 2048, 0),
+    (5, 256, 1024, 1), (0, 128, 0, 1), (2, 64, 4096, 1),
+]
+
+
+@pytest.mark.parametrize("arith", ["exact", "fast"])
+@pytest.mark.parametrize("compact_every,block,chunk,graph", LAUNCH_SHAPES)
+def test_launch_shapes_do_not_change_results(arith, compact_every, block, chunk, graph):
     recs, arrs, L = _setup(workloads.toy_ring(), small_beam(3000, p0c=450e9, seed=22, scale=8.0))
-    base, _ = gpu_track(recs, {k: v.copy() for k, v in arrs.items()}, line_length=L, num_turns=20)
+    base, _ = gpu_track(recs, {k: v.copy() for k, v in arrs.items()}, line_length=L, num_turns=20,
+                        arith=arith, compact_every=0, block_size=256, chunk_bytes=0, use_graph=0)
+    assert np.sum(base["state"] <= 0) > 100      # the case loses particles
     got, _ = gpu_track(recs, {k: v.copy() for k, v in arrs.items()}, line_length=L, num_turns=20,
-                       compact_every=compact_every, block_size=block)
+                       arith=arith, compact_every=compact_every, block_size=block,
+                       chunk_bytes=chunk, use_graph=graph)
     for f in base:
         assert np.array_equal(got[f], base[f], equal_nan=True), f
+
+
+def test_streamed_table_matches_oracle_on_thick_ring():
+    """The 6993-element ring streamed through shared memory in 4 KB chunks
+    with compaction every turn: exact mode still equals the oracle."""
+    recs, arrs, L = _setup(workloads.thick_ring(), small_beam(2000, p0c=450e9, seed=31, scale=4.0))
+    ref = {k: v.copy() for k, v in arrs.items()}
+    pyoracle.track(recs, ref, line_length=L, num_turns=3)
+    got, _ = gpu_track(recs, {k: v.copy() for k, v in arrs.items()}, line_length=L, num_turns=3,
+                       compact_every=1, chunk_bytes=4096, use_graph=1)
+    compare(got, ref, 5e-14)
+
+
+@pytest.mark.parametrize("arith", ["exact", "fast"])
+def test_nan_coordinates_lost_at_global_aperture(arith):
+    """A 3-cell ring closed with 0.35 rad bends is unstable: particles
+    overflow to NaN inside a bend. The reference loses them at that bend's
+    global aperture check (state -1), not at the next local aperture."""
+    line = workloads.thick_ring(seed=1, n_arcs=1, n_cells=3)
+    recs, arrs, L = _setup(line, small_beam(1500, seed=41, scale=3.0))
+    ref = {k: v.copy() for k, v in arrs.items()}
+    pyoracle.track(recs, ref, line_length=L, num_turns=12)
+    assert np.sum(ref["state"] == -1) > 100
+    got, _ = gpu_track(recs, {k: v.copy() for k, v in arrs.items()}, line_length=L, num_turns=12,
+                       arith=arith)
+    if arith == "exact":
+        for f in ("state", "at_element", "at_turn"):
+            assert np.array_equal(got[f], ref[f]), f
+    else:
+        # fast arithmetic may move a loss by its rounding; the global
+        # aperture still catches the overflowing particles
+        assert np.sum(got["state"] == -1) > 100
+
+
+def test_batch_matches_per_seed_oracle():
+    """Three error seeds of one ring in one persistent launch, particles of
+    the seeds interleaved: each particle equals the oracle run of its seed."""
+    from xtg_testutil import gpu_track_batch
+    seeds = [workloads.thick_ring(seed=s, n_arcs=1, n_cells=3, bend_angle=2 * math.pi / 1104)
+             for s in (1, 2, 3)]
+    sets = [line._element_records() for line in seeds]
+    _, arrs, L = _setup(seeds[0], small_beam(1500, seed=41, scale=6.0))
+    rng = np.random.default_rng(5)
+    lat = rng.integers(0, 3, size=len(arrs["x"])).astype(np.int32)
+    got = gpu_track_batch(sets, {k: v.copy() for k, v in arrs.items()}, lat, line_length=L,
+                          num_turns=12, compact_every=4)
+    for s in range(3):
+        sel = lat == s
+        ref = {k: v[sel].copy() for k, v in arrs.items()}
+        pyoracle.track(sets[s], ref, line_length=L, num_turns=12)
+        compare({k: v[sel] for k, v in got.items()}, ref, 5e-14)
 
 
 def test_edge_cases():

@@ -1,0 +1,173 @@
+"""Surrogate kernels: the tensor-core contraction against a torch fp32
+reference (ragged sizes, transposed operands), bias reduction, Adam, and the
+whole network's gradients against torch CPU float64 autograd on the same
+BF16 weights (relative error <= 1e-2); training on a synthetic boundary;
+the screening logic (CPU)."""
+import math
+
+import numpy as np
+import pytest
+
+from xtrack_gb300 import surrogate as sg
+
+
+# ---------------------------------------------------------------- CPU
+def test_screen_masks_and_outcome():
+    p = np.array([0.0, 0.01, 0.3, 0.7, 0.96, 1.0] * 100)
+    track, audit = sg.screen(p, audit=0.1, seed=3)
+    unsure = (p > 0.05) & (p < 0.95)
+    assert np.all(track[unsure]) and not np.any(audit[unsure])
+    assert 0 < audit.sum() < (~unsure).sum()
+    out = sg.screened_outcome(p, track, np.zeros(track.sum(), dtype=bool))
+    assert not np.any(out[track])
+    assert np.all(out[(~track) & (p >= 0.95)]) and not np.any(out[(~track) & (p <= 0.05)])
+
+
+def test_targets_and_features():
+    s, t = sg.targets(np.array([1, 0, -1, 0]), np.array([100, 0, 9, 99]), 100)
+    assert s.tolist() == [1, 0, 0, 0]
+    assert t[1] == 0.0 and abs(t[0] - 1.0) < 1e-6
+    f = sg.coord_features(np.array([1.0, 2.0]), np.array([0.1, 0.2]), 2.7e-4)
+    assert f.shape == (2, sg.N_COORD_FEATURES)
+    from xtrack_gb300 import workloads
+    line = workloads.thick_ring(seed=4, n_arcs=1, n_cells=2, bend_angle=2 * math.pi / 1104)
+    sf = sg.seed_features(line)
+    assert sf.shape == (sg.N_SEED_FEATURES,) and np.all(np.isfinite(sf))
+    assert np.any(sf > 0)
+    line2 = workloads.thick_ring(seed=4, n_arcs=1, n_cells=2, bend_angle=2 * math.pi / 1104,
+                                 with_errors=False)
+    assert np.all(sg.seed_features(line2) == 0)
+
+
+# ---------------------------------------------------------------- GPU
+def _bf(x):
+    import torch
+    return x.to(torch.bfloat16)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("M,N,K", [(37, 70, 38), (256, 256, 256), (1000, 2, 256), (64, 256, 1)])
+@pytest.mark.parametrize("transpose", [False, True])
+def test_gemm_matches_torch(M, N, K, transpose):
+    import torch
+    from xtrack_gb300 import _abi
+    lib = _abi.load_library()
+    g = torch.Generator().manual_seed(M * 7 + N)
+    A = _bf(torch.randn(M, K, generator=g)).cuda()
+    B = _bf(torch.randn(N, K, generator=g)).cuda()
+    bias = torch.randn(N, generator=g).cuda()
+    if transpose:
+        At = A.t().contiguous()      # (k, m) storage
+        Bt = B.t().contiguous()
+        a = (At, 1, M)
+        b = (Bt, 1, N)
+    else:
+        a = (A, K, 1)
+        b = (B, K, 1)
+    Z = torch.empty(M, N, device="cuda")
+    Y = torch.empty(M, N, dtype=torch.bfloat16, device="cuda")
+    C = torch.ones(M, N, device="cuda")
+    st = _abi.check_mlp(lib.xtg_mlp_gemm(
+        sg._ptr(a[0]), a[1], a[2], sg._ptr(b[0]), b[1], b[2], M, N, K, sg._ptr(bias),
+        _abi.MLP_ACT_GELU, sg._ptr(Z), N, sg._ptr(Y), N, sg._ptr(C), N, 1, None))
+    torch.cuda.synchronize()
+    ref = A.float() @ B.float().t() + bias
+    tol = 1e-4 * math.sqrt(K) * float(ref.abs().max())
+    assert float((Z - ref).abs().max()) <= tol
+    assert float((C - (ref + 1)).abs().max()) <= tol
+    gelu = torch.nn.functional.gelu(ref)
+    assert float((Y.float() - gelu).abs().max()) <= 1e-2 * float(gelu.abs().max()) + tol
+
+
+@pytest.mark.gpu
+def test_colsum_and_adam():
+    import torch
+    from xtrack_gb300 import _abi
+    lib = _abi.load_library()
+    g = torch.Generator().manual_seed(1)
+    X = torch.randn(3001, 77, generator=g).cuda()
+    out = torch.empty(77, device="cuda")
+    _abi.check_mlp(lib.xtg_mlp_colsum(sg._ptr(X), 3001, 77, 77, sg._ptr(out), 0, None))
+    out2 = torch.empty(77, device="cuda")
+    _abi.check_mlp(lib.xtg_mlp_colsum(sg._ptr(X), 3001, 77, 77, sg._ptr(out2), 0, None))
+    assert torch.equal(out, out2)                       # fixed order
+    assert torch.allclose(out.double(), X.double().sum(0), rtol=1e-5, atol=1e-4)
+    w = torch.randn(1000, generator=g)
+    grad = torch.randn(1000, generator=g)
+    m1 = torch.zeros(1000)
+    m2 = torch.zeros(1000)
+    wd, w16 = w.clone().cuda(), torch.empty(1000, dtype=torch.bfloat16, device="cuda")
+    m1d, m2d, gd = m1.cuda(), m2.cuda(), grad.cuda()
+    for step in (1, 2, 3):
+        _abi.check_mlp(lib.xtg_mlp_adam(sg._ptr(wd), sg._ptr(w16), sg._ptr(gd), sg._ptr(m1d),
+                                        sg._ptr(m2d), 1000, 1e-2, 0.9, 0.999, 1e-8, 0.01, step,
+                                        None))
+        m1 = 0.9 * m1 + 0.1 * grad
+        m2 = 0.999 * m2 + 0.001 * grad * grad
+        mh = m1 / (1 - 0.9 ** step)
+        vh = m2 / (1 - 0.999 ** step)
+        w = w - 1e-2 * (mh / (vh.sqrt() + 1e-8) + 0.01 * w)
+    assert torch.allclose(wd.cpu(), w, rtol=1e-5, atol=1e-6)
+    assert torch.equal(w16.cpu(), wd.cpu().to(torch.bfloat16))
+
+
+@pytest.mark.gpu
+def test_network_gradients_match_float64_autograd():
+    import torch
+    net = sg.SurvivalMLP(seed=5)
+    rng = np.random.default_rng(2)
+    B = 96
+    X = rng.normal(size=(B, net.dims[0])).astype(np.float32)
+    surv = (rng.random(B) < 0.5).astype(np.float32)
+    lt = rng.random(B).astype(np.float32)
+    X16 = net.prepare_input(X)
+    out = net.forward(X16, keep=True)
+    loss, dout, dout16 = net.loss_and_grad(out, torch.from_numpy(surv).cuda(),
+                                           torch.from_numpy(lt).cuda())
+    net.backward(dout, dout16)
+    torch.cuda.synchronize()
+    # float64 reference on the same (bf16) weights and inputs
+    Ws = [w.double().cpu().requires_grad_(True) for w in net.W16]
+    bs = [b.double().cpu().requires_grad_(True) for b in net.b]
+    h = X16.double().cpu()
+    for l in range(net.n_layers):
+        z = h @ Ws[l].t() + bs[l]
+        h = torch.nn.functional.gelu(z) if l < net.n_layers - 1 else z
+    s = torch.from_numpy(surv).double()
+    t = torch.from_numpy(lt).double()
+    bce = torch.nn.functional.binary_cross_entropy_with_logits(h[:, 0], s, reduction="none")
+    turn = net.w_turn * (h[:, 1] - t) ** 2 * (1 - s)
+    ref_loss = (bce + turn)
+    (ref_loss.sum() / B).backward()
+    hd = h.detach()
+    assert torch.allclose(out.double().cpu(), hd, rtol=0, atol=1e-2 * float(hd.abs().max()))
+    # bf16 activations move the logits by ~1e-2 of their scale; the loss
+    # moves with them
+    rl = ref_loss.detach().numpy()
+    assert np.max(np.abs(loss.cpu().numpy() - rl)) <= 2e-2 * np.max(rl)
+    for l in range(net.n_layers):
+        for got, ref in ((net.gW[l].cpu().double(), Ws[l].grad), (net.gb[l].cpu().double(), bs[l].grad)):
+            rel = float((got - ref).norm() / ref.norm())
+            assert rel <= 1e-2, (l, rel)
+
+
+@pytest.mark.gpu
+def test_training_learns_a_stability_boundary():
+    """Synthetic scan: survival inside r < 6 + 2 cos(2 theta) (sigma units).
+    The trained network classifies held-out points >= 95 % right and most
+    of them confidently (outside the 0.05..0.95 screening band)."""
+    rng = np.random.default_rng(0)
+    n = 40000
+    r = rng.uniform(0, 12, n)
+    th = rng.uniform(0, np.pi / 2, n)
+    X = np.concatenate([sg.coord_features(r, th, 0.0), np.zeros((n, sg.N_SEED_FEATURES))], 1)
+    surv = (r < 6 + 2 * np.cos(2 * th)).astype(np.float32)
+    lt = np.where(surv > 0, 1.0, np.clip((12 - r) / 6, 0, 1)).astype(np.float32)
+    net = sg.SurvivalMLP(seed=1)
+    hist = net.fit(X[:32000], surv[:32000], lt[:32000], epochs=8, batch=1024, lr=2e-3)
+    assert hist[-1] < 0.5 * hist[0]
+    p, _ = net.predict(X[32000:])
+    acc = np.mean((p >= 0.5) == (surv[32000:] > 0))
+    assert acc >= 0.95, acc
+    track, _ = sg.screen(p, audit=0.0)
+    assert track.mean() < 0.3

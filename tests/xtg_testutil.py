@@ -19,7 +19,8 @@ def gpu_track(records, arrs, arith="exact", q0=1.0, mass0=938272088.16, t_sim=0.
               num_turns=1, ele_start=0, num_ele_track=None, flag_end_turn_actions=1,
               flag_reset_s=1, line_length=0.0, track_flags=0, use_exact_drifts=False,
               cavity_preserve_angle=False, global_xy_limit=1.0, monitor=None,
-              flag_monitor=0, num_ele_line=None, compact_every=0, block_size=0):
+              flag_monitor=0, num_ele_line=None, compact_every=None, block_size=None,
+              chunk_bytes=None, use_graph=None):
     """One xtg_track call on cuda:0 over copies of the host arrays ``arrs``.
     Returns (arrays, monitor_data) as numpy."""
     import torch
@@ -44,8 +45,13 @@ def gpu_track(records, arrs, arith="exact", q0=1.0, mass0=938272088.16, t_sim=0.
     _abi.check(lib.xtg_lattice_create(recs.ctypes.data_as(ctypes.c_void_p), n, ctypes.byref(cfg),
                                       ctypes.byref(h)))
     try:
-        if compact_every or block_size:
-            _abi.check(lib.xtg_set_launch_config(h, block_size, compact_every, None, None))
+        tu = _abi.XtgTuning()
+        _abi.check(lib.xtg_get_tuning(h, ctypes.byref(tu)))
+        for name, v in (("compact_every", compact_every), ("block_size", block_size),
+                        ("chunk_bytes", chunk_bytes), ("use_graph", use_graph)):
+            if v is not None:
+                setattr(tu, name, int(v))
+        _abi.check(lib.xtg_set_tuning(h, ctypes.byref(tu)))
         mst = None
         mdata = None
         if monitor is not None:
@@ -62,11 +68,58 @@ def gpu_track(records, arrs, arith="exact", q0=1.0, mass0=938272088.16, t_sim=0.
                                  line_length, ctypes.byref(mst) if mst is not None else None,
                                  int(track_flags), None))
         _abi.check(lib.xtg_sync(None))
+        _abi.check(lib.xtg_device_status(h))
     finally:
         lib.xtg_lattice_destroy(h)
     out = {k: v.cpu().numpy() for k, v in t.items()}
     mon = {k: v.cpu().numpy() for k, v in mdata.items()} if mdata is not None else None
     return out, mon
+
+
+def gpu_track_batch(record_sets, arrs, lattice_index, arith="exact", q0=1.0,
+                    mass0=938272088.16, num_turns=1, line_length=0.0, global_xy_limit=1.0,
+                    compact_every=None, chunk_bytes=None, use_graph=None, block_size=None):
+    """One xtg_track_batch call on cuda:0: particle i is tracked through the
+    lattice built from ``record_sets[lattice_index[i]]``."""
+    import torch
+    lib = _abi.load_library()
+    n = len(record_sets[0])
+    dev = torch.device("cuda:0")
+    t = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in arrs.items()}
+    idx = torch.from_numpy(np.ascontiguousarray(lattice_index, dtype=np.int32)).to(dev)
+    ps = _abi.particles_struct_from_ptrs(len(arrs["x"]), q0, mass0, 0.0,
+                                         {k: v.data_ptr() for k, v in t.items()})
+    cfg = _abi.XtgConfig()
+    cfg.has_global_xy_limit = 0 if global_xy_limit is None else 1
+    cfg.global_xy_limit = 0.0 if global_xy_limit is None else float(global_xy_limit)
+    cfg.arith = _abi.ARITH_EXACT if arith == "exact" else _abi.ARITH_FAST
+    handles = []
+    b = ctypes.c_void_p()
+    try:
+        for recs in record_sets:
+            h = ctypes.c_void_p()
+            recs = np.ascontiguousarray(recs)
+            _abi.check(lib.xtg_lattice_create(recs.ctypes.data_as(ctypes.c_void_p), n,
+                                              ctypes.byref(cfg), ctypes.byref(h)))
+            handles.append(h)
+        arr = (ctypes.c_void_p * len(handles))(*[h.value for h in handles])
+        _abi.check(lib.xtg_batch_create(arr, len(handles), ctypes.byref(b)))
+        tu = _abi.XtgTuning(block_size=256, compact_every=0, chunk_bytes=49152, use_graph=0)
+        for name, v in (("compact_every", compact_every), ("block_size", block_size),
+                        ("chunk_bytes", chunk_bytes), ("use_graph", use_graph)):
+            if v is not None:
+                setattr(tu, name, int(v))
+        _abi.check(lib.xtg_batch_set_tuning(b, ctypes.byref(tu)))
+        _abi.check(lib.xtg_track_batch(b, ctypes.byref(ps), ctypes.c_void_p(idx.data_ptr()),
+                                       num_turns, 0, n, 1, 1, 0, n, line_length, None, 0, None))
+        _abi.check(lib.xtg_sync(None))
+        _abi.check(lib.xtg_batch_device_status(b))
+    finally:
+        if b.value:
+            lib.xtg_batch_destroy(b)
+        for h in handles:
+            lib.xtg_lattice_destroy(h)
+    return {k: v.cpu().numpy() for k, v in t.items()}
 
 
 def make_monitor(start, stop, pid_range, fields=("x", "px", "y", "py", "zeta", "delta", "s",

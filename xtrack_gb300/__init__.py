@@ -13,5 +13,7 @@ from .monitors import ParticlesMonitor
 from .slicing import Strategy, Teapot, Uniform
 from .line import Line, TrackerConfig
 from .tracker import Tracker, TrackFlags
+from .batch import BatchTracker
+from .tuning import autotune
 
 __version__ = "0.1.0"

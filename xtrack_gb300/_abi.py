@@ -134,6 +134,15 @@ class XtgMonitor(ctypes.Structure):
     ]
 
 
+class XtgTuning(ctypes.Structure):
+    _fields_ = [
+        ("block_size", ctypes.c_int32),
+        ("compact_every", ctypes.c_int32),
+        ("chunk_bytes", ctypes.c_int32),
+        ("use_graph", ctypes.c_int32),
+    ]
+
+
 class XtgConfig(ctypes.Structure):
     _fields_ = [
         ("use_exact_drifts", ctypes.c_int32),
@@ -163,9 +172,15 @@ LIB_PATH = os.path.join(_PKG_DIR, "libxtrack_gb300.so")
 
 EXPORTED_SYMBOLS = (
     "xtg_abi_version", "xtg_get_last_error", "xtg_lattice_create", "xtg_lattice_destroy",
-    "xtg_lattice_info", "xtg_track", "xtg_set_launch_config", "xtg_sync",
-    "xtg_launch_count", "xtg_measure_fp64_peak",
+    "xtg_lattice_info", "xtg_track", "xtg_get_tuning", "xtg_set_tuning", "xtg_device_status",
+    "xtg_batch_create", "xtg_batch_destroy", "xtg_batch_get_tuning", "xtg_batch_set_tuning", "xtg_batch_device_status",
+    "xtg_track_batch", "xtg_sync", "xtg_launch_count", "xtg_measure_fp64_peak",
+    "xtg_mlp_gemm", "xtg_mlp_act_backward", "xtg_mlp_colsum", "xtg_mlp_loss", "xtg_mlp_adam",
+    "xtg_mlp_to_bf16", "xtg_mlp_get_last_error",
 )
+
+MLP_ACT_NONE = 0
+MLP_ACT_GELU = 1
 
 _lib = None
 
@@ -197,9 +212,42 @@ def load_library(path=None):
                               c.c_int32, c.c_int32, c.c_int32, c.c_int32, c.c_double,
                               c.POINTER(XtgMonitor), c.c_uint64, c.c_void_p]
     lib.xtg_track.restype = c.c_int32
-    lib.xtg_set_launch_config.argtypes = [c.c_void_p, c.c_int32, c.c_int32, c.POINTER(c.c_int32),
-                                          c.POINTER(c.c_int32)]
-    lib.xtg_set_launch_config.restype = c.c_int32
+    lib.xtg_get_tuning.argtypes = [c.c_void_p, c.POINTER(XtgTuning)]
+    lib.xtg_get_tuning.restype = c.c_int32
+    lib.xtg_set_tuning.argtypes = [c.c_void_p, c.POINTER(XtgTuning)]
+    lib.xtg_set_tuning.restype = c.c_int32
+    lib.xtg_device_status.argtypes = [c.c_void_p]
+    lib.xtg_device_status.restype = c.c_int32
+    lib.xtg_batch_create.argtypes = [c.POINTER(c.c_void_p), c.c_int32, c.POINTER(c.c_void_p)]
+    lib.xtg_batch_create.restype = c.c_int32
+    lib.xtg_batch_destroy.argtypes = [c.c_void_p]
+    lib.xtg_batch_destroy.restype = c.c_int32
+    lib.xtg_batch_get_tuning.argtypes = [c.c_void_p, c.POINTER(XtgTuning)]
+    lib.xtg_batch_get_tuning.restype = c.c_int32
+    lib.xtg_batch_set_tuning.argtypes = [c.c_void_p, c.POINTER(XtgTuning)]
+    lib.xtg_batch_set_tuning.restype = c.c_int32
+    lib.xtg_batch_device_status.argtypes = [c.c_void_p]
+    lib.xtg_batch_device_status.restype = c.c_int32
+    lib.xtg_track_batch.argtypes = [c.c_void_p, c.POINTER(XtgParticles), c.c_void_p, c.c_int32,
+                                    c.c_int32, c.c_int32, c.c_int32, c.c_int32, c.c_int32, c.c_int32,
+                                    c.c_double, c.POINTER(XtgMonitor), c.c_uint64, c.c_void_p]
+    lib.xtg_track_batch.restype = c.c_int32
+    vp, i64, i32, f32 = c.c_void_p, c.c_int64, c.c_int32, c.c_float
+    lib.xtg_mlp_gemm.argtypes = [vp, i64, i64, vp, i64, i64, i32, i32, i32, vp, i32, vp, i64,
+                                 vp, i64, vp, i64, i32, vp]
+    lib.xtg_mlp_gemm.restype = i32
+    lib.xtg_mlp_act_backward.argtypes = [vp, vp, i64, i32, vp, vp, vp]
+    lib.xtg_mlp_act_backward.restype = i32
+    lib.xtg_mlp_colsum.argtypes = [vp, i64, i32, i64, vp, i32, vp]
+    lib.xtg_mlp_colsum.restype = i32
+    lib.xtg_mlp_loss.argtypes = [vp, vp, vp, i64, f32, vp, vp, vp, vp]
+    lib.xtg_mlp_loss.restype = i32
+    lib.xtg_mlp_adam.argtypes = [vp, vp, vp, vp, vp, i64, f32, f32, f32, f32, f32, i64, vp]
+    lib.xtg_mlp_adam.restype = i32
+    lib.xtg_mlp_to_bf16.argtypes = [vp, i64, vp, vp]
+    lib.xtg_mlp_to_bf16.restype = i32
+    lib.xtg_mlp_get_last_error.argtypes = [c.c_char_p, i64]
+    lib.xtg_mlp_get_last_error.restype = i32
     lib.xtg_sync.argtypes = [c.c_void_p]
     lib.xtg_sync.restype = c.c_int32
     lib.xtg_launch_count.restype = c.c_int64
@@ -228,4 +276,14 @@ class XtgError(RuntimeError):
 def check(status, lib=None):
     if status != XTG_OK:
         raise XtgError(status, last_error(lib))
+    return status
+
+
+def check_mlp(status, lib=None):
+    """``check`` for the xtg_mlp_* entry points (their own error slot)."""
+    if status != XTG_OK:
+        lib = lib or load_library()
+        buf = ctypes.create_string_buffer(512)
+        lib.xtg_mlp_get_last_error(buf, len(buf))
+        raise XtgError(status, buf.value.decode(errors="replace"))
     return status

@@ -23,7 +23,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-fmad=false", "-std=c++17", "-Xcompiler",
               "-fPIC,-ffp-contract=off,-O2", "--expt-relaxed-constexpr"]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math"]
 
-CU_SOURCES = ["xtg_track.cu"]
+CU_SOURCES = ["xtg_track.cu", "xtg_mlp.cu"]
 CXX_SOURCES = ["xtg_lattice.cpp"]
 
 

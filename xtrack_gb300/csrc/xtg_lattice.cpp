@@ -373,7 +373,7 @@ void pack_drift(double length, bool exact, bool global_aper, RecBuf* rb) {
     r->exact = exact ? 1 : 0;
 }
 
-void pack_magnet(const xtg_element& e, bool backtrack, RecBuf* rb) {
+void pack_magnet(const xtg_element& e, bool backtrack, bool exact, RecBuf* rb) {
     MagnetIn m = magnet_inputs(e);
     const bool statically_thick =
         (e.slice == XTG_SLICE_NONE && e.cls != XTG_CLS_MULTIPOLE) || e.slice == XTG_SLICE_THICK;
@@ -537,7 +537,10 @@ void pack_magnet(const xtg_element& e, bool backtrack, RecBuf* rb) {
         // exact kick passes (track_magnet_kick.h:67-94)
         std::vector<double> coefs;
         int32_t top;
+        // Only the arithmetic mode of the table stores its coefficients; the
+        // orders are kept in both (they also drive the FLOP accounting).
         top = exact_pass_coefs(m.order, m.inv_factorial_order, m.knl, m.ksl, factor_body, &coefs);
+        if (!exact) coefs.clear();
         {
             int32_t off = rb->append(coefs.data(), coefs.size(), coef_base);
             R()->pass[0].top = top;
@@ -547,6 +550,7 @@ void pack_magnet(const xtg_element& e, bool backtrack, RecBuf* rb) {
         double const factor_rel = factor_body * m.rel_ref_strength;
         top = exact_pass_coefs(m.order_rel, one_over_factorial(m.order_rel), m.knl_rel,
                                m.ksl_rel, factor_rel, &coefs);
+        if (!exact) coefs.clear();
         {
             int32_t off = rb->append(coefs.data(), coefs.size(), coef_base);
             R()->pass[1].top = top;
@@ -560,6 +564,7 @@ void pack_magnet(const xtg_element& e, bool backtrack, RecBuf* rb) {
             ksl_main[i] = ksl_main[i] * L;
         }
         top = exact_pass_coefs(3, 1. / (3 * 2), knl_main, ksl_main, 1, &coefs);
+        if (!exact) coefs.clear();
         {
             int32_t off = rb->append(coefs.data(), coefs.size(), coef_base);
             R()->pass[2].top = top;
@@ -591,7 +596,7 @@ void pack_magnet(const xtg_element& e, bool backtrack, RecBuf* rb) {
             if (cn[i] != 0 || cs[i] != 0) { ftop = i; break; }
         }
         std::vector<double> fc;
-        for (int i = ftop; i >= 0; i--) {
+        for (int i = ftop; i >= 0 && !exact; i--) {
             fc.push_back(cn[i] * kw[0]);
             fc.push_back(cs[i] * kw[0]);
         }
@@ -600,6 +605,34 @@ void pack_magnet(const xtg_element& e, bool backtrack, RecBuf* rb) {
         R()->fast_coef = off;
     }
     rb->pad16();
+
+    // A lone kick without edges gets the compact record (same coefficients).
+    const MagnetRec* r = R();
+    if (r->body_active && r->edge_entry == EDGE_NONE && r->edge_exit == EDGE_NONE &&
+        r->drift_model == -1 && r->only_drift == 0 && r->n_kicks == 1 &&
+        r->integrator == INT_UNIFORM) {
+        RecBuf kb;
+        kb.init(sizeof(KickRec));
+        KickRec* k = kb.head<KickRec>();
+        k->h = r->h;
+        k->h.op = OP_KICK;
+        k->fast_top = r->fast_top;
+        k->fast_coef = r->fast_coef;
+        k->curv_terms = r->curv_terms;
+        for (int q = 0; q < 3; q++) k->pass[q] = r->pass[q];
+        k->kw = r->kw[0];
+        k->hl = r->hl[0];
+        k->C0 = r->C0[0];
+        k->C1 = r->C1[0];
+        k->htot = r->htot;
+        k->Q0 = r->Q0;
+        k->Q1 = r->Q1;
+        size_t const ncoef = (rb->bytes.size() - coef_base) / sizeof(double);
+        kb.append(reinterpret_cast<const double*>(rb->bytes.data() + coef_base), ncoef,
+                  sizeof(KickRec));
+        kb.pad16();
+        rb->bytes.swap(kb.bytes);
+    }
 }
 
 void pack_cavity(const xtg_element& e, bool backtrack, RecBuf* rb) {
@@ -750,7 +783,7 @@ int32_t pack_lattice(const xtg_element* els, int64_t n, const xtg_config& cfg,
                 if (backtrack) length = -e.weight * e.length;
                 pack_drift(length, cfg.use_exact_drifts != 0, true, &rb);
             } else {
-                pack_magnet(e, backtrack, &rb);
+                pack_magnet(e, backtrack, cfg.arith == XTG_ARITH_EXACT, &rb);
             }
             break;
         }
@@ -789,6 +822,14 @@ double canonical_flops(const unsigned char* rec) {
         return 0.0;
     case OP_CAVITY:
         return 25.0;
+    case OP_KICK: {
+        const KickRec* r = reinterpret_cast<const KickRec*>(rec);
+        double kick = 8.0 * (r->fast_top > 0 ? r->fast_top : 0) + 4.0;
+        if (r->curv_terms & 1) kick += 5;
+        if (r->curv_terms & 2) kick += 3;
+        if (r->curv_terms & 4) kick += 10;
+        return kick;
+    }
     case OP_MAGNET: {
         const MagnetRec* r = reinterpret_cast<const MagnetRec*>(rec);
         double f = 0;

@@ -35,6 +35,7 @@ struct PState {
     double chi, charge_ratio, beta0, p0c;
     double ax, ay;
     int64_t state, at_element, at_turn;
+    bool chi_one;     // chi == 1: per-element products precomputed at chi = 1 apply
 };
 
 XTG_DEV void refresh_energy_cache(PState& p) {
@@ -315,63 +316,112 @@ XTG_COLD PState magnet_drift_curved(PState p, double length, int drift_model, do
 
 // One kick_simple pass in the reference arithmetic (track_magnet_kick.h:
 // 182-260). `co` holds quintuples (A, B, knl, ksl, invf) from `top` down.
-XTG_DEV void exact_pass(PState& p, const double* __restrict__ co, int top, double factor,
-                        double kick_weight, double x, double y) {
-    double dpx_mul, dpy_mul;
-    if (p.chi == 1.0) {
-        dpx_mul = co[0];
-        dpy_mul = co[1];
-        for (int i = top; i > 0; i--) {
-            co += 5;
-            double const zre = dpx_mul * x - dpy_mul * y;
-            double const zim = dpx_mul * y + dpy_mul * x;
-            dpx_mul = co[0] + zre;
-            dpy_mul = co[1] + zim;
-        }
-    } else {
-        double const chi = p.chi;
-        dpx_mul = chi * co[2] * factor * co[4];
-        dpy_mul = chi * co[3] * factor * co[4];
-        for (int i = top; i > 0; i--) {
-            co += 5;
-            double const zre = dpx_mul * x - dpy_mul * y;
-            double const zim = dpx_mul * y + dpy_mul * x;
-            double const this_knl = chi * co[2] * factor;
-            double const this_ksl = chi * co[3] * factor;
-            dpx_mul = this_knl * co[4] + zre;
-            dpy_mul = this_ksl * co[4] + zim;
-        }
+// At chi = 1, chi*knl*factor*invf equals the precomputed A (and B).
+XTG_DEV void exact_pass_chi1(PState& p, const double* __restrict__ co, int top,
+                             double kick_weight, double x, double y) {
+    double dpx_mul = co[0];
+    double dpy_mul = co[1];
+    for (int i = top; i > 0; i--) {
+        co += 5;
+        double const zre = dpx_mul * x - dpy_mul * y;
+        double const zim = dpx_mul * y + dpy_mul * x;
+        dpx_mul = co[0] + zre;
+        dpy_mul = co[1] + zim;
     }
     dpx_mul = -dpx_mul;
     p.px = p.px + kick_weight * dpx_mul;
     p.py = p.py + kick_weight * dpy_mul;
 }
 
-// track_magnet_kick.h:23-144 for kick-weight slot k of a magnet record.
+XTG_DEV void exact_pass(PState& p, const double* __restrict__ co, int top, double factor,
+                        double kick_weight, double x, double y) {
+    double const chi = p.chi;
+    double dpx_mul = chi * co[2] * factor * co[4];
+    double dpy_mul = chi * co[3] * factor * co[4];
+    for (int i = top; i > 0; i--) {
+        co += 5;
+        double const zre = dpx_mul * x - dpy_mul * y;
+        double const zim = dpx_mul * y + dpy_mul * x;
+        double const this_knl = chi * co[2] * factor;
+        double const this_ksl = chi * co[3] * factor;
+        dpx_mul = this_knl * co[4] + zre;
+        dpy_mul = this_ksl * co[4] + zim;
+    }
+    dpx_mul = -dpx_mul;
+    p.px = p.px + kick_weight * dpx_mul;
+    p.py = p.py + kick_weight * dpy_mul;
+}
+
+// The parameters of one kick, read from a MagnetRec (kick-weight slot k) or
+// from a compact KickRec.
+struct KickArgs {
+    const ExactPass* pass;
+    int fast_top, fast_coef, curv;
+    double kw, hl, C0, C1, htot, Q0, Q1, fscale;
+};
+
+XTG_DEV KickArgs kick_args(const MagnetRec& r, int k) {
+    KickArgs a;
+    a.pass = r.pass;
+    a.fast_top = r.fast_top;
+    a.fast_coef = r.fast_coef;
+    a.curv = r.curv_terms;
+    a.kw = r.kw[k];
+    a.hl = r.hl[k];
+    a.C0 = r.C0[k];
+    a.C1 = r.C1[k];
+    a.htot = r.htot;
+    a.Q0 = r.Q0;
+    a.Q1 = r.Q1;
+    a.fscale = r.fast_scale[k];
+    return a;
+}
+
+XTG_DEV KickArgs kick_args(const KickRec& r) {
+    KickArgs a;
+    a.pass = r.pass;
+    a.fast_top = r.fast_top;
+    a.fast_coef = r.fast_coef;
+    a.curv = r.curv_terms;
+    a.kw = r.kw;
+    a.hl = r.hl;
+    a.C0 = r.C0;
+    a.C1 = r.C1;
+    a.htot = r.htot;
+    a.Q0 = r.Q0;
+    a.Q1 = r.Q1;
+    a.fscale = 1.0;
+    return a;
+}
+
+// track_magnet_kick.h:23-144.
 template <bool kExact>
-XTG_DEV void magnet_kick(PState& p, const MagnetRec& r, const double* __restrict__ coefs, int k) {
+XTG_DEV void apply_kick(PState& p, const KickArgs& a, const double* __restrict__ coefs) {
     double const x = p.x, y = p.y;
     if (kExact) {
-        double const kw = r.kw[k];
+        double const kw = a.kw;
 #pragma unroll 1
         for (int q = 0; q < 3; q++) {
-            if (r.pass[q].top >= 0)
-                exact_pass(p, coefs + r.pass[q].coef, r.pass[q].top, r.pass[q].factor, kw, x, y);
+            int const top = a.pass[q].top;
+            if (top >= 0) {
+                if (p.chi_one) exact_pass_chi1(p, coefs + a.pass[q].coef, top, kw, x, y);
+                else exact_pass(p, coefs + a.pass[q].coef, top, a.pass[q].factor, kw, x, y);
+            }
         }
-        int const curv = r.curv_terms;
+        int const curv = a.curv;
         if (curv) {
             double dpx = 0.0, dpy = 0.0, dzeta = 0.0;
             double const chi = p.chi;
             double C0, C1;
-            if (chi == 1.0) {
-                C0 = r.C0[k];
-                C1 = r.C1[k];
+            if (p.chi_one) {
+                C0 = a.C0;
+                C1 = a.C1;
             } else {
-                C0 = -chi * r.Q0 * kw * r.htot;
-                C1 = r.htot * chi * r.Q1 * kw;
+                C0 = -chi * a.Q0 * kw * a.htot;
+                C1 = a.htot * chi * a.Q1 * kw;
             }
             if (curv & 1) {
-                double const hl = r.hl[k];
+                double const hl = a.hl;
                 dpx = dpx + hl * p.opd;
                 dzeta = dzeta + -p.rv0v * hl * x;
             }
@@ -387,9 +437,9 @@ XTG_DEV void magnet_kick(PState& p, const MagnetRec& r, const double* __restrict
     } else {
         // merged polynomial sum_i (cn_i + i cs_i) z^i, z = x + i y
         double pr = 0.0, pi = 0.0;
-        int const top = r.fast_top;
+        int const top = a.fast_top;
         if (top >= 0) {
-            const double* __restrict__ c = coefs + r.fast_coef;
+            const double* __restrict__ c = coefs + a.fast_coef;
             pr = c[0];
             pi = c[1];
             for (int i = top; i > 0; i--) {
@@ -400,27 +450,32 @@ XTG_DEV void magnet_kick(PState& p, const MagnetRec& r, const double* __restrict
                 pi = ni;
             }
         }
-        double const cs = p.chi * r.fast_scale[k];
-        double dpx = -cs * pr;
-        double dpy = cs * pi;
-        int const curv = r.curv_terms;
+        // every term is accumulated straight into px / py, in the
+        // reference's order (multipoles, then curvature terms)
+        double const cs = p.chi_one ? a.fscale : p.chi * a.fscale;
+        p.px = fma(-cs, pr, p.px);
+        p.py = fma(cs, pi, p.py);
+        int const curv = a.curv;
         if (curv) {
             double const chi = p.chi;
             if (curv & 1) {
-                double const hl = r.hl[k];
-                dpx = fma(hl, p.opd, dpx);
+                double const hl = a.hl;
+                p.px = fma(hl, p.opd, p.px);
                 p.zeta = fma(-p.rv0v * hl, x, p.zeta);
             }
-            if (curv & 2) dpx = fma(chi * r.C0[k], x, dpx);
+            if (curv & 2) p.px = fma(p.chi_one ? a.C0 : chi * a.C0, x, p.px);
             if (curv & 4) {
-                double const c1 = chi * r.C1[k];
-                dpx = fma(c1, fma(-x, x, 0.5 * y * y), dpx);
-                dpy = fma(c1 * x, y, dpy);
+                double const c1 = p.chi_one ? a.C1 : chi * a.C1;
+                p.px = fma(c1, fma(-x, x, 0.5 * y * y), p.px);
+                p.py = fma(c1 * x, y, p.py);
             }
         }
-        p.px = p.px + dpx;
-        p.py = p.py + dpy;
     }
+}
+
+template <bool kExact>
+XTG_DEV void magnet_kick(PState& p, const MagnetRec& r, const double* __restrict__ coefs, int k) {
+    apply_kick<kExact>(p, kick_args(r, k), coefs);
 }
 
 // track_magnet_edge.h:16-80 with the linear model (track_dipole_edge_linear.h)

@@ -23,6 +23,8 @@ enum Op : int32_t {
     OP_CAVITY = 3,        // Cavity and its slices
     OP_LIMIT_ELLIPSE = 4,
     OP_LIMIT_RECT = 5,
+    OP_KICK = 6,          // a magnet that is a single kick with no edges (thin
+                          // multipoles, thin slices): compact form of OP_MAGNET
 };
 
 // RecHeader.flags
@@ -107,6 +109,19 @@ struct alignas(16) MagnetRec {
     double entry_r21, entry_r43, exit_r21, exit_r43;
     // --- exact kick passes: knl, knl_rel, main strengths ---
     ExactPass pass[3];
+    // coefficient area follows (doubles)
+};
+
+// Compact record of a thin kick (model -1, one kick, no edges). Same
+// meaning as the MagnetRec fields of kick-weight slot 0.
+struct alignas(16) KickRec {
+    RecHeader h;
+    int32_t fast_top;
+    int32_t fast_coef;
+    int32_t curv_terms;
+    int32_t reserved;
+    ExactPass pass[3];
+    double kw, hl, C0, C1, htot, Q0, Q1, reserved2;
     // coefficient area follows (doubles)
 };
 

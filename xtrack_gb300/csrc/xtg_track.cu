@@ -2,10 +2,25 @@
 // include/xtrack_gb300.h.
 //
 // Replaces xtrack's generated `track_line` kernel (xtrack/tracker.py:
-// 543-750). One thread owns one particle for a whole launch: its
-// coordinates live in registers, elements are read from the packed table
-// (xtg_table.h) as warp-uniform records, and particle memory is touched only
-// at launch boundaries and monitor records.
+// 543-750). The reference launches one thread per particle slot and lets a
+// lost particle's thread idle for the rest of the launch; it reads every
+// element through a table of references in global memory. Here:
+//
+//  * rounds: a call is split into rounds of `compact_every` turns. Before
+//    each round, a compaction kernel (warp ballot + prefix sum, grouped by
+//    lattice with match_any) lists the particles still alive, and a queue
+//    kernel cuts that list into work items of one block each;
+//  * a persistent kernel pulls work items from the device queue. Each thread
+//    owns one particle, keeps its coordinates in registers for the whole
+//    round and walks the packed element table (xtg_table.h) with
+//    warp-uniform records and a warp-uniform switch on the element type;
+//  * the element table is staged in shared memory: with one bulk copy per
+//    lattice when the tracked range fits, otherwise streamed in chunks
+//    through a double-buffered cp.async.bulk + mbarrier pipeline. Every wait
+//    is bounded; on time-out the kernel records XTG_E_TIMEOUT and returns;
+//  * several lattices (error seeds) share one launch: a work item belongs to
+//    one lattice, named by the particles' lattice index;
+//  * the rounds of a call can be replayed from a captured CUDA graph.
 //
 // Compiled with -fmad=false: the exact-arithmetic path must not have its
 // products fused into additions. The fast path uses explicit fma().
@@ -14,6 +29,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <atomic>
 #include <memory>
 #include <mutex>
@@ -42,87 +58,134 @@ static int32_t set_error(int32_t code, const char* fmt, ...) {
     return code;
 }
 
-#define XTG_CUDA_CHECK(call)                                                         \
-    do {                                                                             \
-        cudaError_t e_ = (call);                                                     \
-        if (e_ != cudaSuccess)                                                       \
-            return set_error(XTG_E_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_)); \
+#define XTG_CUDA_CHECK(call)                                                                 \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess)                                                               \
+            return set_error(XTG_E_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_));   \
     } while (0)
 
-// ---------------------------------------------------------------------------
-// lattice handle
-// ---------------------------------------------------------------------------
-struct DevTable {
-    unsigned char* d_bytes = nullptr;
-    int64_t* d_offsets = nullptr;
-    int64_t n_bytes = 0;
-    std::vector<int64_t> h_offsets;
-    std::vector<double> flops;
-};
+// largest staging chunk: two chunks plus the static shared memory of the
+// push kernel stay within the 227 KB a block may use
+static constexpr int32_t kMaxChunkBytes = 113 * 1024;
 
-struct xtg_lattice {
-    std::vector<xtg_element> elements;
-    xtg_config config;
-    int device = 0;
-    DevTable fwd;
-    DevTable bwd;          // built on first backtracking call
-    bool has_bwd = false;
-    int32_t block_size = 256;
-    int32_t compact_every = 0;   // turns per launch (0: all turns in one launch)
-    std::mutex mu;
-};
-
-static int32_t upload_table(const PackedLattice& pl, DevTable* t) {
-    t->n_bytes = (int64_t)pl.bytes.size();
-    t->h_offsets = pl.offsets;
-    t->flops = pl.flops_fast;
-    size_t nb = pl.bytes.size() > 0 ? pl.bytes.size() : 16;
-    XTG_CUDA_CHECK(cudaMalloc(&t->d_bytes, nb));
-    XTG_CUDA_CHECK(cudaMalloc(&t->d_offsets, pl.offsets.size() * sizeof(int64_t)));
-    if (!pl.bytes.empty())
-        XTG_CUDA_CHECK(cudaMemcpy(t->d_bytes, pl.bytes.data(), pl.bytes.size(), cudaMemcpyHostToDevice));
-    XTG_CUDA_CHECK(cudaMemcpy(t->d_offsets, pl.offsets.data(), pl.offsets.size() * sizeof(int64_t),
-                              cudaMemcpyHostToDevice));
-    return XTG_OK;
-}
-
-static void free_table(DevTable* t) {
-    if (t->d_bytes) cudaFree(t->d_bytes);
-    if (t->d_offsets) cudaFree(t->d_offsets);
-    t->d_bytes = nullptr;
-    t->d_offsets = nullptr;
-}
+// device error word values
+#define XTG_DEV_ERR_TIMEOUT 1
+#define XTG_DEV_ERR_LATTICE_INDEX 2
 
 // ---------------------------------------------------------------------------
-// kernel
+// kernel arguments
 // ---------------------------------------------------------------------------
-struct KParams {
-    const unsigned char* __restrict__ table;
-    int64_t rec_begin;           // byte offset of the first record to track
-    int32_t rec_count;           // records per turn
-    int32_t num_turns;
-    int64_t capacity;
-    xtg_particles P;
-    xtg_monitor M;
+struct TrackArgs {
+    const unsigned char* __restrict__ table;   // all lattices' records, concatenated
+    const int64_t* __restrict__ lat_base;      // byte offset of each lattice's table
+    const int64_t* __restrict__ rec_off;       // per lattice: n+1 record offsets
+    const int32_t* __restrict__ chunk_end;     // per lattice: n+1 chunk ends (staging)
+    int64_t stride;                            // n+1
+    int32_t rec_first;                         // first record of the tracked range
+    int32_t rec_count;                         // records per turn
+    int32_t num_turns;                         // turns of this round
+    int32_t chunk_bytes;                       // 0: read records from global memory
+    int32_t smem_bytes;                        // dynamic shared memory of the block
     int32_t flag_monitor;
     int32_t flag_end_turn_actions;
     int32_t flag_reset_s;
     int32_t backtrack;
-    int64_t num_ele_line;
-    double line_length;
-    uint64_t track_flags;
     int32_t has_global;
     int32_t preserve_angle;
     double global_lim;
+    int64_t num_ele_line;
+    double line_length;
+    uint64_t track_flags;
+    const int32_t* __restrict__ idx;           // active particle indices
+    const int4* __restrict__ items;            // (lattice, start, count, -)
+    const int32_t* n_items;
+    int32_t* item_counter;
+    int32_t* err;
+    xtg_particles P;
+    xtg_monitor M;
 };
 
 __device__ __forceinline__ bool flag_on(uint64_t flags, int bit) { return (flags >> bit) & 1u; }
 
-// particles_monitor.h:12-77 record (LocalParticle_to_Particles into the
-// monitor's data at `store_at`; NULL arrays are not recorded).
-__device__ __forceinline__ void monitor_store(const KParams& kp, const PState& p, int64_t i, int64_t k) {
-    const xtg_particles& D = kp.M.data;
-    const xtg_particles& S = kp.P;
+// ---------------------------------------------------------------------------
+// PTX helpers: mbarrier and 1-D bulk copies (the TMA engine), shared::cta
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_fence_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes,
+                                              uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait (about 2 s of SM clock): on time-out records the error word
+// and returns false.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int32_t* err) {
+    if (mbar_try_wait(bar, parity)) return true;
+    long long const t0 = clock64();
+    while (!mbar_try_wait(bar, parity)) {
+        if (clock64() - t0 > 4000000000LL) {
+            atomicExch(err, XTG_DEV_ERR_TIMEOUT);
+            return false;
+        }
+    }
+    return true;
+}
+
+// After a timed-out wait: thread 0 waits (again bounded) for the bulk copies
+// it issued that were not seen complete, so that no copy still writes into
+// the block's shared memory when the block exits.
+__device__ __forceinline__ void drain_copies(uint64_t* bars, const uint32_t* phase, uint32_t pending,
+                                             int32_t* err) {
+    for (int b = 0; b < 2; b++)
+        if (pending & (1u << b)) (void)mbar_wait_bounded(&bars[b], phase[b], err);
+}
+
+// Copies `bytes` (multiple of 16, at most 1 MB, 16-byte aligned ends) into
+// shared memory; the consumers wait on `bar`. Called by one thread.
+__device__ __forceinline__ void issue_copy(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    mbar_expect_tx(bar, bytes);
+    bulk_copy_g2s(dst, src, bytes, bar);
+}
+
+// ---------------------------------------------------------------------------
+// monitor (particles_monitor.h:12-77)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void monitor_store(const TrackArgs& a, const PState& p, int64_t i, int64_t k) {
+    const xtg_particles& D = a.M.data;
+    const xtg_particles& S = a.P;
     if (D.x) D.x[k] = p.x;
     if (D.px) D.px[k] = p.px;
     if (D.y) D.y[k] = p.y;
@@ -149,13 +212,13 @@ __device__ __forceinline__ void monitor_store(const KParams& kp, const PState& p
     if (D.parent_particle_id) D.parent_particle_id[k] = S.parent_particle_id ? S.parent_particle_id[i] : 0;
 }
 
-__device__ __forceinline__ void monitor(const KParams& kp, const PState& p, int64_t i, int64_t pid) {
-    const xtg_monitor& m = kp.M;
+__device__ __forceinline__ void monitor(const TrackArgs& a, const PState& p, int64_t i, int64_t pid) {
+    const xtg_monitor& m = a.M;
     int64_t at_turn;
     if (m.ebe_mode) {
         at_turn = p.at_element;
     } else {
-        if (kp.backtrack) return;
+        if (a.backtrack) return;
         at_turn = p.at_turn;
     }
     int64_t const n_turns_record = m.stop_at_turn - m.start_at_turn;
@@ -163,7 +226,7 @@ __device__ __forceinline__ void monitor(const KParams& kp, const PState& p, int6
         if (at_turn >= m.start_at_turn && at_turn < m.stop_at_turn && pid < m.part_id_end &&
             pid >= m.part_id_start) {
             int64_t const store_at = n_turns_record * (pid - m.part_id_start) + at_turn - m.start_at_turn;
-            if (store_at >= 0 && store_at < m.n_records) monitor_store(kp, p, i, store_at);
+            if (store_at >= 0 && store_at < m.n_records) monitor_store(a, p, i, store_at);
         }
     } else if (m.n_repetitions > 1) {
         if (at_turn < m.start_at_turn) return;
@@ -174,21 +237,28 @@ __device__ __forceinline__ void monitor(const KParams& kp, const PState& p, int6
             int64_t const store_at = n_turns_record * (m.part_id_end - m.part_id_start) * i_frame +
                                      n_turns_record * (pid - m.part_id_start) +
                                      (at_turn - i_frame * m.repetition_period) - m.start_at_turn;
-            if (store_at >= 0 && store_at < m.n_records) monitor_store(kp, p, i, store_at);
+            if (store_at >= 0 && store_at < m.n_records) monitor_store(a, p, i, store_at);
         }
     }
 }
 
-// Applies one packed record; returns whether the global aperture applies.
+// ---------------------------------------------------------------------------
+// one element record
+// ---------------------------------------------------------------------------
 template <bool kExact>
 __device__ __forceinline__ bool apply_record(PState& p, const unsigned char* __restrict__ rec,
-                                             const KParams& kp, const RfCtx& rf) {
+                                             const TrackArgs& a, const RfCtx& rf) {
     const RecHeader& h = *reinterpret_cast<const RecHeader*>(rec);
     switch (h.op) {
     case OP_DRIFT: {
         const DriftRec& r = *reinterpret_cast<const DriftRec*>(rec);
         if (r.exact) drift_exact<kExact>(p, r.length);
         else drift_expanded<kExact>(p, r.length);
+        break;
+    }
+    case OP_KICK: {
+        const KickRec& r = *reinterpret_cast<const KickRec*>(rec);
+        apply_kick<kExact>(p, kick_args(r), reinterpret_cast<const double*>(rec + sizeof(KickRec)));
         break;
     }
     case OP_MAGNET: {
@@ -206,7 +276,7 @@ __device__ __forceinline__ bool apply_record(PState& p, const unsigned char* __r
     }
     case OP_LIMIT_ELLIPSE: {
         // limitellipse.h:12-38
-        if (!flag_on(kp.track_flags, XTG_FLAG_IGNORE_LOCAL_APERTURE)) {
+        if (!flag_on(a.track_flags, XTG_FLAG_IGNORE_LOCAL_APERTURE)) {
             const LimitEllipseRec& r = *reinterpret_cast<const LimitEllipseRec*>(rec);
             double const temp = p.x * p.x * r.b_squ + p.y * p.y * r.a_squ;
             if (!(temp <= r.a_b_squ)) p.state = 0;
@@ -215,7 +285,7 @@ __device__ __forceinline__ bool apply_record(PState& p, const unsigned char* __r
     }
     case OP_LIMIT_RECT: {
         // limitrect.h:9-36
-        if (!flag_on(kp.track_flags, XTG_FLAG_IGNORE_LOCAL_APERTURE)) {
+        if (!flag_on(a.track_flags, XTG_FLAG_IGNORE_LOCAL_APERTURE)) {
             const LimitRectRec& r = *reinterpret_cast<const LimitRectRec*>(rec);
             bool const alive = (p.x >= r.min_x) && (p.x <= r.max_x) && (p.y >= r.min_y) && (p.y <= r.max_y);
             if (!alive) p.state = 0;
@@ -228,85 +298,326 @@ __device__ __forceinline__ bool apply_record(PState& p, const unsigned char* __r
     return (h.flags & F_GLOBAL_APER) != 0;
 }
 
+// Walks records [rec, rec_end) for one particle; stops at a loss.
 template <bool kExact>
-__global__ void __launch_bounds__(256) track_kernel(const KParams kp) {
-    int64_t const i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= kp.capacity) return;
-    const xtg_particles& P = kp.P;
-    int64_t const state0 = P.state[i];
-    if (state0 <= 0) return;   // inactive: the reference leaves it unchanged
+__device__ __forceinline__ void walk(PState& p, bool& active, const unsigned char* rec,
+                                     const unsigned char* rec_end, const TrackArgs& a, const RfCtx& rf,
+                                     bool ignore_global, int64_t i, int64_t pid) {
+    int64_t const incr = a.backtrack ? -1 : 1;
+    while (active && rec < rec_end) {
+        if (a.flag_monitor == 2) monitor(a, p, i, pid);
+        bool const thick = apply_record<kExact>(p, rec, a, rf);
+        if (thick && !ignore_global) {
+            // local_particle_custom_api.h:259-287
+            double const lim = a.global_lim;
+            bool const within = (p.x >= -lim) && (p.x <= lim) && (p.y >= -lim) && (p.y <= lim);
+            if (p.state > 0 && !within) p.state = -1;
+        }
+        if (p.state <= 0) {
+            active = false;
+            break;
+        }
+        p.at_element += incr;
+        rec += reinterpret_cast<const RecHeader*>(rec)->nbytes;
+    }
+}
 
-    PState p;
-    p.x = P.x[i]; p.px = P.px[i]; p.y = P.y[i]; p.py = P.py[i];
-    p.zeta = P.zeta[i]; p.delta = P.delta[i]; p.ptau = P.ptau[i];
-    p.rpp = P.rpp[i]; p.rvv = P.rvv[i]; p.s = P.s[i];
-    p.chi = P.chi[i]; p.charge_ratio = P.charge_ratio[i];
-    p.beta0 = P.beta0[i]; p.p0c = P.p0c[i];
-    p.ax = P.ax ? P.ax[i] : 0.;
-    p.ay = P.ay ? P.ay[i] : 0.;
-    p.state = state0;
-    p.at_element = P.at_element[i];
-    p.at_turn = P.at_turn[i];
-    refresh_energy_cache(p);
-    int64_t const pid = (kp.flag_monitor != 0) ? P.particle_id[i] : 0;
+__device__ __forceinline__ void begin_turn(const TrackArgs& a, PState& p, int64_t i, int64_t pid) {
+    if (a.backtrack) {
+        if (a.flag_end_turn_actions > 0) {
+            // local_particle_custom_api.h:79-94
+            p.at_turn -= 1;
+            p.at_element = a.num_ele_line;
+            if (a.flag_reset_s > 0) p.s = a.line_length;
+        }
+    } else if (a.flag_monitor == 1) {
+        monitor(a, p, i, pid);
+    }
+}
 
+__device__ __forceinline__ void end_turn(const TrackArgs& a, PState& p, bool active, int64_t i,
+                                         int64_t pid) {
+    if (a.flag_monitor == 2) monitor(a, p, i, pid);
+    if (a.backtrack) {
+        if (a.flag_monitor == 1) monitor(a, p, i, pid);
+    } else if (a.flag_end_turn_actions > 0 && active) {
+        // local_particle_custom_api.h:67-76
+        p.at_turn += 1;
+        p.at_element = 0;
+        if (a.flag_reset_s > 0) p.s = 0.;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// the persistent push kernel
+// ---------------------------------------------------------------------------
+template <bool kExact>
+__global__ void __launch_bounds__(256, 1) track_kernel(const TrackArgs a) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ uint64_t full_bar[2];
+    __shared__ int s_item;
+    __shared__ int s_abort;
+    __shared__ int s_resident;       // lattice whose range is resident, or -1
+
+    int const tid = threadIdx.x;
+    bool const staged = a.chunk_bytes > 0;
+    if (tid == 0) {
+        mbar_init(&full_bar[0], 1);
+        mbar_init(&full_bar[1], 1);
+        mbar_fence_init();
+        s_abort = 0;
+        s_resident = -1;
+    }
+    __syncthreads();
+    uint32_t phase[2] = {0u, 0u};   // parity of the next completion of each buffer
+    uint32_t pending = 0u;          // thread 0: buffers with a copy in flight
+
+    const xtg_particles& P = a.P;
     RfCtx rf;
     rf.q0 = P.q0;
     rf.t_sim = P.t_sim;
-    rf.line_length = kp.line_length;
-    rf.kill = flag_on(kp.track_flags, XTG_FLAG_KILL_CAVITY_KICK);
-    rf.preserve_angle = kp.preserve_angle != 0;
-    bool const ignore_global = flag_on(kp.track_flags, XTG_FLAG_IGNORE_GLOBAL_APERTURE) || !kp.has_global;
-    double const lim = kp.global_lim;
-    int64_t const incr = kp.backtrack ? -1 : 1;
+    rf.line_length = a.line_length;
+    rf.kill = flag_on(a.track_flags, XTG_FLAG_KILL_CAVITY_KICK);
+    rf.preserve_angle = a.preserve_angle != 0;
+    bool const ignore_global = flag_on(a.track_flags, XTG_FLAG_IGNORE_GLOBAL_APERTURE) || !a.has_global;
 
-    bool active = true;
-    for (int32_t iturn = 0; iturn < kp.num_turns && active; iturn++) {
-        if (kp.backtrack) {
-            if (kp.flag_end_turn_actions > 0) {
-                // local_particle_custom_api.h:79-94
-                p.at_turn -= 1;
-                p.at_element = kp.num_ele_line;
-                if (kp.flag_reset_s > 0) p.s = kp.line_length;
-            }
-        } else if (kp.flag_monitor == 1) {
-            monitor(kp, p, i, pid);
+    for (;;) {
+        if (tid == 0) s_item = atomicAdd(a.item_counter, 1);
+        __syncthreads();
+        int const it = s_item;
+        int const nit = *((volatile const int32_t*)a.n_items);
+        __syncthreads();
+        if (it >= nit) break;
+        int4 const w = a.items[it];
+        int const lat = w.x;
+
+        // load the particle
+        bool const have = tid < w.z;
+        int64_t const i = have ? (int64_t)a.idx[w.y + tid] : 0;
+        PState p;
+        bool active = false;
+        int64_t pid = 0;
+        if (have) {
+            p.state = P.state[i];
+            active = p.state > 0;
         }
-        const unsigned char* __restrict__ rec = kp.table + kp.rec_begin;
-        for (int32_t e = 0; e < kp.rec_count; e++) {
-            if (kp.flag_monitor == 2) monitor(kp, p, i, pid);
-            bool const thick = apply_record<kExact>(p, rec, kp, rf);
-            if (thick && !ignore_global) {
-                // local_particle_custom_api.h:259-287
-                bool const within = (p.x >= -lim) && (p.x <= lim) && (p.y >= -lim) && (p.y <= lim);
-                if (p.state > 0 && !within) p.state = -1;
-            }
-            if (p.state <= 0) {
-                active = false;
-                break;
-            }
-            p.at_element += incr;
-            rec += reinterpret_cast<const RecHeader*>(rec)->nbytes;
+        if (active) {
+            p.x = P.x[i]; p.px = P.px[i]; p.y = P.y[i]; p.py = P.py[i];
+            p.zeta = P.zeta[i]; p.delta = P.delta[i]; p.ptau = P.ptau[i];
+            p.rpp = P.rpp[i]; p.rvv = P.rvv[i]; p.s = P.s[i];
+            p.chi = P.chi[i]; p.charge_ratio = P.charge_ratio[i];
+            p.beta0 = P.beta0[i]; p.p0c = P.p0c[i];
+            p.ax = P.ax ? P.ax[i] : 0.;
+            p.ay = P.ay ? P.ay[i] : 0.;
+            p.at_element = P.at_element[i];
+            p.at_turn = P.at_turn[i];
+            p.chi_one = (p.chi == 1.0);
+            refresh_energy_cache(p);
+            if (a.flag_monitor != 0) pid = P.particle_id[i];
         }
-        if (kp.flag_monitor == 2) monitor(kp, p, i, pid);
-        if (kp.backtrack) {
-            if (kp.flag_monitor == 1) monitor(kp, p, i, pid);
-        } else if (kp.flag_end_turn_actions > 0 && active) {
-            // local_particle_custom_api.h:67-76
-            p.at_turn += 1;
-            p.at_element = 0;
-            if (kp.flag_reset_s > 0) p.s = 0.;
+        bool const touched = active;
+
+        const unsigned char* base = a.table + a.lat_base[lat];
+        const int64_t* off = a.rec_off + (int64_t)lat * a.stride;
+        int32_t const r0 = a.rec_first, r1 = a.rec_first + a.rec_count;
+        int64_t const b0 = off[r0];
+        int64_t const range_bytes = off[r1] - b0;
+        bool const streamed = staged && range_bytes > a.smem_bytes;
+        const int32_t* cend = a.chunk_end + (int64_t)lat * a.stride;
+        unsigned char* const buf1 = smem + a.chunk_bytes;
+
+        // where the records of a whole turn are read from when not streamed
+        const unsigned char* whole = base + b0;
+        if (staged && !streamed) {
+            // resident: one bulk copy of the whole range, reused by every turn
+            // and by every later work item of the same lattice
+            if (s_resident != lat) {
+                __syncthreads();   // no warp still reads the previous content
+                if (tid == 0 && range_bytes > 0) {
+                    issue_copy(smem, base + b0, (uint32_t)range_bytes, &full_bar[0]);
+                    pending |= 1u;
+                }
+                if (range_bytes > 0) {
+                    if (mbar_wait_bounded(&full_bar[0], phase[0], a.err)) {
+                        phase[0] ^= 1u;
+                        pending &= ~1u;
+                    } else {
+                        s_abort = 1;
+                    }
+                }
+                __syncthreads();
+                if (s_abort) {
+                    if (tid == 0) drain_copies(full_bar, phase, pending, a.err);
+                    return;
+                }
+                if (tid == 0) s_resident = lat;
+            }
+            whole = smem;
+        }
+        // producer cursor of the streamed pipeline (used by thread 0 only)
+        int32_t pt = 0, pr = r0;
+        if (streamed) {
+            __syncthreads();   // no warp still reads a resident copy
+            if (tid == 0) {
+                s_resident = -1;
+                for (int b = 0; b < 2 && pt < a.num_turns; b++) {
+                    int32_t e = cend[pr];
+                    if (e > r1) e = r1;
+                    issue_copy(b ? buf1 : smem, base + off[pr], (uint32_t)(off[e] - off[pr]), &full_bar[b]);
+                    pending |= 1u << b;
+                    pr = e;
+                    if (pr >= r1) {
+                        pr = r0;
+                        pt++;
+                    }
+                }
+            }
+        }
+        int32_t k = 0;   // chunk counter of this item (streamed)
+        for (int32_t t = 0; t < a.num_turns; t++) {
+            // a block whose particles are all lost stops early, unless it
+            // must keep the streamed pipeline in step
+            if (!streamed && !__syncthreads_or(active)) break;
+            bool const was_active = active;
+            if (active) begin_turn(a, p, i, pid);
+            int32_t cr = r0;
+            while (cr < r1) {
+                int32_t e = r1;
+                const unsigned char* sb = whole;
+                const unsigned char* se = whole + range_bytes;
+                int b = 0;
+                if (streamed) {
+                    b = k & 1;
+                    e = cend[cr];
+                    if (e > r1) e = r1;
+                    if (mbar_wait_bounded(&full_bar[b], phase[b], a.err)) {
+                        phase[b] ^= 1u;
+                        pending &= ~(1u << b);
+                    } else {
+                        s_abort = 1;
+                    }
+                    __syncthreads();
+                    if (s_abort) {
+                        if (tid == 0) drain_copies(full_bar, phase, pending, a.err);
+                        return;
+                    }
+                    sb = b ? buf1 : smem;
+                    se = sb + (off[e] - off[cr]);
+                }
+                if (active) walk<kExact>(p, active, sb, se, a, rf, ignore_global, i, pid);
+                if (streamed) {
+                    __syncthreads();   // buffer b consumed by every warp
+                    if (tid == 0 && pt < a.num_turns) {
+                        int32_t pe = cend[pr];
+                        if (pe > r1) pe = r1;
+                        issue_copy(b ? buf1 : smem, base + off[pr], (uint32_t)(off[pe] - off[pr]), &full_bar[b]);
+                        pending |= 1u << b;
+                        pr = pe;
+                        if (pr >= r1) {
+                            pr = r0;
+                            pt++;
+                        }
+                    }
+                    k++;
+                }
+                cr = e;
+            }
+            if (was_active) end_turn(a, p, active, i, pid);
+        }
+
+        // write back (inactive particles are left untouched, as in the reference)
+        if (touched) {
+            P.x[i] = p.x; P.px[i] = p.px; P.y[i] = p.y; P.py[i] = p.py;
+            P.zeta[i] = p.zeta; P.delta[i] = p.delta; P.ptau[i] = p.ptau;
+            P.rpp[i] = p.rpp; P.rvv[i] = p.rvv; P.s[i] = p.s;
+            if (P.ax) P.ax[i] = p.ax;
+            if (P.ay) P.ay[i] = p.ay;
+            P.state[i] = p.state;
+            P.at_element[i] = p.at_element;
+            P.at_turn[i] = p.at_turn;
         }
     }
+}
 
-    P.x[i] = p.x; P.px[i] = p.px; P.y[i] = p.y; P.py[i] = p.py;
-    P.zeta[i] = p.zeta; P.delta[i] = p.delta; P.ptau[i] = p.ptau;
-    P.rpp[i] = p.rpp; P.rvv[i] = p.rvv; P.s[i] = p.s;
-    if (P.ax) P.ax[i] = p.ax;
-    if (P.ay) P.ay[i] = p.ay;
-    P.state[i] = p.state;
-    P.at_element[i] = p.at_element;
-    P.at_turn[i] = p.at_turn;
+// ---------------------------------------------------------------------------
+// compaction and work queue
+// ---------------------------------------------------------------------------
+
+// Per-lattice particle counts over all slots, so that the index list of
+// lattice l lives in [lat_pbase[l], lat_pbase[l+1]).
+__global__ void count_lattices_kernel(const int32_t* __restrict__ lat, int64_t n, int32_t n_lat,
+                                      int32_t* lat_total, int32_t* err) {
+    int64_t const i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int32_t const l = lat[i];
+    if (l < 0 || l >= n_lat) {
+        atomicExch(err, XTG_DEV_ERR_LATTICE_INDEX);   // the particle is not tracked
+        return;
+    }
+    atomicAdd(&lat_total[l], 1);
+}
+
+__global__ void prefix_lattices_kernel(const int32_t* lat_total, int32_t n_lat, int64_t n,
+                                       int64_t* lat_pbase, int32_t single) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    if (single) {
+        lat_pbase[0] = 0;
+        lat_pbase[1] = n;
+        return;
+    }
+    int64_t acc = 0;
+    for (int32_t l = 0; l < n_lat; l++) {
+        lat_pbase[l] = acc;
+        acc += lat_total[l];
+    }
+    lat_pbase[n_lat] = acc;
+}
+
+// Lists the alive particles of each lattice. Lanes are grouped by lattice
+// (match_any); within a group a ballot gives each alive lane its rank (a
+// prefix sum of the ballot) and one atomic per group reserves the slots.
+__global__ void compact_kernel(const int64_t* __restrict__ state, const int32_t* __restrict__ lat,
+                               int64_t n, int32_t n_lat, const int64_t* __restrict__ lat_pbase,
+                               int32_t* lat_count, int32_t* __restrict__ idx) {
+    int64_t const i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int const lane = threadIdx.x & 31;
+    bool const in = i < n;
+    int32_t l = 0;
+    if (in && lat) l = lat[i];
+    bool const alive = in && state[i] > 0 && l >= 0 && l < n_lat;
+    unsigned const alive_mask = __ballot_sync(0xffffffffu, alive);
+    unsigned const group = __match_any_sync(0xffffffffu, alive ? l : -1) & alive_mask;
+    int32_t base = 0;
+    int const leader = alive ? (__ffs(group) - 1) : lane;
+    if (alive && lane == leader) base = atomicAdd(&lat_count[l], __popc(group));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (alive) {
+        int const rank = __popc(group & ((1u << lane) - 1u));
+        idx[lat_pbase[l] + base + rank] = (int32_t)i;
+    }
+}
+
+// Cuts each lattice's list into items of at most `block` particles and
+// resets the queue counter.
+__global__ void items_kernel(const int32_t* lat_count, const int64_t* lat_pbase, int32_t n_lat,
+                             int32_t block, int4* items, int32_t* n_items, int32_t* item_counter) {
+    if (threadIdx.x == 0) {
+        int32_t acc = 0;
+        for (int32_t l = 0; l < n_lat; l++) acc += (lat_count[l] + block - 1) / block;
+        *n_items = acc;
+        *item_counter = 0;
+    }
+    // one thread per lattice writes that lattice's items
+    for (int32_t l = threadIdx.x; l < n_lat; l += blockDim.x) {
+        int32_t first = 0;
+        for (int32_t q = 0; q < l; q++) first += (lat_count[q] + block - 1) / block;
+        int32_t const c = lat_count[l];
+        int32_t const ni = (c + block - 1) / block;
+        for (int32_t j = 0; j < ni; j++) {
+            int32_t const cnt = min(block, c - j * block);
+            items[first + j] = make_int4(l, (int32_t)(lat_pbase[l] + (int64_t)j * block), cnt, 0);
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -327,6 +638,409 @@ __global__ void dfma_probe_kernel(double* out, int iters, double a, double b) {
 }
 
 // ---------------------------------------------------------------------------
+// host side: device tables, workspace, execution context
+// ---------------------------------------------------------------------------
+struct DevTables {
+    unsigned char* d_bytes = nullptr;
+    int64_t* d_lat_base = nullptr;
+    int64_t* d_rec_off = nullptr;
+    int32_t* d_chunk_end = nullptr;
+    int32_t chunk_bytes_built = -1;
+    int32_t n_lat = 0;
+    int64_t n_rec = 0;                         // records per lattice
+    std::vector<int64_t> h_rec_off;            // n_lat * (n_rec + 1)
+    int64_t max_record = 0;
+    bool built = false;
+};
+
+static void free_tables(DevTables* t) {
+    if (t->d_bytes) cudaFree(t->d_bytes);
+    if (t->d_lat_base) cudaFree(t->d_lat_base);
+    if (t->d_rec_off) cudaFree(t->d_rec_off);
+    if (t->d_chunk_end) cudaFree(t->d_chunk_end);
+    *t = DevTables();
+}
+
+struct Workspace {
+    int64_t cap = 0;
+    int32_t n_lat_cap = 0;
+    int32_t* idx = nullptr;
+    int32_t* lat_total = nullptr;
+    int32_t* lat_count = nullptr;
+    int64_t* lat_pbase = nullptr;
+    int4* items = nullptr;
+    int64_t items_cap = 0;
+    int32_t* counters = nullptr;   // [0] n_items, [1] item_counter, [2] error word
+};
+
+static void free_ws(Workspace* w) {
+    cudaFree(w->idx);
+    cudaFree(w->lat_total);
+    cudaFree(w->lat_count);
+    cudaFree(w->lat_pbase);
+    cudaFree(w->items);
+    cudaFree(w->counters);
+    *w = Workspace();
+}
+
+struct ExecCtx {
+    std::vector<std::vector<xtg_element>> lattices;
+    xtg_config config;
+    int device = 0;
+    DevTables fwd, bwd;
+    Workspace ws;
+    xtg_tuning tune;
+    std::vector<double> flops;                 // per element (first lattice)
+    std::mutex mu;
+    ExecCtx() {
+        tune.block_size = 256;
+        tune.compact_every = 0;
+        tune.chunk_bytes = 49152;
+        tune.use_graph = 0;
+    }
+    ~ExecCtx() {
+        free_tables(&fwd);
+        free_tables(&bwd);
+        free_ws(&ws);
+    }
+};
+
+struct xtg_lattice {
+    ExecCtx ctx;
+};
+
+struct xtg_batch {
+    ExecCtx ctx;
+};
+
+static int32_t build_tables(ExecCtx* C, bool backtrack, DevTables* T) {
+    std::vector<unsigned char> bytes;
+    std::vector<int64_t> lat_base, rec_off;
+    int64_t n = -1;
+    int64_t max_rec = 0;
+    for (size_t l = 0; l < C->lattices.size(); l++) {
+        PackedLattice pl;
+        std::string err;
+        const auto& els = C->lattices[l];
+        int32_t st = pack_lattice(els.data(), (int64_t)els.size(), C->config, backtrack, &pl, &err);
+        if (st != XTG_OK) return set_error(st, "lattice %zu: %s", l, err.c_str());
+        if (n < 0) {
+            n = (int64_t)els.size();
+            if (!backtrack) C->flops = pl.flops_fast;
+        }
+        lat_base.push_back((int64_t)bytes.size());
+        bytes.insert(bytes.end(), pl.bytes.begin(), pl.bytes.end());
+        rec_off.insert(rec_off.end(), pl.offsets.begin(), pl.offsets.end());
+        for (int64_t r = 0; r < n; r++) max_rec = std::max(max_rec, pl.offsets[r + 1] - pl.offsets[r]);
+    }
+    free_tables(T);
+    T->n_lat = (int32_t)C->lattices.size();
+    T->n_rec = n;
+    T->h_rec_off = rec_off;
+    T->max_record = max_rec;
+    size_t const nb = bytes.empty() ? 16 : bytes.size();
+    XTG_CUDA_CHECK(cudaMalloc(&T->d_bytes, nb));
+    if (!bytes.empty()) XTG_CUDA_CHECK(cudaMemcpy(T->d_bytes, bytes.data(), bytes.size(), cudaMemcpyHostToDevice));
+    XTG_CUDA_CHECK(cudaMalloc(&T->d_lat_base, lat_base.size() * sizeof(int64_t)));
+    XTG_CUDA_CHECK(cudaMemcpy(T->d_lat_base, lat_base.data(), lat_base.size() * sizeof(int64_t),
+                              cudaMemcpyHostToDevice));
+    XTG_CUDA_CHECK(cudaMalloc(&T->d_rec_off, rec_off.size() * sizeof(int64_t)));
+    XTG_CUDA_CHECK(cudaMemcpy(T->d_rec_off, rec_off.data(), rec_off.size() * sizeof(int64_t),
+                              cudaMemcpyHostToDevice));
+    T->built = true;
+    T->chunk_bytes_built = -1;
+    return XTG_OK;
+}
+
+// chunk_end[r]: the largest r' > r with off[r'] - off[r] <= chunk (records
+// are never split; every record fits in a chunk, checked by the caller).
+static int32_t build_chunks(DevTables* T, int32_t chunk) {
+    if (T->chunk_bytes_built == chunk) return XTG_OK;
+    int64_t const stride = T->n_rec + 1;
+    std::vector<int32_t> ce((size_t)(stride * T->n_lat));
+    for (int32_t l = 0; l < T->n_lat; l++) {
+        const int64_t* off = T->h_rec_off.data() + l * stride;
+        int64_t e = 0;
+        for (int64_t r = 0; r <= T->n_rec; r++) {
+            if (r == T->n_rec) {
+                ce[l * stride + r] = (int32_t)T->n_rec;
+                continue;
+            }
+            if (e < r + 1) e = r + 1;
+            while (e < T->n_rec && off[e + 1] - off[r] <= chunk) e++;
+            ce[l * stride + r] = (int32_t)e;
+        }
+    }
+    if (T->d_chunk_end) cudaFree(T->d_chunk_end);
+    T->d_chunk_end = nullptr;
+    XTG_CUDA_CHECK(cudaMalloc(&T->d_chunk_end, ce.size() * sizeof(int32_t)));
+    XTG_CUDA_CHECK(cudaMemcpy(T->d_chunk_end, ce.data(), ce.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    T->chunk_bytes_built = chunk;
+    return XTG_OK;
+}
+
+static int32_t ensure_ws(Workspace* W, int64_t cap, int32_t n_lat) {
+    if (cap > W->cap) {
+        if (W->idx) cudaFree(W->idx);
+        W->idx = nullptr;
+        XTG_CUDA_CHECK(cudaMalloc(&W->idx, (size_t)std::max<int64_t>(cap, 1) * sizeof(int32_t)));
+        W->cap = cap;
+    }
+    int64_t const items_needed = (cap + 63) / 64 + n_lat + 1;   // blocks of >= 64 threads
+    if (items_needed > W->items_cap) {
+        if (W->items) cudaFree(W->items);
+        W->items = nullptr;
+        XTG_CUDA_CHECK(cudaMalloc(&W->items, (size_t)items_needed * sizeof(int4)));
+        W->items_cap = items_needed;
+    }
+    if (n_lat > W->n_lat_cap) {
+        cudaFree(W->lat_total);
+        cudaFree(W->lat_count);
+        cudaFree(W->lat_pbase);
+        W->lat_total = W->lat_count = nullptr;
+        W->lat_pbase = nullptr;
+        XTG_CUDA_CHECK(cudaMalloc(&W->lat_total, n_lat * sizeof(int32_t)));
+        XTG_CUDA_CHECK(cudaMalloc(&W->lat_count, n_lat * sizeof(int32_t)));
+        XTG_CUDA_CHECK(cudaMalloc(&W->lat_pbase, (n_lat + 1) * sizeof(int64_t)));
+        W->n_lat_cap = n_lat;
+    }
+    if (!W->counters) {
+        XTG_CUDA_CHECK(cudaMalloc(&W->counters, 4 * sizeof(int32_t)));
+        XTG_CUDA_CHECK(cudaMemset(W->counters, 0, 4 * sizeof(int32_t)));
+    }
+    return XTG_OK;
+}
+
+static bool particles_complete(const xtg_particles* P) {
+    return P->x && P->px && P->y && P->py && P->zeta && P->delta && P->ptau && P->rpp && P->rvv && P->s &&
+           P->chi && P->charge_ratio && P->beta0 && P->p0c && P->state && P->at_element && P->at_turn &&
+           P->particle_id;
+}
+
+template <bool kExact>
+static int32_t configure_kernel(int32_t smem) {
+    static int32_t configured = -1;
+    if (configured < smem) {
+        XTG_CUDA_CHECK(cudaFuncSetAttribute(track_kernel<kExact>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            smem));
+        configured = smem;
+    }
+    return XTG_OK;
+}
+
+template <bool kExact>
+static int32_t persistent_grid(int32_t block, int32_t smem, int* grid) {
+    int dev = 0, sms = 0, per_sm = 0;
+    XTG_CUDA_CHECK(cudaGetDevice(&dev));
+    XTG_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    XTG_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, track_kernel<kExact>, block, smem));
+    if (per_sm < 1)
+        return set_error(XTG_E_VALUE, "block size %d with %d B of shared memory does not fit", block, smem);
+    *grid = per_sm * sms;
+    return XTG_OK;
+}
+
+// One round: compact the alive particles, build the work queue, push
+// `a.num_turns` turns. All on `s`, no host synchronization.
+template <bool kExact>
+static int32_t launch_round(ExecCtx* C, const TrackArgs& a, const int32_t* lat, int64_t cap, int32_t block,
+                            int grid, int32_t smem, cudaStream_t s) {
+    Workspace& W = C->ws;
+    int32_t const n_lat = C->fwd.n_lat;
+    XTG_CUDA_CHECK(cudaMemsetAsync(W.lat_count, 0, n_lat * sizeof(int32_t), s));
+    int64_t const cgrid = (cap + 255) / 256;
+    compact_kernel<<<(unsigned)cgrid, 256, 0, s>>>(a.P.state, lat, cap, n_lat, W.lat_pbase, W.lat_count, W.idx);
+    items_kernel<<<1, 256, 0, s>>>(W.lat_count, W.lat_pbase, n_lat, block, W.items, W.counters + 0,
+                                   W.counters + 1);
+    track_kernel<kExact><<<grid, block, smem, s>>>(a);
+    g_launch_count.fetch_add(3);
+    XTG_CUDA_CHECK(cudaGetLastError());
+    return XTG_OK;
+}
+
+template <bool kExact>
+static int32_t run_rounds(ExecCtx* C, TrackArgs a, const int32_t* lat, int64_t cap, int32_t num_turns,
+                          cudaStream_t s) {
+    int32_t const block = C->tune.block_size;
+    int32_t smem = 0;
+    if (a.chunk_bytes > 0) {
+        smem = 2 * a.chunk_bytes;
+        int32_t st = configure_kernel<kExact>(smem);
+        if (st != XTG_OK) return st;
+    }
+    a.smem_bytes = smem;
+    int grid = 0;
+    int32_t st = persistent_grid<kExact>(block, smem, &grid);
+    if (st != XTG_OK) return st;
+    int32_t const per = C->tune.compact_every > 0 ? std::min(C->tune.compact_every, num_turns) : num_turns;
+    int32_t const full = num_turns / per;
+    int32_t const rest = num_turns % per;
+    a.num_turns = per;
+    if (C->tune.use_graph && full > 1) {
+        // capture one round on a side stream and replay it `full` times
+        cudaStream_t cs = nullptr;
+        cudaEvent_t ev = nullptr;
+        cudaGraph_t g = nullptr;
+        cudaGraphExec_t ex = nullptr;
+        XTG_CUDA_CHECK(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+        XTG_CUDA_CHECK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        XTG_CUDA_CHECK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+        st = launch_round<kExact>(C, a, lat, cap, block, grid, smem, cs);
+        cudaError_t ce = cudaStreamEndCapture(cs, &g);
+        if (st == XTG_OK && ce == cudaSuccess) ce = cudaGraphInstantiate(&ex, g, 0);
+        if (g) cudaGraphDestroy(g);
+        if (st == XTG_OK && ce == cudaSuccess) {
+            g_launch_count.fetch_sub(3);   // counted per replay below
+            for (int32_t r = 0; r < full && ce == cudaSuccess; r++) {
+                ce = cudaGraphLaunch(ex, s);
+                g_launch_count.fetch_add(3);
+            }
+        }
+        if (ex) cudaGraphExecDestroy(ex);
+        cudaStreamDestroy(cs);
+        cudaEventDestroy(ev);
+        if (st != XTG_OK) return st;
+        if (ce != cudaSuccess) return set_error(XTG_E_CUDA, "graph replay failed: %s", cudaGetErrorString(ce));
+    } else {
+        for (int32_t r = 0; r < full; r++) {
+            st = launch_round<kExact>(C, a, lat, cap, block, grid, smem, s);
+            if (st != XTG_OK) return st;
+        }
+    }
+    if (rest > 0) {
+        a.num_turns = rest;
+        st = launch_round<kExact>(C, a, lat, cap, block, grid, smem, s);
+        if (st != XTG_OK) return st;
+    }
+    return XTG_OK;
+}
+
+static int32_t track_impl(ExecCtx* C, const xtg_particles* particles, const int32_t* lattice_index,
+                          int32_t num_turns, int32_t ele_start, int32_t num_ele_track,
+                          int32_t flag_end_turn_actions, int32_t flag_reset_s_at_end_turn,
+                          int32_t flag_monitor, int32_t num_ele_line, double line_length,
+                          const xtg_monitor* monitor, uint64_t track_flags, void* stream) {
+    if (!particles) return set_error(XTG_E_NULL, "xtg_track: NULL particles");
+    if (!particles_complete(particles)) return set_error(XTG_E_NULL, "xtg_track: a required particle array is NULL");
+    int64_t const n = C->fwd.n_rec;
+    if (num_turns < 0) return set_error(XTG_E_VALUE, "xtg_track: num_turns < 0");
+    if (ele_start < 0 || num_ele_track < 0 || (int64_t)ele_start + num_ele_track > n)
+        return set_error(XTG_E_VALUE, "xtg_track: element range [%d, %d+%d) outside [0, %lld)", ele_start,
+                         ele_start, num_ele_track, (long long)n);
+    if (flag_monitor < 0 || flag_monitor > 2)
+        return set_error(XTG_E_VALUE, "xtg_track: flag_monitor must be 0, 1 or 2");
+    if (flag_monitor != 0 && !monitor)
+        return set_error(XTG_E_NULL, "xtg_track: flag_monitor set but monitor is NULL");
+    if (monitor && flag_monitor != 0) {
+        if (monitor->n_repetitions > 1 && monitor->repetition_period <= 0)
+            return set_error(XTG_E_VALUE, "xtg_track: repetition_period must be > 0");
+        if (monitor->n_records < 0) return set_error(XTG_E_VALUE, "xtg_track: monitor n_records < 0");
+    }
+    int64_t const cap = particles->capacity;
+    if (cap < 0) return set_error(XTG_E_VALUE, "xtg_track: capacity < 0");
+    if (cap > (int64_t)INT32_MAX - 1024) return set_error(XTG_E_CAPACITY, "xtg_track: capacity above 2^31");
+    if (cap == 0 || num_turns == 0) return XTG_OK;
+    int cur = 0;
+    XTG_CUDA_CHECK(cudaGetDevice(&cur));
+    if (cur != C->device)
+        return set_error(XTG_E_VALUE, "xtg_track: tables were built on device %d, current is %d", C->device, cur);
+
+    std::lock_guard<std::mutex> lock(C->mu);
+    bool const backtrack = (track_flags >> XTG_FLAG_BACKTRACK) & 1u;
+    DevTables* T = &C->fwd;
+    int32_t rec_first = ele_start;
+    if (backtrack) {
+        if (!C->bwd.built) {
+            int32_t st = build_tables(C, true, &C->bwd);
+            if (st != XTG_OK) return st;
+        }
+        T = &C->bwd;
+        rec_first = (int32_t)(n - ((int64_t)ele_start + num_ele_track));
+    }
+    // a chunk holds at least the largest record (records are never split)
+    int32_t chunk = C->tune.chunk_bytes;
+    if (chunk > 0) {
+        if (T->max_record > chunk) chunk = (int32_t)((T->max_record + 15) / 16 * 16);
+        if (chunk > kMaxChunkBytes)
+            return set_error(XTG_E_CAPACITY, "an element record (%lld B) exceeds the staging limit (%d B)",
+                             (long long)T->max_record, kMaxChunkBytes);
+        int32_t st = build_chunks(T, chunk);
+        if (st != XTG_OK) return st;
+    }
+    int32_t const n_lat = T->n_lat;
+    int32_t st = ensure_ws(&C->ws, cap, n_lat);
+    if (st != XTG_OK) return st;
+    Workspace& W = C->ws;
+    cudaStream_t s = (cudaStream_t)stream;
+
+    // per-lattice regions of the index list
+    const int32_t* lat = (lattice_index && n_lat > 1) ? lattice_index : nullptr;
+    if (lat) {
+        XTG_CUDA_CHECK(cudaMemsetAsync(W.lat_total, 0, n_lat * sizeof(int32_t), s));
+        count_lattices_kernel<<<(unsigned)((cap + 255) / 256), 256, 0, s>>>(lat, cap, n_lat, W.lat_total,
+                                                                              W.counters + 2);
+        prefix_lattices_kernel<<<1, 32, 0, s>>>(W.lat_total, n_lat, cap, W.lat_pbase, 0);
+        g_launch_count.fetch_add(2);
+    } else {
+        prefix_lattices_kernel<<<1, 32, 0, s>>>(W.lat_total, 1, cap, W.lat_pbase, 1);
+        g_launch_count.fetch_add(1);
+    }
+    XTG_CUDA_CHECK(cudaGetLastError());
+
+    TrackArgs a;
+    memset(&a, 0, sizeof(a));
+    a.table = T->d_bytes;
+    a.lat_base = T->d_lat_base;
+    a.rec_off = T->d_rec_off;
+    a.chunk_end = T->d_chunk_end;
+    a.stride = T->n_rec + 1;
+    a.rec_first = rec_first;
+    a.rec_count = num_ele_track;
+    a.chunk_bytes = chunk;
+    a.flag_monitor = flag_monitor;
+    a.flag_end_turn_actions = flag_end_turn_actions;
+    a.flag_reset_s = flag_reset_s_at_end_turn;
+    a.backtrack = backtrack ? 1 : 0;
+    a.has_global = C->config.has_global_xy_limit;
+    a.preserve_angle = C->config.cavity_preserve_angle;
+    a.global_lim = C->config.global_xy_limit;
+    a.num_ele_line = num_ele_line;
+    a.line_length = line_length;
+    a.track_flags = track_flags;
+    a.idx = W.idx;
+    a.items = W.items;
+    a.n_items = W.counters + 0;
+    a.item_counter = W.counters + 1;
+    a.err = W.counters + 2;
+    a.P = *particles;
+    if (monitor) a.M = *monitor;
+
+    if (C->config.arith == XTG_ARITH_EXACT) return run_rounds<true>(C, a, lat, cap, num_turns, s);
+    return run_rounds<false>(C, a, lat, cap, num_turns, s);
+}
+
+static int32_t read_device_status(const ExecCtx* C) {
+    if (!C->ws.counters) return XTG_OK;
+    int32_t h[4] = {0, 0, 0, 0};
+    XTG_CUDA_CHECK(cudaDeviceSynchronize());
+    XTG_CUDA_CHECK(cudaMemcpy(h, C->ws.counters, sizeof(h), cudaMemcpyDeviceToHost));
+    if (h[2] != 0) XTG_CUDA_CHECK(cudaMemset(C->ws.counters + 2, 0, sizeof(int32_t)));
+    if (h[2] == XTG_DEV_ERR_TIMEOUT) return set_error(XTG_E_TIMEOUT, "a bounded device wait timed out");
+    if (h[2] == XTG_DEV_ERR_LATTICE_INDEX)
+        return set_error(XTG_E_VALUE, "a particle has a lattice index outside the batch");
+    return XTG_OK;
+}
+
+static int32_t check_tuning(const xtg_tuning* t) {
+    if (!(t->block_size == 64 || t->block_size == 128 || t->block_size == 256))
+        return set_error(XTG_E_VALUE, "block_size must be 64, 128 or 256");
+    if (t->compact_every < 0) return set_error(XTG_E_VALUE, "compact_every must be >= 0");
+    if (t->chunk_bytes < 0 || t->chunk_bytes % 16 || t->chunk_bytes > kMaxChunkBytes)
+        return set_error(XTG_E_VALUE, "chunk_bytes must be a multiple of 16 in [0, %d]", kMaxChunkBytes);
+    return XTG_OK;
+}
+
+// ---------------------------------------------------------------------------
 // C-ABI
 // ---------------------------------------------------------------------------
 extern "C" {
@@ -341,38 +1055,39 @@ int32_t xtg_get_last_error(char* buf, int64_t n) {
 
 int64_t xtg_launch_count(void) { return g_launch_count.load(); }
 
+// launches of the other translation units of the library (not exported)
+__attribute__((visibility("hidden"))) int64_t xtg_internal_launch_add(int64_t n) {
+    return g_launch_count.fetch_add(n) + n;
+}
+
 int32_t xtg_lattice_create(const xtg_element* elements, int64_t n_elements, const xtg_config* config,
                            xtg_lattice** out) {
     if (!out || !config) return set_error(XTG_E_NULL, "xtg_lattice_create: NULL argument");
     *out = nullptr;
     if (n_elements < 0) return set_error(XTG_E_VALUE, "xtg_lattice_create: n_elements < 0");
     if (n_elements > 0 && !elements) return set_error(XTG_E_NULL, "xtg_lattice_create: elements is NULL");
-    if (n_elements > (int64_t)INT32_MAX) return set_error(XTG_E_CAPACITY, "too many elements");
+    if (n_elements > (int64_t)INT32_MAX - 1) return set_error(XTG_E_CAPACITY, "too many elements");
     if (config->arith != XTG_ARITH_EXACT && config->arith != XTG_ARITH_FAST)
         return set_error(XTG_E_VALUE, "xtg_config.arith must be XTG_ARITH_EXACT or XTG_ARITH_FAST");
-    std::unique_ptr<xtg_lattice> L(new xtg_lattice());
-    L->elements.assign(elements, elements + n_elements);
-    L->config = *config;
     // validate and pack before touching the device, so that an unsupported
     // element is reported as such on any host
-    PackedLattice pl;
-    std::string err;
-    int32_t st = pack_lattice(L->elements.data(), n_elements, L->config, false, &pl, &err);
-    if (st != XTG_OK) return set_error(st, "%s", err.c_str());
-    XTG_CUDA_CHECK(cudaGetDevice(&L->device));
-    st = upload_table(pl, &L->fwd);
-    if (st != XTG_OK) {
-        free_table(&L->fwd);
-        return st;
+    {
+        PackedLattice pl;
+        std::string err;
+        int32_t st = pack_lattice(elements, n_elements, *config, false, &pl, &err);
+        if (st != XTG_OK) return set_error(st, "%s", err.c_str());
     }
+    std::unique_ptr<xtg_lattice> L(new xtg_lattice());
+    L->ctx.lattices.emplace_back(elements, elements + n_elements);
+    L->ctx.config = *config;
+    XTG_CUDA_CHECK(cudaGetDevice(&L->ctx.device));
+    int32_t st = build_tables(&L->ctx, false, &L->ctx.fwd);
+    if (st != XTG_OK) return st;
     *out = L.release();
     return XTG_OK;
 }
 
 int32_t xtg_lattice_destroy(xtg_lattice* lattice) {
-    if (!lattice) return XTG_OK;
-    free_table(&lattice->fwd);
-    free_table(&lattice->bwd);
     delete lattice;
     return XTG_OK;
 }
@@ -380,31 +1095,35 @@ int32_t xtg_lattice_destroy(xtg_lattice* lattice) {
 int32_t xtg_lattice_info(const xtg_lattice* L, int64_t* n_elements, int64_t ele_start, int64_t num_ele,
                          double* flops_per_particle) {
     if (!L) return set_error(XTG_E_NULL, "xtg_lattice_info: NULL lattice");
-    int64_t const n = (int64_t)L->elements.size();
+    int64_t const n = L->ctx.fwd.n_rec;
     if (n_elements) *n_elements = n;
     if (flops_per_particle) {
         if (ele_start < 0 || num_ele < 0 || ele_start + num_ele > n)
             return set_error(XTG_E_VALUE, "xtg_lattice_info: element range out of bounds");
         double f = 0;
-        for (int64_t k = ele_start; k < ele_start + num_ele; k++) f += L->fwd.flops[k];
+        for (int64_t k = ele_start; k < ele_start + num_ele; k++) f += L->ctx.flops[k];
         *flops_per_particle = f;
     }
     return XTG_OK;
 }
 
-int32_t xtg_set_launch_config(xtg_lattice* L, int32_t block_size, int32_t compact_every, int32_t* out_bs,
-                              int32_t* out_ce) {
-    if (!L) return set_error(XTG_E_NULL, "xtg_set_launch_config: NULL lattice");
-    if (block_size != 0) {
-        if (block_size < 32 || block_size > 256 || block_size % 32)
-            return set_error(XTG_E_VALUE, "block_size must be a multiple of 32 in [32, 256]");
-        L->block_size = block_size;
-    }
-    if (compact_every < 0) return set_error(XTG_E_VALUE, "compact_every must be >= 0");
-    if (compact_every > 0) L->compact_every = compact_every;
-    if (out_bs) *out_bs = L->block_size;
-    if (out_ce) *out_ce = L->compact_every;
+int32_t xtg_get_tuning(const xtg_lattice* L, xtg_tuning* out) {
+    if (!L || !out) return set_error(XTG_E_NULL, "xtg_get_tuning: NULL argument");
+    *out = L->ctx.tune;
     return XTG_OK;
+}
+
+int32_t xtg_set_tuning(xtg_lattice* L, const xtg_tuning* t) {
+    if (!L || !t) return set_error(XTG_E_NULL, "xtg_set_tuning: NULL argument");
+    int32_t st = check_tuning(t);
+    if (st != XTG_OK) return st;
+    L->ctx.tune = *t;
+    return XTG_OK;
+}
+
+int32_t xtg_device_status(const xtg_lattice* L) {
+    if (!L) return set_error(XTG_E_NULL, "xtg_device_status: NULL lattice");
+    return read_device_status(&L->ctx);
 }
 
 int32_t xtg_sync(void* stream) {
@@ -412,90 +1131,79 @@ int32_t xtg_sync(void* stream) {
     return XTG_OK;
 }
 
-static bool particles_complete(const xtg_particles* P) {
-    return P->x && P->px && P->y && P->py && P->zeta && P->delta && P->ptau && P->rpp && P->rvv && P->s &&
-           P->chi && P->charge_ratio && P->beta0 && P->p0c && P->state && P->at_element && P->at_turn &&
-           P->particle_id;
-}
-
 int32_t xtg_track(const xtg_lattice* lattice, const xtg_particles* particles, int32_t num_turns,
                   int32_t ele_start, int32_t num_ele_track, int32_t flag_end_turn_actions,
                   int32_t flag_reset_s_at_end_turn, int32_t flag_monitor, int32_t num_ele_line,
                   double line_length, const xtg_monitor* monitor, uint64_t track_flags, void* stream) {
     if (!lattice || !particles) return set_error(XTG_E_NULL, "xtg_track: NULL lattice or particles");
-    xtg_lattice* L = const_cast<xtg_lattice*>(lattice);
-    if (!particles_complete(particles)) return set_error(XTG_E_NULL, "xtg_track: a required particle array is NULL");
-    int64_t const n = (int64_t)L->elements.size();
-    if (num_turns < 0) return set_error(XTG_E_VALUE, "xtg_track: num_turns < 0");
-    if (ele_start < 0 || num_ele_track < 0 || (int64_t)ele_start + num_ele_track > n)
-        return set_error(XTG_E_VALUE, "xtg_track: element range [%d, %d+%d) outside [0, %lld)", ele_start,
-                         ele_start, num_ele_track, (long long)n);
-    if (flag_monitor < 0 || flag_monitor > 2) return set_error(XTG_E_VALUE, "xtg_track: flag_monitor must be 0, 1 or 2");
-    if (flag_monitor != 0 && !monitor) return set_error(XTG_E_NULL, "xtg_track: flag_monitor set but monitor is NULL");
-    if (monitor && flag_monitor != 0) {
-        if (monitor->n_repetitions > 1 && monitor->repetition_period <= 0)
-            return set_error(XTG_E_VALUE, "xtg_track: repetition_period must be > 0");
-        if (monitor->n_records < 0) return set_error(XTG_E_VALUE, "xtg_track: monitor n_records < 0");
-    }
-    if (particles->capacity < 0) return set_error(XTG_E_VALUE, "xtg_track: capacity < 0");
-    if (particles->capacity == 0 || num_turns == 0) return XTG_OK;
+    ExecCtx* C = &const_cast<xtg_lattice*>(lattice)->ctx;
+    return track_impl(C, particles, nullptr, num_turns, ele_start, num_ele_track, flag_end_turn_actions,
+                      flag_reset_s_at_end_turn, flag_monitor, num_ele_line, line_length, monitor, track_flags,
+                      stream);
+}
 
-    int cur = 0;
-    XTG_CUDA_CHECK(cudaGetDevice(&cur));
-    if (cur != L->device) return set_error(XTG_E_VALUE, "xtg_track: lattice was built on device %d, current is %d", L->device, cur);
-
-    bool const backtrack = (track_flags >> XTG_FLAG_BACKTRACK) & 1u;
-    const DevTable* T = &L->fwd;
-    int64_t rec_first = ele_start;
-    if (backtrack) {
-        std::lock_guard<std::mutex> lock(L->mu);
-        if (!L->has_bwd) {
-            PackedLattice pl;
-            std::string err;
-            int32_t st = pack_lattice(L->elements.data(), n, L->config, true, &pl, &err);
-            if (st != XTG_OK) return set_error(st, "%s", err.c_str());
-            st = upload_table(pl, &L->bwd);
-            if (st != XTG_OK) return st;
-            L->has_bwd = true;
+int32_t xtg_batch_create(const xtg_lattice* const* lattices, int32_t n_lattices, xtg_batch** out) {
+    if (!lattices || !out) return set_error(XTG_E_NULL, "xtg_batch_create: NULL argument");
+    *out = nullptr;
+    if (n_lattices < 1) return set_error(XTG_E_VALUE, "xtg_batch_create: no lattices");
+    std::unique_ptr<xtg_batch> B(new xtg_batch());
+    for (int32_t l = 0; l < n_lattices; l++) {
+        if (!lattices[l]) return set_error(XTG_E_NULL, "xtg_batch_create: lattice %d is NULL", l);
+        const ExecCtx& c = lattices[l]->ctx;
+        if (l == 0) {
+            B->ctx.config = c.config;
+            B->ctx.device = c.device;
+            B->ctx.tune = c.tune;
+        } else {
+            if (c.lattices[0].size() != B->ctx.lattices[0].size())
+                return set_error(XTG_E_VALUE, "xtg_batch_create: lattice %d has %zu elements, lattice 0 %zu", l,
+                                 c.lattices[0].size(), B->ctx.lattices[0].size());
+            if (memcmp(&c.config, &B->ctx.config, sizeof(xtg_config)) != 0)
+                return set_error(XTG_E_VALUE, "xtg_batch_create: lattice %d has a different config", l);
         }
-        T = &L->bwd;
-        // reference order ele_stop-1 .. ele_start == reversed-table records
-        rec_first = n - ((int64_t)ele_start + num_ele_track);
+        B->ctx.lattices.push_back(c.lattices[0]);
     }
-
-    KParams kp;
-    memset(&kp, 0, sizeof(kp));
-    kp.table = T->d_bytes;
-    kp.rec_begin = T->h_offsets[rec_first];
-    kp.rec_count = num_ele_track;
-    kp.capacity = particles->capacity;
-    kp.P = *particles;
-    if (monitor) kp.M = *monitor;
-    kp.flag_monitor = flag_monitor;
-    kp.flag_end_turn_actions = flag_end_turn_actions;
-    kp.flag_reset_s = flag_reset_s_at_end_turn;
-    kp.backtrack = backtrack ? 1 : 0;
-    kp.num_ele_line = num_ele_line;
-    kp.line_length = line_length;
-    kp.track_flags = track_flags;
-    kp.has_global = L->config.has_global_xy_limit;
-    kp.preserve_angle = L->config.cavity_preserve_angle;
-    kp.global_lim = L->config.global_xy_limit;
-
-    cudaStream_t s = (cudaStream_t)stream;
-    int const bs = L->block_size;
-    int64_t const grid64 = (kp.capacity + bs - 1) / bs;
-    if (grid64 > INT32_MAX) return set_error(XTG_E_CAPACITY, "xtg_track: too many particles");
-    dim3 grid((unsigned)grid64), block(bs);
-    int32_t const per_launch = L->compact_every > 0 ? L->compact_every : num_turns;
-    for (int32_t t = 0; t < num_turns; t += per_launch) {
-        kp.num_turns = (num_turns - t) < per_launch ? (num_turns - t) : per_launch;
-        if (L->config.arith == XTG_ARITH_EXACT) track_kernel<true><<<grid, block, 0, s>>>(kp);
-        else track_kernel<false><<<grid, block, 0, s>>>(kp);
-        g_launch_count.fetch_add(1);
-        XTG_CUDA_CHECK(cudaGetLastError());
-    }
+    int32_t st = build_tables(&B->ctx, false, &B->ctx.fwd);
+    if (st != XTG_OK) return st;
+    *out = B.release();
     return XTG_OK;
+}
+
+int32_t xtg_batch_destroy(xtg_batch* batch) {
+    delete batch;
+    return XTG_OK;
+}
+
+int32_t xtg_batch_get_tuning(const xtg_batch* B, xtg_tuning* out) {
+    if (!B || !out) return set_error(XTG_E_NULL, "xtg_batch_get_tuning: NULL argument");
+    *out = B->ctx.tune;
+    return XTG_OK;
+}
+
+int32_t xtg_batch_set_tuning(xtg_batch* B, const xtg_tuning* t) {
+    if (!B || !t) return set_error(XTG_E_NULL, "xtg_batch_set_tuning: NULL argument");
+    int32_t st = check_tuning(t);
+    if (st != XTG_OK) return st;
+    B->ctx.tune = *t;
+    return XTG_OK;
+}
+
+int32_t xtg_batch_device_status(const xtg_batch* B) {
+    if (!B) return set_error(XTG_E_NULL, "xtg_batch_device_status: NULL batch");
+    return read_device_status(&B->ctx);
+}
+
+int32_t xtg_track_batch(xtg_batch* batch, const xtg_particles* particles, const int32_t* lattice_index,
+                        int32_t num_turns, int32_t ele_start, int32_t num_ele_track,
+                        int32_t flag_end_turn_actions, int32_t flag_reset_s_at_end_turn, int32_t flag_monitor,
+                        int32_t num_ele_line, double line_length, const xtg_monitor* monitor,
+                        uint64_t track_flags, void* stream) {
+    if (!batch || !particles) return set_error(XTG_E_NULL, "xtg_track_batch: NULL batch or particles");
+    if (!lattice_index && batch->ctx.fwd.n_lat > 1)
+        return set_error(XTG_E_NULL, "xtg_track_batch: lattice_index is required with several lattices");
+    return track_impl(&batch->ctx, particles, lattice_index, num_turns, ele_start, num_ele_track,
+                      flag_end_turn_actions, flag_reset_s_at_end_turn, flag_monitor, num_ele_line, line_length,
+                      monitor, track_flags, stream);
 }
 
 int32_t xtg_measure_fp64_peak(double* flops_per_s) {

@@ -1,0 +1,268 @@
+"""Learned screening of dynamic-aperture scans.
+
+A multilayer perceptron (default: 4 hidden layers of width 256, GELU)
+predicts, from a particle's normalised initial coordinates and its seed's
+multipole-error summary, the probability that it survives the turn budget
+and, if lost, its normalised log loss turn. It is trained on the
+``state`` / ``at_turn`` maps that batched tracking produces, entirely with
+the library's own kernels: BF16 tensor-core contractions with FP32
+accumulation for forward and backward passes, a fixed-order bias-gradient
+reduction and an Adam step on FP32 master weights (include/xtrack_gb300.h,
+``xtg_mlp_*``). Torch only holds the device memory.
+
+``screened_scan`` then tracks only the particles the network is unsure
+about (P(survive) between two thresholds) plus a random audit fraction and
+takes the network's answer for the rest; plain tracking of every particle
+stays the reference the screened result is judged against (DA error in
+beam sigma, misclassification rate on the audit).
+
+No reference counterpart: xtrack has no learned component.
+"""
+import ctypes
+import math
+
+import numpy as np
+import torch
+
+from . import _abi
+
+N_SEED_FEATURES = 32
+N_COORD_FEATURES = 6
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+class SurvivalMLP:
+    """MLP n_in -> width (x depth, GELU) -> 2 outputs, BF16 weights and
+    activations, FP32 accumulation, Adam on FP32 master weights."""
+
+    def __init__(self, n_in=N_COORD_FEATURES + N_SEED_FEATURES, width=256, depth=4, seed=0,
+                 device="cuda", w_turn=0.5):
+        self.device = torch.device(device)
+        if self.device.type != "cuda":
+            raise RuntimeError("SurvivalMLP runs on a CUDA device only")
+        self._lib = _abi.load_library()
+        self.dims = [n_in] + [width] * depth + [2]
+        self.w_turn = float(w_turn)
+        g = torch.Generator().manual_seed(seed)
+        self.W, self.b = [], []
+        for k_in, k_out in zip(self.dims[:-1], self.dims[1:]):
+            std = math.sqrt(2.0 / k_in)
+            self.W.append((torch.randn(k_out, k_in, generator=g, dtype=torch.float64) * std)
+                          .float().to(self.device))
+            self.b.append(torch.zeros(k_out, dtype=torch.float32, device=self.device))
+        self.W16 = [w.to(torch.bfloat16) for w in self.W]
+        self.mW = [torch.zeros_like(w) for w in self.W]
+        self.vW = [torch.zeros_like(w) for w in self.W]
+        self.mb = [torch.zeros_like(b) for b in self.b]
+        self.vb = [torch.zeros_like(b) for b in self.b]
+        self.gW = [torch.zeros_like(w) for w in self.W]
+        self.gb = [torch.zeros_like(b) for b in self.b]
+        self.step_count = 0
+        self.x_mean = torch.zeros(n_in, dtype=torch.float32, device=self.device)
+        self.x_std = torch.ones(n_in, dtype=torch.float32, device=self.device)
+        self._acts = None
+
+    # ------------------------------------------------------------------
+    @property
+    def n_layers(self):
+        return len(self.W)
+
+    def _stream(self):
+        return ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+
+    def set_normalisation(self, X):
+        X = torch.as_tensor(X, dtype=torch.float32, device=self.device)
+        self.x_mean = X.mean(0)
+        self.x_std = X.std(0).clamp_min(1e-12)
+
+    def prepare_input(self, X):
+        """Normalised BF16 copy of the features (fp32 [B, n_in])."""
+        X = torch.as_tensor(X, dtype=torch.float32, device=self.device)
+        Xn = ((X - self.x_mean) / self.x_std).contiguous()
+        X16 = torch.empty(Xn.shape, dtype=torch.bfloat16, device=self.device)
+        _abi.check_mlp(self._lib.xtg_mlp_to_bf16(_ptr(Xn), Xn.numel(), _ptr(X16), self._stream()),
+                       self._lib)
+        return X16
+
+    def forward(self, X16, keep=False):
+        """Outputs fp32 [B, 2] for BF16 input [B, n_in]; keeps the
+        activations for ``backward`` when ``keep``."""
+        B = X16.shape[0]
+        st = self._stream()
+        acts = [(None, X16)]
+        y = X16
+        out = None
+        for l in range(self.n_layers):
+            k_in, k_out = self.dims[l], self.dims[l + 1]
+            last = l == self.n_layers - 1
+            Z = torch.empty(B, k_out, dtype=torch.float32, device=self.device)
+            Y = None if last else torch.empty(B, k_out, dtype=torch.bfloat16, device=self.device)
+            _abi.check_mlp(self._lib.xtg_mlp_gemm(
+                _ptr(y), k_in, 1, _ptr(self.W16[l]), k_in, 1, B, k_out, k_in, _ptr(self.b[l]),
+                _abi.MLP_ACT_NONE if last else _abi.MLP_ACT_GELU, _ptr(Z), k_out,
+                _ptr(Y), k_out, None, 0, 0, st), self._lib)
+            acts.append((Z, Y))
+            y = Y
+            out = Z
+        self._acts = acts if keep else None
+        return out
+
+    def loss_and_grad(self, out, survive, logturn):
+        B = out.shape[0]
+        st = self._stream()
+        dout = torch.empty(B, 2, dtype=torch.float32, device=self.device)
+        dout16 = torch.empty(B, 2, dtype=torch.bfloat16, device=self.device)
+        loss = torch.empty(B, dtype=torch.float32, device=self.device)
+        _abi.check_mlp(self._lib.xtg_mlp_loss(_ptr(out), _ptr(survive), _ptr(logturn), B,
+                                              self.w_turn, _ptr(dout), _ptr(dout16), _ptr(loss),
+                                              st), self._lib)
+        return loss, dout, dout16
+
+    def backward(self, dout, dout16):
+        """Fills self.gW / self.gb from the kept activations."""
+        if self._acts is None:
+            raise RuntimeError("forward(keep=True) must precede backward")
+        st = self._stream()
+        B = dout.shape[0]
+        dZ, dZ16 = dout, dout16
+        for l in range(self.n_layers - 1, -1, -1):
+            k_in, k_out = self.dims[l], self.dims[l + 1]
+            y_prev = self._acts[l][1]                      # bf16 [B, k_in]
+            # dW[n, k] = sum_b dZ[b, n] y_prev[b, k]
+            _abi.check_mlp(self._lib.xtg_mlp_gemm(
+                _ptr(dZ16), 1, k_out, _ptr(y_prev), 1, k_in, k_out, k_in, B, None,
+                _abi.MLP_ACT_NONE, None, 0, None, 0, _ptr(self.gW[l]), k_in, 0, st), self._lib)
+            _abi.check_mlp(self._lib.xtg_mlp_colsum(_ptr(dZ), B, k_out, k_out, _ptr(self.gb[l]),
+                                                    0, st), self._lib)
+            if l == 0:
+                break
+            # dY_prev[b, k] = sum_n dZ[b, n] W[n, k]
+            dY = torch.empty(B, k_in, dtype=torch.float32, device=self.device)
+            _abi.check_mlp(self._lib.xtg_mlp_gemm(
+                _ptr(dZ16), k_out, 1, _ptr(self.W16[l]), 1, k_in, B, k_in, k_out, None,
+                _abi.MLP_ACT_NONE, None, 0, None, 0, _ptr(dY), k_in, 0, st), self._lib)
+            Z_prev = self._acts[l][0]
+            dZ = torch.empty(B, k_in, dtype=torch.float32, device=self.device)
+            dZ16 = torch.empty(B, k_in, dtype=torch.bfloat16, device=self.device)
+            _abi.check_mlp(self._lib.xtg_mlp_act_backward(_ptr(dY), _ptr(Z_prev), dY.numel(),
+                                                          _abi.MLP_ACT_GELU, _ptr(dZ), _ptr(dZ16),
+                                                          st), self._lib)
+
+    def adam_step(self, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8, weight_decay=0.0):
+        self.step_count += 1
+        st = self._stream()
+        for l in range(self.n_layers):
+            _abi.check_mlp(self._lib.xtg_mlp_adam(
+                _ptr(self.W[l]), _ptr(self.W16[l]), _ptr(self.gW[l]), _ptr(self.mW[l]),
+                _ptr(self.vW[l]), self.W[l].numel(), lr, beta1, beta2, eps, weight_decay,
+                self.step_count, st), self._lib)
+            _abi.check_mlp(self._lib.xtg_mlp_adam(
+                _ptr(self.b[l]), None, _ptr(self.gb[l]), _ptr(self.mb[l]), _ptr(self.vb[l]),
+                self.b[l].numel(), lr, beta1, beta2, eps, 0.0, self.step_count, st), self._lib)
+
+    # ------------------------------------------------------------------
+    def fit(self, X, survive, logturn, epochs=10, batch=4096, lr=1e-3, seed=0, lr_final=None):
+        """Adam training on (X, survive, logturn); returns the mean loss of
+        each epoch. ``lr`` decays linearly to ``lr_final`` (default lr/10)."""
+        X = torch.as_tensor(X, dtype=torch.float32, device=self.device)
+        s = torch.as_tensor(survive, dtype=torch.float32, device=self.device).contiguous()
+        t = torch.as_tensor(logturn, dtype=torch.float32, device=self.device).contiguous()
+        self.set_normalisation(X)
+        X16 = self.prepare_input(X)
+        n = X16.shape[0]
+        g = torch.Generator(device="cpu").manual_seed(seed)
+        hist = []
+        steps_total = epochs * max(1, (n + batch - 1) // batch)
+        lr_final = lr / 10 if lr_final is None else lr_final
+        k = 0
+        for _ in range(epochs):
+            perm = torch.randperm(n, generator=g).to(self.device)
+            tot = torch.zeros((), dtype=torch.float64, device=self.device)
+            for i0 in range(0, n, batch):
+                idx = perm[i0:i0 + batch]
+                xb = X16.index_select(0, idx).contiguous()
+                out = self.forward(xb, keep=True)
+                loss, dout, dout16 = self.loss_and_grad(out, s.index_select(0, idx).contiguous(),
+                                                        t.index_select(0, idx).contiguous())
+                self.backward(dout, dout16)
+                cur = lr + (lr_final - lr) * k / max(1, steps_total - 1)
+                self.adam_step(lr=cur)
+                tot += loss.double().sum()
+                k += 1
+            hist.append(float(tot.item()) / n)
+        return hist
+
+    def predict(self, X, batch=65536):
+        """(P(survive), normalised log loss turn) as numpy arrays."""
+        X16 = self.prepare_input(X)
+        ps, ts = [], []
+        for i0 in range(0, X16.shape[0], batch):
+            out = self.forward(X16[i0:i0 + batch].contiguous())
+            ps.append(torch.sigmoid(out[:, 0]).cpu().numpy())
+            ts.append(out[:, 1].cpu().numpy())
+        return np.concatenate(ps), np.concatenate(ts)
+
+
+# ----------------------------------------------------------------------
+# features and targets
+# ----------------------------------------------------------------------
+_FAMILIES = ("Bend", "Quadrupole", "Sextupole", "Multipole")
+
+
+def seed_features(line):
+    """32 numbers that summarise a seed's multipole errors: for each magnet
+    family (bends, quadrupoles, sextupoles, thin multipoles) and each order
+    0..3, the RMS over the family of knl_rel and of ksl_rel, in units of
+    1e-4."""
+    acc = {(f, n, s): [] for f in _FAMILIES for n in range(4) for s in (0, 1)}
+    for name in line.element_names:
+        e = line.element_dict[name]
+        fam = type(e).__name__
+        if fam not in _FAMILIES:
+            continue
+        for s, arr in ((0, getattr(e, "knl_rel", None)), (1, getattr(e, "ksl_rel", None))):
+            arr = np.zeros(1) if arr is None else np.asarray(arr, dtype=np.float64)
+            for n in range(4):
+                acc[(fam, n, s)].append(arr[n] if n < len(arr) else 0.0)
+    out = [math.sqrt(np.mean(np.square(v))) * 1e4 if v else 0.0 for v in acc.values()]
+    return np.asarray(out, dtype=np.float64)
+
+
+def coord_features(r, theta, delta, delta_scale=2.7e-4):
+    """Six normalised initial-condition features of a polar-grid particle."""
+    r = np.asarray(r, dtype=np.float64)
+    theta = np.asarray(theta, dtype=np.float64)
+    d = np.broadcast_to(np.asarray(delta, dtype=np.float64), r.shape)
+    return np.stack([r * np.cos(theta), r * np.sin(theta), r, theta, d / delta_scale,
+                     (r * np.cos(theta)) ** 2 + 0.5 * (r * np.sin(theta)) ** 2], axis=1)
+
+
+def targets(state, at_turn, num_turns):
+    """(survive, normalised log loss turn) from a tracking result."""
+    state = np.asarray(state)
+    at_turn = np.asarray(at_turn, dtype=np.float64)
+    survive = ((state > 0) | (at_turn >= num_turns)).astype(np.float32)
+    logturn = (np.log10(at_turn + 1.0) / math.log10(num_turns + 1.0)).astype(np.float32)
+    return survive, logturn
+
+
+def screen(p_survive, lo=0.05, hi=0.95, audit=0.02, seed=0):
+    """Boolean masks (track, audit): particles with lo < P < hi are tracked;
+    an extra random ``audit`` fraction of the others is tracked too."""
+    p = np.asarray(p_survive)
+    unsure = (p > lo) & (p < hi)
+    rng = np.random.default_rng(seed)
+    aud = (~unsure) & (rng.random(p.shape) < audit)
+    return unsure | aud, aud
+
+
+def screened_outcome(p_survive, tracked_mask, tracked_survive, hi=0.95):
+    """Survival map of a screened scan: the tracked particles' outcome where
+    tracked, else the network's (P >= hi: survives)."""
+    out = np.asarray(p_survive) >= hi
+    out = out.copy()
+    out[tracked_mask] = np.asarray(tracked_survive, dtype=bool)
+    return out

@@ -102,12 +102,26 @@ class Tracker:
                                               num_elements, ctypes.byref(f)), self._lib)
         return f.value
 
-    def set_launch_config(self, block_size=0, compact_every=0):
-        bs = ctypes.c_int32()
-        ce = ctypes.c_int32()
-        _abi.check(self._lib.xtg_set_launch_config(self._handle, block_size, compact_every,
-                                                   ctypes.byref(bs), ctypes.byref(ce)), self._lib)
-        return bs.value, ce.value
+    def get_tuning(self):
+        t = _abi.XtgTuning()
+        _abi.check(self._lib.xtg_get_tuning(self._handle, ctypes.byref(t)), self._lib)
+        return {f: getattr(t, f) for f, _ in _abi.XtgTuning._fields_}
+
+    def set_tuning(self, **kw):
+        """block_size (64/128/256), compact_every (turns), chunk_bytes (0: no
+        shared-memory staging), use_graph. Results do not depend on them."""
+        cur = self.get_tuning()
+        unknown = set(kw) - set(cur)
+        if unknown:
+            raise KeyError(f"unknown tuning keys {unknown}")
+        cur.update(kw)
+        t = _abi.XtgTuning(**{k: int(v) for k, v in cur.items()})
+        _abi.check(self._lib.xtg_set_tuning(self._handle, ctypes.byref(t)), self._lib)
+        return cur
+
+    def device_status(self):
+        """Synchronizes and raises if a bounded wait inside a kernel gave up."""
+        _abi.check(self._lib.xtg_device_status(self._handle), self._lib)
 
     # ------------------------------------------------------------------
     def _get_monitor(self, particles, turn_by_turn_monitor, num_turns):

@@ -57,9 +57,11 @@ def _rel_errors(rng, main_order, sigma=1e-4, r_ref=0.017, max_order=10):
 
 def thick_ring(seed=1, n_arcs=8, n_cells=23, with_errors=True, num_kicks=8,
                model="drift-kick-drift-expanded", integrator="uniform", k3l=0.5,
-               aperture=(0.022, 0.0176)):
+               aperture=(0.022, 0.0176), bend_angle=None):
+    """``bend_angle`` defaults to 2 pi / (6 n_arcs n_cells) (a closed ring);
+    shorter test rings pass the full ring's angle to keep its cell optics."""
     rng = np.random.default_rng(seed)
-    angle = 2 * math.pi / (6 * n_arcs * n_cells)
+    angle = 2 * math.pi / (6 * n_arcs * n_cells) if bend_angle is None else bend_angle
     kw = dict(model=model, integrator=integrator, num_multipole_kicks=num_kicks)
     ax, ay = aperture
     elements, names = [], []
