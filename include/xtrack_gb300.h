@@ -216,6 +216,29 @@ int32_t xtg_track(const xtg_lattice* lattice, const xtg_particles* particles,
                   const xtg_monitor* monitor, uint64_t track_flags,
                   void* stream);
 
+/*
+ * Allocation-free variant of xtg_track. No reference counterpart: the
+ * reference's track_line has no scratch to place. The push's scratch (index
+ * list, work queue, counters) lives in one static device array sized for
+ * XTG_NOALLOC_MAX_PARTICLES particles (about 4.3 MB per device) instead of
+ * the lattice's workspace, so a call makes no cudaMalloc/cudaFree and no
+ * framework allocation. Same arguments and results as xtg_track; the
+ * element table is read from global memory (the tuning's chunk_bytes and
+ * use_graph are not used), compact_every and block_size are. Capacities
+ * above XTG_NOALLOC_MAX_PARTICLES are rejected with XTG_E_CAPACITY; so is
+ * backtracking until an xtg_track call has built the lattice's reversed
+ * table. The first call on a device does the set-up (looks up the array's
+ * address and clears its error word): make it before any stream capture.
+ * All calls on a device share the one array: calls that overlap in time
+ * (on different streams or host threads) race and must not be issued.
+ */
+#define XTG_NOALLOC_MAX_PARTICLES 1048576
+int32_t xtg_track_noalloc(const xtg_lattice* lattice, const xtg_particles* particles,
+                          int32_t num_turns, int32_t ele_start, int32_t num_ele_track,
+                          int32_t flag_end_turn_actions, int32_t flag_reset_s_at_end_turn,
+                          int32_t flag_monitor, int32_t num_ele_line, double line_length,
+                          const xtg_monitor* monitor, uint64_t track_flags, void* stream);
+
 /* Launch tuning of the push. Results do not depend on it. */
 typedef struct xtg_tuning {
     int32_t block_size;      /* threads per block: 64, 128 or 256            */

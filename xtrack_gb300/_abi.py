@@ -15,6 +15,7 @@ import os
 import numpy as np
 
 XTG_MAX_KNL = 21
+XTG_NOALLOC_MAX_PARTICLES = 1048576
 
 XTG_OK = 0
 XTG_E_NULL = -1
@@ -172,7 +173,7 @@ LIB_PATH = os.path.join(_PKG_DIR, "libxtrack_gb300.so")
 
 EXPORTED_SYMBOLS = (
     "xtg_abi_version", "xtg_get_last_error", "xtg_lattice_create", "xtg_lattice_destroy",
-    "xtg_lattice_info", "xtg_track", "xtg_get_tuning", "xtg_set_tuning", "xtg_device_status",
+    "xtg_lattice_info", "xtg_track", "xtg_track_noalloc", "xtg_get_tuning", "xtg_set_tuning", "xtg_device_status",
     "xtg_batch_create", "xtg_batch_destroy", "xtg_batch_get_tuning", "xtg_batch_set_tuning", "xtg_batch_device_status",
     "xtg_track_batch", "xtg_sync", "xtg_launch_count", "xtg_measure_fp64_peak",
     "xtg_mlp_gemm", "xtg_mlp_act_backward", "xtg_mlp_colsum", "xtg_mlp_loss", "xtg_mlp_adam",
@@ -212,6 +213,8 @@ def load_library(path=None):
                               c.c_int32, c.c_int32, c.c_int32, c.c_int32, c.c_double,
                               c.POINTER(XtgMonitor), c.c_uint64, c.c_void_p]
     lib.xtg_track.restype = c.c_int32
+    lib.xtg_track_noalloc.argtypes = lib.xtg_track.argtypes
+    lib.xtg_track_noalloc.restype = c.c_int32
     lib.xtg_get_tuning.argtypes = [c.c_void_p, c.POINTER(XtgTuning)]
     lib.xtg_get_tuning.restype = c.c_int32
     lib.xtg_set_tuning.argtypes = [c.c_void_p, c.POINTER(XtgTuning)]

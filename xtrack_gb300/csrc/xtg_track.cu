@@ -1019,6 +1019,77 @@ static int32_t track_impl(ExecCtx* C, const xtg_particles* particles, const int3
     return run_rounds<false>(C, a, lat, cap, num_turns, s);
 }
 
+// ---------------------------------------------------------------------------
+// allocation-free push: the scratch of the rounds lives in one static device
+// array instead of the lattice's workspace
+// ---------------------------------------------------------------------------
+// Layout (bytes from the 256-aligned start): active-particle index list,
+// work items, counters {n_items, item_counter, error word, pad}, lattice
+// count, lattice bases.
+constexpr int64_t kNoAllocItems = XTG_NOALLOC_MAX_PARTICLES / 64 + 2;
+constexpr int64_t kNoAllocIdxOff = 0;
+constexpr int64_t kNoAllocItemsOff = kNoAllocIdxOff + XTG_NOALLOC_MAX_PARTICLES * 4;
+constexpr int64_t kNoAllocCountersOff = kNoAllocItemsOff + kNoAllocItems * 16;
+constexpr int64_t kNoAllocLatCountOff = kNoAllocCountersOff + 16;
+constexpr int64_t kNoAllocLatBaseOff = kNoAllocLatCountOff + 16;
+constexpr int64_t kNoAllocBytes = kNoAllocLatBaseOff + 16;
+static_assert(kNoAllocItemsOff % 16 == 0 && kNoAllocLatBaseOff % 8 == 0, "scratch alignment");
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+static std::mutex g_noalloc_mu;
+static unsigned char* g_noalloc_addr[64] = {nullptr};
+
+// Per-device set-up on the first call: the array's address, and the error
+// word cleared (the rest is rewritten by every round before it is read).
+static int32_t noalloc_scratch(int dev, unsigned char** out) {
+    if (dev < 0 || dev >= 64) return set_error(XTG_E_VALUE, "xtg_track_noalloc: device %d out of range", dev);
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        XTG_CUDA_CHECK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        XTG_CUDA_CHECK(cudaMemset((unsigned char*)p + kNoAllocCountersOff, 0, 16));
+        g_noalloc_addr[dev] = (unsigned char*)p;
+    }
+    *out = g_noalloc_addr[dev];
+    return XTG_OK;
+}
+
+template <bool kExact>
+static int32_t run_rounds_noalloc(unsigned char* scratch, TrackArgs a, int64_t cap, int32_t num_turns,
+                                  int32_t block, int32_t compact_every, cudaStream_t s) {
+    int32_t* idx = reinterpret_cast<int32_t*>(scratch + kNoAllocIdxOff);
+    int4* items = reinterpret_cast<int4*>(scratch + kNoAllocItemsOff);
+    int32_t* counters = reinterpret_cast<int32_t*>(scratch + kNoAllocCountersOff);
+    int32_t* lat_count = reinterpret_cast<int32_t*>(scratch + kNoAllocLatCountOff);
+    int64_t* lat_pbase = reinterpret_cast<int64_t*>(scratch + kNoAllocLatBaseOff);
+    a.idx = idx;
+    a.items = items;
+    a.n_items = counters + 0;
+    a.item_counter = counters + 1;
+    a.err = counters + 2;
+    a.chunk_bytes = 0;
+    a.smem_bytes = 0;
+    int grid = 0;
+    int32_t st = persistent_grid<kExact>(block, 0, &grid);
+    if (st != XTG_OK) return st;
+    prefix_lattices_kernel<<<1, 32, 0, s>>>(lat_count, 1, cap, lat_pbase, 1);
+    g_launch_count.fetch_add(1);
+    int32_t const per = compact_every > 0 ? std::min(compact_every, num_turns) : num_turns;
+    for (int32_t done = 0; done < num_turns; done += per) {
+        a.num_turns = std::min(per, num_turns - done);
+        // the lattice count must start at zero in every round
+        XTG_CUDA_CHECK(cudaMemsetAsync(lat_count, 0, sizeof(int32_t), s));
+        compact_kernel<<<(unsigned)((cap + 255) / 256), 256, 0, s>>>(a.P.state, nullptr, cap, 1, lat_pbase,
+                                                                   lat_count, idx);
+        items_kernel<<<1, 256, 0, s>>>(lat_count, lat_pbase, 1, block, items, counters + 0, counters + 1);
+        track_kernel<kExact><<<grid, block, 0, s>>>(a);
+        g_launch_count.fetch_add(3);
+        XTG_CUDA_CHECK(cudaGetLastError());
+    }
+    return XTG_OK;
+}
+
 static int32_t read_device_status(const ExecCtx* C) {
     if (!C->ws.counters) return XTG_OK;
     int32_t h[4] = {0, 0, 0, 0};
@@ -1140,6 +1211,84 @@ int32_t xtg_track(const xtg_lattice* lattice, const xtg_particles* particles, in
     return track_impl(C, particles, nullptr, num_turns, ele_start, num_ele_track, flag_end_turn_actions,
                       flag_reset_s_at_end_turn, flag_monitor, num_ele_line, line_length, monitor, track_flags,
                       stream);
+}
+
+int32_t xtg_track_noalloc(const xtg_lattice* lattice, const xtg_particles* particles, int32_t num_turns,
+                          int32_t ele_start, int32_t num_ele_track, int32_t flag_end_turn_actions,
+                          int32_t flag_reset_s_at_end_turn, int32_t flag_monitor, int32_t num_ele_line,
+                          double line_length, const xtg_monitor* monitor, uint64_t track_flags, void* stream) {
+    if (!lattice || !particles) return set_error(XTG_E_NULL, "xtg_track_noalloc: NULL lattice or particles");
+    int64_t const cap = particles->capacity;
+    if (cap < 0) return set_error(XTG_E_VALUE, "xtg_track_noalloc: capacity < 0");
+    if (cap > XTG_NOALLOC_MAX_PARTICLES)
+        return set_error(XTG_E_CAPACITY,
+                         "xtg_track_noalloc: capacity %lld exceeds the static scratch limit of %d particles "
+                         "(use xtg_track)",
+                         (long long)cap, XTG_NOALLOC_MAX_PARTICLES);
+    if (!particles_complete(particles))
+        return set_error(XTG_E_NULL, "xtg_track_noalloc: a required particle array is NULL");
+    ExecCtx* C = &const_cast<xtg_lattice*>(lattice)->ctx;
+    int64_t const n = C->fwd.n_rec;
+    if (num_turns < 0) return set_error(XTG_E_VALUE, "xtg_track_noalloc: num_turns < 0");
+    if (ele_start < 0 || num_ele_track < 0 || (int64_t)ele_start + num_ele_track > n)
+        return set_error(XTG_E_VALUE, "xtg_track_noalloc: element range [%d, %d+%d) outside [0, %lld)",
+                         ele_start, ele_start, num_ele_track, (long long)n);
+    if (flag_monitor < 0 || flag_monitor > 2)
+        return set_error(XTG_E_VALUE, "xtg_track_noalloc: flag_monitor must be 0, 1 or 2");
+    if (flag_monitor != 0 && !monitor)
+        return set_error(XTG_E_NULL, "xtg_track_noalloc: flag_monitor set but monitor is NULL");
+    if (monitor && flag_monitor != 0) {
+        if (monitor->n_repetitions > 1 && monitor->repetition_period <= 0)
+            return set_error(XTG_E_VALUE, "xtg_track_noalloc: repetition_period must be > 0");
+        if (monitor->n_records < 0) return set_error(XTG_E_VALUE, "xtg_track_noalloc: monitor n_records < 0");
+    }
+    int cur = 0;
+    XTG_CUDA_CHECK(cudaGetDevice(&cur));
+    if (cur != C->device)
+        return set_error(XTG_E_VALUE, "xtg_track_noalloc: tables were built on device %d, current is %d",
+                         C->device, cur);
+    unsigned char* scratch = nullptr;
+    int32_t st = noalloc_scratch(cur, &scratch);
+    if (st != XTG_OK) return st;
+    if (cap == 0 || num_turns == 0) return XTG_OK;
+
+    std::lock_guard<std::mutex> lock(C->mu);
+    bool const backtrack = (track_flags >> XTG_FLAG_BACKTRACK) & 1u;
+    const DevTables* T = &C->fwd;
+    int32_t rec_first = ele_start;
+    if (backtrack) {
+        if (!C->bwd.built)
+            return set_error(XTG_E_VALUE,
+                             "xtg_track_noalloc: the backtracking table of this lattice is not built "
+                             "(one xtg_track call with backtracking builds it)");
+        T = &C->bwd;
+        rec_first = (int32_t)(n - ((int64_t)ele_start + num_ele_track));
+    }
+    TrackArgs a;
+    memset(&a, 0, sizeof(a));
+    a.table = T->d_bytes;
+    a.lat_base = T->d_lat_base;
+    a.rec_off = T->d_rec_off;
+    a.chunk_end = nullptr;
+    a.stride = T->n_rec + 1;
+    a.rec_first = rec_first;
+    a.rec_count = num_ele_track;
+    a.flag_monitor = flag_monitor;
+    a.flag_end_turn_actions = flag_end_turn_actions;
+    a.flag_reset_s = flag_reset_s_at_end_turn;
+    a.backtrack = backtrack ? 1 : 0;
+    a.has_global = C->config.has_global_xy_limit;
+    a.preserve_angle = C->config.cavity_preserve_angle;
+    a.global_lim = C->config.global_xy_limit;
+    a.num_ele_line = num_ele_line;
+    a.line_length = line_length;
+    a.track_flags = track_flags;
+    a.P = *particles;
+    if (monitor) a.M = *monitor;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (C->config.arith == XTG_ARITH_EXACT)
+        return run_rounds_noalloc<true>(scratch, a, cap, num_turns, C->tune.block_size, C->tune.compact_every, s);
+    return run_rounds_noalloc<false>(scratch, a, cap, num_turns, C->tune.block_size, C->tune.compact_every, s);
 }
 
 int32_t xtg_batch_create(const xtg_lattice* const* lattices, int32_t n_lattices, xtg_batch** out) {
