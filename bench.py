@@ -179,9 +179,18 @@ def run_gpu(args):
     fp64_peak = peak.value
 
     stream = torch.cuda.current_stream(dev)
+    monitor = None
+    if args.monitor_first:
+        # turn-by-turn monitor of the first particles, 6 coordinates, over
+        # the timed steps (the monitor-stress configuration)
+        from xtrack_gb300.monitors import ParticlesMonitor
+        t0_turn = args.warmup
+        monitor = ParticlesMonitor(start_at_turn=t0_turn, stop_at_turn=t0_turn + args.steps,
+                                   num_particles=min(args.monitor_first, n),
+                                   fields=("x", "px", "y", "py", "zeta", "delta"), device=dev)
 
     def step():
-        tracker._track(beam, num_turns=1)
+        tracker._track(beam, num_turns=1, turn_by_turn_monitor=monitor)
 
     for _ in range(args.warmup):
         step()
@@ -251,11 +260,16 @@ def run_gpu(args):
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
            "arith": args.arith,
            "config": {"workload": "thick LHC-like ring, 8x23 FODO cells, 6993 elements, "
-                                  "1e6 protons 7 TeV, 1 turn per step",
+                                  f"{n:.3g} protons 7 TeV, 1 turn per step",
                       "particles_per_gpu": n, "elements": n_el, "turns_per_step": 1,
-                      "l2": "inputs larger than L2 (152 MB of particle arrays), no flush",
+                      "l2": f"inputs larger than L2 ({n * 152 / 1e6:.0f} MB of particle "
+                            "arrays), no flush" if n * 152 > 129e6 else
+                            "inputs smaller than L2 (not a headline configuration)",
                       "alive_before": n_alive0, "alive_after": n_alive1,
-                      "tuning": tuning},
+                      "tuning": tuning,
+                      "monitor": (None if monitor is None else
+                                  {"particles": monitor.part_id_end, "fields": 6,
+                                   "bytes_per_step": monitor.part_id_end * 48})},
            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                    "d2h_bytes_per_step": h2d},
            "gpu_launches": int(launches),
@@ -428,6 +442,8 @@ def main():
     ap.add_argument("--compact-every", dest="compact_every", type=int, default=None)
     ap.add_argument("--chunk-bytes", dest="chunk_bytes", type=int, default=None)
     ap.add_argument("--use-graph", dest="use_graph", type=int, default=None)
+    ap.add_argument("--monitor-first", dest="monitor_first", type=int, default=0,
+                    help="record 6 coordinates per turn of the first N particles")
     ap.add_argument("--workload", default="thick_ring", choices=["thick_ring", "da_screen"])
     ap.add_argument("--da-turns", dest="da_turns", type=int, default=300)
     ap.add_argument("--da-particles", dest="da_particles", type=int, default=20000,

@@ -1,0 +1,110 @@
+"""xtrack-format dictionaries and JSON: round trips of every element class
+and of sliced lines (same raw records), rejection of out-of-scope fields,
+and a real lattice: the thin HL-LHC v1.4 line of the reference's test data,
+loaded through the serializer, whose golden vectors come from the
+reference-compiled code (tests/golden/make_lhc_fixture.py)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import pyoracle
+import xtrack_gb300 as xt
+from xtrack_gb300 import serialization as ser
+from xtrack_gb300 import workloads
+from lattice_cases import element_zoo, sliced_line
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LHC = os.path.join(HERE, "golden", "lhc", "hllhc14_thin_64p_10t.npz")
+
+
+def _same_records(a, b):
+    return np.ascontiguousarray(a).tobytes() == np.ascontiguousarray(b).tobytes()
+
+
+@pytest.mark.parametrize("factory", [workloads.toy_ring, element_zoo, lambda: sliced_line(True),
+                                     lambda: sliced_line(False),
+                                     lambda: workloads.thick_ring(n_arcs=1, n_cells=2)])
+def test_dict_and_json_round_trip(factory, tmp_path):
+    line = factory()
+    d = line.to_dict()
+    json.dumps(d)                                   # plain JSON types only
+    back = xt.Line.from_dict(d)
+    assert back.element_names == line.element_names
+    assert _same_records(back._element_records(), line._element_records())
+    path = str(tmp_path / "line.json")
+    line.to_json(path)
+    again = xt.load(path)
+    assert _same_records(again._element_records(), line._element_records())
+
+
+def test_reference_style_dicts():
+    # as xtrack writes them: ints for models, 'h' instead of 'angle', k0_from_h
+    d = {"elements": {
+        "d": {"__class__": "Drift", "length": 1.5},
+        "m": {"__class__": "Multipole", "order": 1, "inv_factorial_order": 1.0, "length": 0.0,
+              "hxl": 0.0, "hyl": 0.0, "radiation_flag": 0, "knl": [0.0, 1e-3], "ksl": [0.0, 0.0]},
+        "b": {"__class__": "Bend", "length": 2.0, "h": 0.01, "k0_from_h": 1, "k1": 0.0,
+              "model": 6, "integrator": 3, "num_multipole_kicks": 4, "edge_entry_model": 0,
+              "shift_x": 0.0, "rot_s_rad": 0.0},
+        "c": {"__class__": "Cavity", "voltage": 2e6, "frequency": 400e6, "phase": 3.14},
+        "a": {"__class__": "LimitEllipse", "a_squ": 4e-4, "b_squ": 4e-4, "a_b_squ": 1.6e-7}},
+        "element_names": ["d", "m", "b", "c", "a"]}
+    line = xt.Line.from_dict(d)
+    b = line["b"]
+    assert b.k0 == "from_h" and abs(b.angle - 0.02) < 1e-15
+    assert b.model == "drift-kick-drift-expanded" and b.integrator == "uniform"
+    assert line["m"].knl.tolist() == [0.0, 1e-3]
+    assert line["c"].phase == 3.14
+
+
+@pytest.mark.parametrize("bad", [
+    {"__class__": "Drift", "length": 1.0, "shift_x": 1e-3},
+    {"__class__": "Multipole", "knl": [0.0], "radiation_flag": 1},
+    {"__class__": "Multipole", "knl": [0.0], "hyl": 1e-3},
+    {"__class__": "Cavity", "voltage": 1.0, "lag_taper": 5.0},
+    {"__class__": "Drift", "length": 1.0, "mystery": 2},
+    {"__class__": "BeamBeamBiGaussian2D"},
+])
+def test_out_of_scope_fields_are_rejected(bad):
+    with pytest.raises(ValueError):
+        ser.element_from_dict(bad, "e")
+
+
+def _lhc():
+    d = np.load(LHC)
+    meta = json.loads(str(d["meta"]))
+    recs = d["records"]
+    arrs = pyoracle.host_arrays({k[3:]: d[k].copy() for k in d.files if k.startswith("in_")})
+    out = {k[4:]: d[k] for k in d.files if k.startswith("out_")}
+    return recs, arrs, out, meta
+
+
+def test_lhc_fixture_oracle_reproduces_reference():
+    recs, arrs, out, meta = _lhc()
+    assert meta["n_elements"] == len(recs) == 11603
+    pyoracle.track(recs, arrs, line_length=meta["line_length"], num_turns=meta["num_turns"],
+                   q0=meta["q0"], mass0=meta["mass0"])
+    for k, v in out.items():
+        assert np.array_equal(arrs[k], v), k
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("arith", ["exact", "fast"])
+def test_lhc_fixture_gpu(arith):
+    """The real 11603-element thin LHC line on the GPU against the
+    reference-compiled result after 10 turns: exact within 1e-14, fast
+    within 3x the reference's own FMA spread."""
+    from xtg_testutil import compare, compare_within_spread, fma_spread, gpu_track
+    recs, arrs, out, meta = _lhc()
+    kw = dict(line_length=meta["line_length"], num_turns=meta["num_turns"], q0=meta["q0"],
+              mass0=meta["mass0"])
+    got, _ = gpu_track(recs, {k: v.copy() for k, v in arrs.items()}, arith=arith, **kw)
+    if arith == "exact":
+        compare(got, out, 1e-14)
+    else:
+        for f in ("state", "at_turn", "at_element"):
+            assert np.array_equal(got[f], out[f]), f
+        spread, ok = fma_spread(recs, arrs, **kw)
+        compare_within_spread(got, out, spread, ok)

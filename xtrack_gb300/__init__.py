@@ -15,5 +15,6 @@ from .line import Line, TrackerConfig
 from .tracker import Tracker, TrackFlags
 from .batch import BatchTracker
 from .tuning import autotune
+from .serialization import load
 
 __version__ = "0.1.0"

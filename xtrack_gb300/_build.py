@@ -48,6 +48,18 @@ def _stale(target, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
+def _defines():
+    """Build-time options: XTG_FAST_MIN_BLOCKS (1 or 2) sets the register
+    budget of the fast push (see xtg_track.cu)."""
+    out = []
+    v = os.environ.get("XTG_FAST_MIN_BLOCKS")
+    if v:
+        if v not in ("1", "2"):
+            raise ValueError("XTG_FAST_MIN_BLOCKS must be 1 or 2")
+        out.append(f"-DXTG_FAST_MIN_BLOCKS={v}")
+    return out
+
+
 def build(verbose=False, force=False):
     """Compiles the library if any source is newer than it. Returns its path."""
     os.makedirs(BUILD, exist_ok=True)
@@ -61,7 +73,7 @@ def build(verbose=False, force=False):
         o = os.path.join(BUILD, src + ".o")
         objs.append(o)
         if force or _stale(o, [s] + headers):
-            jobs.append([nvcc] + ARCH + NVCC_FLAGS + ["-Xptxas", "-v", "-c", s, "-o", o])
+            jobs.append([nvcc] + ARCH + NVCC_FLAGS + _defines() + ["-Xptxas", "-v", "-c", s, "-o", o])
     for src in CXX_SOURCES:
         s = os.path.join(CSRC, src)
         o = os.path.join(BUILD, src + ".o")

@@ -600,6 +600,7 @@ void pack_magnet(const xtg_element& e, bool backtrack, bool exact, RecBuf* rb) {
             fc.push_back(cn[i] * kw[0]);
             fc.push_back(cs[i] * kw[0]);
         }
+        rb->pad16();   // (cn_i, cs_i) pairs are read as 16-byte vectors
         int32_t off = rb->append(fc.data(), fc.size(), coef_base);
         R()->fast_top = ftop;
         R()->fast_coef = off;

@@ -59,14 +59,18 @@ XTG_DEV void drift_expanded(PState& p, double length) {
         p.s = p.s + length;
         p.zeta = p.zeta + length * dzeta;
     } else {
+        // the reference's grouping, contracted as its FMA build contracts
+        // it: 1 + (xp^2 + yp^2)/2 is rounded before the product with 1/rvv
+        // (regrouping it changes zeta by ~1e-12 m per turn on a 6000-drift
+        // ring, far outside the reference's own FMA/no-FMA spread)
         double const xp = p.px * p.rpp;
         double const yp = p.py * p.rpp;
         double const t = fma(xp, xp, yp * yp);
         double const dzeta = fma(-p.rv0v, fma(t, 0.5, 1.0), 1.0);
         p.x = fma(xp, length, p.x);
         p.y = fma(yp, length, p.y);
-        p.s = p.s + length;
         p.zeta = fma(length, dzeta, p.zeta);
+        p.s = p.s + length;
     }
 }
 
@@ -435,17 +439,19 @@ XTG_DEV void apply_kick(PState& p, const KickArgs& a, const double* __restrict__
             p.zeta = p.zeta + dzeta;
         }
     } else {
-        // merged polynomial sum_i (cn_i + i cs_i) z^i, z = x + i y
+        // merged polynomial sum_i (cn_i + i cs_i) z^i, z = x + i y; the
+        // (cn_i, cs_i) pairs are 16-byte aligned: one 128-bit load each
         double pr = 0.0, pi = 0.0;
         int const top = a.fast_top;
         if (top >= 0) {
-            const double* __restrict__ c = coefs + a.fast_coef;
-            pr = c[0];
-            pi = c[1];
-            for (int i = top; i > 0; i--) {
-                c += 2;
-                double const nr = fma(pr, x, fma(-pi, y, c[0]));
-                double const ni = fma(pr, y, fma(pi, x, c[1]));
+            const double2* __restrict__ c = reinterpret_cast<const double2*>(coefs + a.fast_coef);
+            double2 const c0 = c[0];
+            pr = c0.x;
+            pi = c0.y;
+            for (int i = 1; i <= top; i++) {
+                double2 const ci = c[i];
+                double const nr = fma(pr, x, fma(-pi, y, ci.x));
+                double const ni = fma(pr, y, fma(pi, x, ci.y));
                 pr = nr;
                 pi = ni;
             }

@@ -65,6 +65,12 @@ static int32_t set_error(int32_t code, const char* fmt, ...) {
             return set_error(XTG_E_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_));   \
     } while (0)
 
+// resident blocks of 256 threads per SM the fast push is compiled for (the
+// register budget: 1 -> up to 255 registers, 2 -> 128)
+#ifndef XTG_FAST_MIN_BLOCKS
+#define XTG_FAST_MIN_BLOCKS 1
+#endif
+
 // largest staging chunk: two chunks plus the static shared memory of the
 // push kernel stay within the 227 KB a block may use
 static constexpr int32_t kMaxChunkBytes = 113 * 1024;
@@ -352,7 +358,7 @@ __device__ __forceinline__ void end_turn(const TrackArgs& a, PState& p, bool act
 // the persistent push kernel
 // ---------------------------------------------------------------------------
 template <bool kExact>
-__global__ void __launch_bounds__(256, 1) track_kernel(const TrackArgs a) {
+__global__ void __launch_bounds__(256, kExact ? 1 : XTG_FAST_MIN_BLOCKS) track_kernel(const TrackArgs a) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ uint64_t full_bar[2];
     __shared__ int s_item;

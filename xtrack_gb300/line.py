@@ -180,30 +180,25 @@ class Line:
 
     # ------------------------------------------------------------------
     def to_dict(self):
-        return {"element_names": list(self.element_names),
-                "elements": {n: _element_to_dict(self.element_dict[n]) for n in self.element_names},
-                "config": dict(self.config._v),
-                "extra_config": dict(self._extra_config)}
+        """xtrack-format line dict (serialization.py)."""
+        from .serialization import line_to_dict
+        return line_to_dict(self)
 
     @classmethod
     def from_dict(cls, dct):
-        elements = {}
-        pending = {}
-        for n, d in dct["elements"].items():
-            if d["__class__"].startswith(("ThickSlice", "ThinSlice", "DriftSlice")):
-                pending[n] = d
-            else:
-                elements[n] = _element_from_dict(d)
-        for n, d in pending.items():
-            parent = elements[d["parent_name"]] if d["parent_name"] in elements else \
-                _element_from_dict(d["_parent"])
-            klass = getattr(el, d["__class__"])
-            elements[n] = klass(parent, weight=d["weight"], parent_name=d["parent_name"])
-        line = cls(elements=elements, element_names=dct["element_names"])
-        for k, v in dct.get("config", {}).items():
-            setattr(line.config, k, v)
-        line._extra_config.update(dct.get("extra_config", {}))
-        return line
+        """Line from an xtrack-format line dict (as xtrack's Line.to_dict
+        writes it, line.py:384-508)."""
+        from .serialization import line_from_dict
+        return line_from_dict(dct)
+
+    def to_json(self, path):
+        from .serialization import save_json
+        save_json(self, path)
+
+    @classmethod
+    def from_json(cls, path):
+        from .serialization import load
+        return load(path)
 
 
 def _element_length(e):
@@ -216,30 +211,3 @@ def _element_length(e):
     if getattr(e, "isthick", False):
         return float(getattr(e, "length", 0.0))
     return 0.0
-
-
-_SKIP = {"_parent"}
-
-
-def _element_to_dict(e):
-    d = {"__class__": type(e).__name__}
-    for k, v in vars(e).items():
-        if k in _SKIP:
-            continue
-        if isinstance(v, np.ndarray):
-            v = v.tolist()
-        d[k] = v
-    if isinstance(e, el._Slice):
-        d["_parent"] = _element_to_dict(e._parent)
-    return d
-
-
-def _element_from_dict(d):
-    d = dict(d)
-    klass = getattr(el, d.pop("__class__"))
-    obj = klass.__new__(klass)
-    for k, v in d.items():
-        if isinstance(v, list):
-            v = np.asarray(v, dtype=np.float64)
-        setattr(obj, k, v)
-    return obj
