@@ -628,11 +628,225 @@ static void xto_edge_linear_coefficients(double k, double e1, double e1_fd,
     *r43 = r43_out;
 }
 
-/* track_magnet_edge.h:16-80, linear (0), suppressed (-1) and ax/ay-only (3)
- * models; the full and dipole-only models are rejected by xto_validate. */
+/* ---------------------------------------------------------------------- */
+/* Nonlinear edges (full and dipole-only models)                           */
+/* ---------------------------------------------------------------------- */
+
+/* local_particle_custom_api.h:36-49 */
+static void xto_update_delta(xto_part* p, double new_delta_value) {
+    double const beta0 = p->beta0;
+    double const delta_beta0 = new_delta_value * beta0;
+    double const ptau_beta0 = sqrt(delta_beta0 * delta_beta0 + 2 * delta_beta0 * beta0 + 1) - 1;
+    double const one_plus_delta = 1 + new_delta_value;
+    p->delta = new_delta_value;
+    p->rvv = one_plus_delta / (1 + ptau_beta0);
+    p->rpp = 1 / one_plus_delta;
+    p->ptau = ptau_beta0 / beta0;
+}
+
+/* local_particle_custom_api.h:248-256 */
+static void xto_kill(xto_part* p, int64_t kill_state) {
+    p->x = 1e30;
+    p->px = 1e30;
+    p->y = 1e30;
+    p->py = 1e30;
+    p->zeta = 1e30;
+    xto_update_delta(p, -1);
+    p->state = kill_state;
+}
+
+/* track_yrotation.h:13-48 (no spin) */
+static void xto_yrotation(xto_part* p, double sin_angle, double cos_angle, double tan_angle) {
+    double const beta0 = p->beta0;
+    double const x = p->x, y = p->y, px = p->px, py = p->py;
+    double const t = p->zeta / beta0;
+    double const pt = (p->ptau / beta0) * beta0;       /* get_pzeta * beta0 */
+    double const pz = sqrt(1.0 + 2.0 * pt / beta0 + pt * pt - px * px - py * py);
+    double const ptt = 1.0 + tan_angle * px / pz;
+    double const x_hat = x / (cos_angle * ptt);
+    double const px_hat = cos_angle * px - sin_angle * pz;
+    double const y_hat = y - tan_angle * x * py / (pz * ptt);
+    double const t_hat = t + tan_angle * x * (1.0 / beta0 + pt) / (pz * ptt);
+    p->x = x_hat;
+    p->px = px_hat;
+    p->y = y_hat;
+    p->zeta = t_hat * beta0;
+}
+
+/* track_dipole_fringe.h:16-82 (the MAD-NG form, the default build) */
+static void xto_dipole_fringe(xto_part* p, double fint, double hgap, double k0) {
+    if (fabs(k0) < 10e-10) return;
+    double const beta0 = p->beta0;
+    double const x = p->x, px = p->px, y = p->y, py = p->py;
+    double const t = p->zeta / beta0;
+    double const pt = p->ptau;
+    double const delta = p->delta;
+    double const fh = hgap * fint;
+    double const fsad = (fh > 10e-10) ? 1. / (72 * fh) : 0;
+    double const k0w = k0 * p->chi;
+    double const inv_beta = 1. / beta0;
+    double const b0 = k0w;
+    double const dpp = (1. + delta) * (1. + delta);
+    double const pz = sqrt(dpp - px * px - py * py);
+    double const ipz = 1. / pz;
+    double const relp = 1. / sqrt(dpp);
+    double const tfac = -(inv_beta + pt);
+    double const c2 = b0 * fh * 2;
+    double const c3 = (b0 * b0) * fsad * relp;
+    double const xp = px / pz;
+    double const yp = py / pz;
+    double const xyp = xp * yp;
+    double const yp2 = 1. + yp * yp;
+    double const xp2 = xp * xp;
+    double const iyp2 = 1. / yp2;
+    double const fi0 = atan((xp * iyp2)) - c2 * (1 + xp2 * (1 + yp2)) * ipz;
+    double const cfi = cos(fi0);
+    double const co2 = b0 / (cfi * cfi);
+    double const q = xp * iyp2;
+    double const co1 = co2 / (1 + q * q) * iyp2;
+    double const co3 = co2 * c2;
+    double const fi1 = co1 - co3 * 2 * xp * (1 + yp2) * ipz;
+    double const fi2 = -2 * co1 * xyp * iyp2 - co3 * 2 * xp * xyp * ipz;
+    double const fi3 = +co3 * (1 + xp2 * (1 + yp2)) * (ipz * ipz);
+    double const kx = fi1 * (1 + xp2) * ipz + fi2 * xyp * ipz - fi3 * xp;
+    double const ky = fi1 * xyp * ipz + fi2 * yp2 * ipz - fi3 * yp;
+    double const kz = fi1 * tfac * xp * (ipz * ipz) + fi2 * tfac * yp * (ipz * ipz) - fi3 * tfac * ipz;
+    double const new_y = 2 * y / (1 + sqrt(1 - 2 * ky * y));
+    double const new_x = x + 0.5 * kx * (new_y * new_y);
+    double const new_py = py - 4 * c3 * (new_y * new_y * new_y) - b0 * tan(fi0) * new_y;
+    double const new_t = t + 0.5 * kz * (new_y * new_y) +
+                         c3 * (new_y * new_y * new_y * new_y) * (relp * relp) * tfac;
+    p->x = new_x;
+    p->y = new_y;
+    p->py = new_py;
+    p->zeta = new_t * beta0;
+}
+
+/* track_mult_fringe.h:12-128 */
+static void xto_mult_fringe(xto_part* p, const double* kn, const double* ks, int64_t k_order,
+                            const double* knl, const double* ksl, int64_t kl_order,
+                            double length, int is_exit, uint64_t min_order) {
+    if (k_order == -1 && kl_order == -1) return;
+    if (flag_set(p, 0)) {            /* XS_FLAG_BACKTRACK */
+        xto_kill(p, -32);
+        return;
+    }
+    double const beta0 = p->beta0;
+    double const direction = is_exit ? -1 : 1;
+    double const x = p->x, px = p->px, y = p->y, py = p->py;
+    double const t = p->zeta / beta0;
+    double const pt = p->ptau;
+    double const rpp = p->rpp;
+    double const chi = p->chi;
+    double rx = 1, ix = 0;
+    double fx = 0, fxx = 0, fxy = 0, fy = 0, fyx = 0, fyy = 0;
+    uint32_t const order = (uint32_t)((k_order > kl_order) ? k_order : kl_order);
+    double inv_factorial = 1;
+    for (uint32_t ii = 0; ii <= order; ii++) {
+        if (ii > 1) inv_factorial /= ii;
+        double const component = ii + 1;
+        double const drx = rx;
+        double const dix = ix;
+        rx = drx * x - dix * y;
+        ix = drx * y + dix * x;
+        double kn_total = 0, ks_total = 0;
+        if (ii >= min_order) {
+            if ((int64_t)ii <= k_order) {
+                kn_total += kn[ii] * inv_factorial;
+                ks_total += ks[ii] * inv_factorial;
+            }
+            if ((int64_t)ii <= kl_order && length != 0.) {
+                kn_total += knl[ii] / length * inv_factorial;
+                ks_total += ksl[ii] / length * inv_factorial;
+            }
+        }
+        double const nj = -direction / (4 * (component + 1));
+        double const nf = (component + 2) / component;
+        double const kj = kn_total * chi;
+        double const ksj = ks_total * chi;
+        double u, v, du, dv;
+        if (ii == 0) {
+            u = nj * (-ksj * ix);
+            v = nj * (ksj * rx);
+            du = nj * (-ksj * dix);
+            dv = nj * (ksj * drx);
+        } else {
+            u = nj * (kj * rx - ksj * ix);
+            v = nj * (kj * ix + ksj * rx);
+            du = nj * (kj * drx - ksj * dix);
+            dv = nj * (kj * dix + ksj * drx);
+        }
+        double const dux = component * du;
+        double const dvx = component * dv;
+        double const duy = -component * dv;
+        double const dvy = component * du;
+        fx = fx + u * x + nf * v * y;
+        fy = fy + u * y - nf * v * x;
+        fxx = fxx + dux * x + nf * dvx * y + u;
+        fyy = fyy + duy * y - nf * dvy * x + u;
+        fxy = fxy + duy * x + nf * (dvy * y + v);
+        fyx = fyx + dux * y - nf * (dvx * x + v);
+    }
+    double const a = 1 - fxx * rpp;
+    double const b = -fyx * rpp;
+    double const c = -fxy * rpp;
+    double const d = 1 - fyy * rpp;
+    double const det = (a * d - b * c);
+    double const new_px = (d * px - b * py) / det;
+    double const new_py = (a * py - c * px) / det;
+    double const delta_t = (1 / beta0 + pt) * (new_px * fx + new_py * fy) * (rpp * rpp * rpp);
+    p->x += -fx * rpp;
+    p->y += -fy * rpp;
+    p->px = new_px;
+    p->py = new_py;
+    p->zeta = (t + delta_t) * beta0;
+}
+
+/* track_wedge.h:14-58 (no spin) */
+static void xto_wedge(xto_part* p, double theta, double k0) {
+    double const b1 = k0 * p->chi;
+    if (fabs(b1) < 10e-10) {
+        double const sin_ = sin(theta);
+        double const cos_ = cos(theta);
+        double const tan_ = tan(theta);
+        xto_yrotation(p, -sin_, cos_, -tan_);
+        return;
+    }
+    double const rvv = p->rvv;
+    double const x = p->x, px = p->px, py = p->py;
+    double const one_plus_delta = p->delta + 1.0;
+    double const A = 1.0 / sqrt(one_plus_delta * one_plus_delta - py * py);
+    double const pz = sqrt(one_plus_delta * one_plus_delta - px * px - py * py);
+    double const new_px = px * cos(theta) + (pz - b1 * x) * sin(theta);
+    double const new_pz = sqrt(one_plus_delta * one_plus_delta - new_px * new_px - py * py);
+    double const st = sin(theta);
+    double const new_x = x * cos(theta) +
+                         (x * px * sin(2 * theta) + (st * st) * (2 * x * pz - b1 * (x * x))) /
+                             (new_pz + pz * cos(theta) - px * sin(theta));
+    double const D = asin(A * px) - asin(A * new_px);
+    double const delta_y = py * (theta + D) / b1;
+    double const delta_ell = one_plus_delta * (theta + D) / b1;
+    p->x = new_x;
+    p->y += delta_y;
+    p->px = new_px;
+    p->zeta += -delta_ell / rvv;
+}
+
+/* track_wedge.h:60-82 */
+static void xto_quad_wedge(xto_part* p, double theta, double k1) {
+    double const b2 = k1 * p->chi;
+    double const x = p->x, y = p->y, px = p->px, py = p->py;
+    double const new_px = px - b2 * x * x * theta + b2 * y * y / 2 * theta;
+    double const new_py = py + b2 * x * y * theta;
+    p->px = new_px;
+    p->py = new_py;
+}
+
+/* track_magnet_edge.h:16-158: linear (0), full (1), dipole-only (2),
+ * ax/ay-only (3) and suppressed (-1) models. */
 static void xto_magnet_edge(xto_part* p, int model, int is_exit, double half_gap,
-                            const double* knorm, const double* knl,
-                            double factor_knl_ksl, int64_t kl_order,
+                            const double* knorm, const double* kskew, const double* knl,
+                            const double* ksl, double factor_knl_ksl, int64_t kl_order,
                             const double* knl_rel, double factor_knl_ksl_rel,
                             int64_t order_rel, double length, double face_angle,
                             double face_angle_feed_down, double fringe_integral,
@@ -665,6 +879,44 @@ static void xto_magnet_edge(xto_part* p, int model, int is_exit, double half_gap
         double const chi = p->chi;
         p->px += chi * r21 * x;
         p->py += chi * r43 * y;
+        return;
+    } else if (model == 1 || model == 2) {
+        /* the kill runs in its own per-particle block; the blocks that
+         * follow (the fringe maps, the body, the other edge) skip the
+         * particle, whose state is no longer positive (headers/track.h) */
+        if (factor_for_backtrack < 0) {
+            xto_kill(p, -32);
+            return;
+        }
+        int should_rotate = 0;
+        double sin_ = 0, cos_ = 1, tan_ = 0;
+        if (fabs(face_angle) > 10e-10) {
+            should_rotate = 1;
+            sin_ = sin(face_angle);
+            cos_ = cos(face_angle);
+            tan_ = tan(face_angle);
+        }
+        if (is_exit) k0 = -k0;
+        int64_t const k_order = 3;
+        if (is_exit == 0) {
+            if (should_rotate) xto_yrotation(p, -sin_, cos_, -tan_);
+            xto_dipole_fringe(p, fringe_integral, half_gap, k0);
+            if (model == 1)
+                xto_mult_fringe(p, knorm, kskew, k_order, knl, ksl, kl_order,
+                                length / factor_knl_ksl, is_exit, 1);
+            if (model == 1 && should_rotate && k_order >= 1)
+                xto_quad_wedge(p, -face_angle, knorm[1]);
+            if (should_rotate && k_order >= 0) xto_wedge(p, -face_angle, knorm[0]);
+        } else {
+            if (should_rotate && k_order >= 0) xto_wedge(p, -face_angle, knorm[0]);
+            if (model == 1 && should_rotate && k_order >= 1)
+                xto_quad_wedge(p, -face_angle, knorm[1]);
+            if (model == 1)
+                xto_mult_fringe(p, knorm, kskew, k_order, knl, ksl, kl_order,
+                                length / factor_knl_ksl, is_exit, 1);
+            xto_dipole_fringe(p, fringe_integral, half_gap, k0);
+            if (should_rotate) xto_yrotation(p, -sin_, cos_, -tan_);
+        }
     }
 }
 
@@ -720,13 +972,15 @@ static void xto_track_magnet(xto_part* p, xto_magnet m) {
         factor_backtrack_edge = 1.;
     }
     double const knorm[4] = {m.k0, m.k1, m.k2, m.k3};
+    double const kskew[4] = {m.k0s, m.k1s, m.k2s, m.k3s};
 
     if (m.edge_entry_active) {
-        xto_magnet_edge(p, m.edge_entry_model, 0, m.edge_entry_hgap, knorm,
-                        m.knl, factor_knl_ksl_edge, m.order, m.knl_rel,
+        xto_magnet_edge(p, m.edge_entry_model, 0, m.edge_entry_hgap, knorm, kskew,
+                        m.knl, m.ksl, factor_knl_ksl_edge, m.order, m.knl_rel,
                         factor_knl_ksl_edge * m.rel_ref_strength, m.order_rel,
                         m.length, m.edge_entry_angle, m.edge_entry_angle_fdown,
                         m.edge_entry_fint, factor_backtrack_edge);
+        if (p->state <= 0) return;
     }
 
     if (m.body_active) {
@@ -777,8 +1031,8 @@ static void xto_track_magnet(xto_part* p, xto_magnet m) {
     }
 
     if (m.edge_exit_active) {
-        xto_magnet_edge(p, m.edge_exit_model, 1, m.edge_exit_hgap, knorm,
-                        m.knl, factor_knl_ksl_edge, m.order, m.knl_rel,
+        xto_magnet_edge(p, m.edge_exit_model, 1, m.edge_exit_hgap, knorm, kskew,
+                        m.knl, m.ksl, factor_knl_ksl_edge, m.order, m.knl_rel,
                         factor_knl_ksl_edge * m.rel_ref_strength, m.order_rel,
                         m.length, m.edge_exit_angle, m.edge_exit_angle_fdown,
                         m.edge_exit_fint, factor_backtrack_edge);
@@ -1187,8 +1441,8 @@ int32_t xto_validate(const xtg_element* els, int64_t n, char* msg, int64_t msg_l
             int const exit_ = e->edge_exit_active && (e->slice == XTG_SLICE_NONE || e->slice == XTG_SLICE_EXIT);
             int const em_in = (e->cls == XTG_CLS_BEND) ? e->edge_entry_model : 1;
             int const em_out = (e->cls == XTG_CLS_BEND) ? e->edge_exit_model : 1;
-            if ((entry && (em_in == 1 || em_in == 2)) || (exit_ && (em_out == 1 || em_out == 2)))
-                why = "full / dipole-only fringe models are not supported";
+            if ((entry && (em_in < -1 || em_in > 3)) || (exit_ && (em_out < -1 || em_out > 3)))
+                why = "unknown edge model";
             if (e->integrator < 0 || e->integrator > 3) why = "unknown integrator";
         } else if (e->cls == XTG_CLS_CAVITY) {
             int64_t model = e->model == 0 ? 6 : e->model;

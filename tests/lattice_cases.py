@@ -71,6 +71,50 @@ def element_zoo(seed=3):
     return xt.Line(elements=els, element_names=names)
 
 
+def fringe_zoo(seed=5):
+    """Magnets with the nonlinear edge models: bends with the full and the
+    dipole-only fringe (face angles, fringe integrals, gaps, normal and skew
+    multipoles), and quadrupoles, sextupoles and octupoles with active
+    edges (their edges use the full model)."""
+    rng = np.random.default_rng(seed)
+    els, names = [], []
+
+    def add(name, e):
+        names.append(name)
+        els.append(e)
+
+    angle = 2 * math.pi / 1104
+    add("d0", xt.Drift(length=0.5))
+    for k, (em, e1, e2, fint, hgap) in enumerate([
+            ("full", 0.01, -0.005, 0.4, 0.02), ("full", 0.0, 0.0, 0.5, 0.03),
+            ("dipole-only", 0.008, 0.004, 0.6, 0.025), ("full", -0.012, 0.02, 0.0, 0.0),
+            ("dipole-only", 0.0, 0.0, 0.0, 0.0)]):
+        add(f"b{k}", xt.Bend(length=2.0, angle=angle * (1 + k), k1=1e-3 * (-1) ** k,
+                             knl=[0, 2e-4, 1e-3, 1e-2], ksl=[1e-6, 1e-4, 5e-4],
+                             knl_rel=_errs(rng, 8, 1e-4), ksl_rel=_errs(rng, 8, 1e-4),
+                             model="drift-kick-drift-expanded", integrator="uniform",
+                             num_multipole_kicks=3, edge_entry_model=em, edge_exit_model=em,
+                             edge_entry_angle=e1, edge_exit_angle=e2, edge_entry_fint=fint,
+                             edge_exit_fint=fint * 0.8, edge_entry_hgap=hgap,
+                             edge_exit_hgap=hgap * 1.1))
+        add(f"db{k}", xt.Drift(length=0.3))
+    add("b_mixed", xt.Bend(length=1.5, angle=angle, edge_entry_model="full",
+                           edge_exit_model="linear", edge_entry_angle=0.005, edge_exit_angle=0.003,
+                           edge_entry_fint=0.5, edge_entry_hgap=0.02))
+    add("q_edges", xt.Quadrupole(length=1.1, k1=0.01, k1s=-2e-3, edge_entry_active=True,
+                                 edge_exit_active=True, knl=[0, 0, 1e-3, 5e-3],
+                                 ksl=[0, 0, 2e-4], num_multipole_kicks=4,
+                                 model="drift-kick-drift-expanded", integrator="uniform"))
+    add("q_entry", xt.Quadrupole(length=0.8, k1=-0.008, edge_entry_active=True,
+                                 num_multipole_kicks=2))
+    add("s_edges", xt.Sextupole(length=0.37, k2=0.1, k2s=0.02, edge_entry_active=True,
+                                edge_exit_active=True, num_multipole_kicks=3))
+    add("o_edges", xt.Octupole(length=0.3, k3=2.0, k3s=0.5, edge_exit_active=True,
+                               num_multipole_kicks=2, integrator="teapot"))
+    add("d_end", xt.Drift(length=0.4))
+    return xt.Line(elements=els, element_names=names)
+
+
 def sliced_line(thin=True):
     """A short ring of thick magnets sliced thin (Teapot) or thick (Uniform)."""
     angle = 0.01

@@ -130,6 +130,22 @@ def test_element_zoo(arith, flags):
     compare(got, ref, 5e-14 if arith == "exact" else 1e-10)
 
 
+@pytest.mark.parametrize("arith", ["exact", "fast"])
+@pytest.mark.parametrize("flags", [0, 1 << 0, 1 << 3])
+def test_fringe_zoo(arith, flags):
+    """Full and dipole-only edge models (dipole fringe, multipole fringe,
+    wedges, face rotations) and quadrupole/sextupole/octupole edges. The
+    per-particle atan/cos/tan/asin of the fringe maps come from the device
+    libm, hence the 5e-14 of the exact mode; backtracking kills every
+    particle at its first nonlinear edge (state -32), as the reference does."""
+    from lattice_cases import fringe_zoo
+    recs, arrs, L = _setup(fringe_zoo(), small_beam(256, seed=19, scale=0.5))
+    got, ref = _run_both(recs, arrs, L, arith=arith, num_turns=2, track_flags=flags)
+    compare(got, ref, 5e-14 if arith == "exact" else 1e-10)
+    if flags & 1:
+        assert np.all(got["state"] == -32)
+
+
 @pytest.mark.parametrize("cfg", [{"use_exact_drifts": True}, {"cavity_preserve_angle": True},
                                  {"global_xy_limit": None}, {"global_xy_limit": 0.005}])
 def test_config_switches(cfg):

@@ -53,9 +53,8 @@ def test_ctypes_layout_matches_c():
 
 
 @pytest.mark.parametrize("element,msg", [
-    (xt.Bend(length=1.0, angle=0.01, edge_entry_model="full"), "fringe"),
-    (xt.Quadrupole(length=1.0, k1=0.1, edge_entry_active=True), "fringe"),
     (xt.Bend(length=1.0, angle=0.01, model=42), "model"),
+    (xt.Bend(length=1.0, angle=0.01, edge_entry_model=7), "edge model"),
 ])
 def test_unsupported_elements_rejected_before_device(element, msg):
     line = xt.Line(elements=[xt.Drift(length=1.0), element])

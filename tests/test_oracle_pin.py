@@ -9,7 +9,7 @@ import pytest
 import pyoracle
 import xtrack_gb300 as xt
 from xtrack_gb300 import workloads
-from lattice_cases import element_zoo, sliced_line, small_beam
+from lattice_cases import element_zoo, fringe_zoo, sliced_line, small_beam
 
 pyoracle.ensure_built(with_ref=True)
 pytestmark = pytest.mark.skipif(not pyoracle.ref_available(),
@@ -55,6 +55,19 @@ def test_element_zoo(flags, cfg):
     line = element_zoo()
     a, b = _both(line, small_beam(64, seed=3, scale=0.3), num_turns=2, track_flags=flags, **cfg)
     _assert_identical(a, b)
+
+
+@pytest.mark.parametrize("flags", [0, 1 << 0, 1 << 3])
+def test_fringe_zoo(flags):
+    """Full and dipole-only edge models (and the kill of backtracked
+    particles at such edges) bit for bit against the reference's code."""
+    line = fringe_zoo()
+    a, b = _both(line, small_beam(64, seed=9, scale=0.5), num_turns=2, track_flags=flags)
+    _assert_identical(a, b)
+    if flags & 1:
+        assert np.all(a["state"] == -32)
+    else:
+        assert (a["state"] > 0).sum() > 50
 
 
 @pytest.mark.parametrize("thin", [True, False])

@@ -136,13 +136,22 @@ def make_monitor(start, stop, pid_range, fields=("x", "px", "y", "py", "zeta", "
 
 
 def rel_err(a, b, field):
-    """max |a-b| / max(|b|) over the array (scale-relative error)."""
+    """max |a-b| / max(|b|) over the array (scale-relative error). Equal
+    values (infinities of a killed particle included) count as zero error,
+    two NaNs as equal; the scale ignores non-finite values and the 1e30 that
+    a killed particle's coordinates are set to."""
     a = np.asarray(a, dtype=np.float64)
     b = np.asarray(b, dtype=np.float64)
-    scale = np.max(np.abs(b)) if b.size else 1.0
+    if not b.size:
+        return 0.0
+    fin = np.isfinite(b) & (np.abs(b) < 1e29)
+    scale = np.max(np.abs(b[fin])) if fin.any() else 1.0
     if scale == 0:
         scale = 1.0
-    return float(np.max(np.abs(a - b)) / scale) if b.size else 0.0
+    same = (a == b) | (np.isnan(a) & np.isnan(b))
+    if same.all():
+        return 0.0
+    return float(np.max(np.abs(a[~same] - b[~same])) / scale)
 
 
 def compare(got, ref, coord_tol, fields=COORDS, mask=None):

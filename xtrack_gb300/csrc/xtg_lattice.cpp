@@ -289,6 +289,58 @@ void edge_linear(const MagnetIn& m, bool exit, double factor_knl_ksl_edge,
     *r43 = r43_out * factor_for_backtrack;
 }
 
+// Parameter block of one nonlinear edge (track_magnet_edge.h:40-50 for the
+// fringe's k0, 83-158 for the rest); layout FR_* of xtg_table.h. The
+// trigonometric values of the face angle are evaluated here once, with the
+// same libm calls the reference makes per particle.
+std::vector<double> fringe_block(const MagnetIn& m, bool exit, int model, double factor_knl_ksl_edge) {
+    std::vector<double> fr(FR_KNL, 0.0);
+    double k0 = 0;
+    k0 += m.k0;
+    if (std::fabs(m.length) > 1e-10 && m.order > -1) {
+        k0 += factor_knl_ksl_edge * m.knl[0] / m.length;
+    }
+    double const factor_rel = factor_knl_ksl_edge * m.rel_ref_strength;
+    if (std::fabs(m.length) > 1e-10 && m.order_rel > -1 && m.knl_rel != nullptr) {
+        k0 += factor_rel * m.knl_rel[0] / m.length;
+    }
+    if (exit) k0 = -k0;
+    double const face = exit ? m.edge_exit_angle : m.edge_entry_angle;
+    fr[FR_MODEL] = model;
+    fr[FR_IS_EXIT] = exit ? 1.0 : 0.0;
+    fr[FR_K0] = k0;
+    fr[FR_FINT] = exit ? m.edge_exit_fint : m.edge_entry_fint;
+    fr[FR_HGAP] = exit ? m.edge_exit_hgap : m.edge_entry_hgap;
+    fr[FR_FACE_ANGLE] = face;
+    if (std::fabs(face) > 10e-10) {
+        fr[FR_ROTATE] = 1.0;
+        fr[FR_SIN] = std::sin(face);
+        fr[FR_COS] = std::cos(face);
+        fr[FR_TAN] = std::tan(face);
+    } else {
+        fr[FR_ROTATE] = 0.0;
+        fr[FR_SIN] = 0.0;
+        fr[FR_COS] = 1.0;
+        fr[FR_TAN] = 0.0;
+    }
+    double const theta = -face;
+    fr[FR_WSIN] = std::sin(theta);
+    fr[FR_WCOS] = std::cos(theta);
+    fr[FR_WTAN] = std::tan(theta);
+    fr[FR_WSIN2] = std::sin(2 * theta);
+    fr[FR_LENGTH] = m.length / factor_knl_ksl_edge;
+    fr[FR_KL_ORDER] = (double)m.order;
+    double const kn[4] = {m.k0, m.k1, m.k2, m.k3};
+    double const ks[4] = {m.k0s, m.k1s, m.k2s, m.k3s};
+    for (int i = 0; i < 4; i++) {
+        fr[FR_KNORM + i] = kn[i];
+        fr[FR_KSKEW + i] = ks[i];
+    }
+    for (int64_t i = 0; i <= m.order; i++) fr.push_back(m.knl[i]);
+    for (int64_t i = 0; i <= m.order; i++) fr.push_back(m.ksl[i]);
+    return fr;
+}
+
 // Builds the reference-arithmetic coefficient quintuples of one
 // kick_simple pass. Returns the effective top order (-1 when all zero).
 int32_t exact_pass_coefs(int64_t order, double inv_factorial, const double* knl,
@@ -344,8 +396,8 @@ int32_t validate_element(const xtg_element& e, int64_t idx, std::string* why) {
         int em_in = (e.cls == XTG_CLS_BEND) ? e.edge_entry_model : 1;
         int em_out = (e.cls == XTG_CLS_BEND) ? e.edge_exit_model : 1;
         if (e.cls == XTG_CLS_MULTIPOLE) entry = exit_ = false;
-        if ((entry && (em_in == 1 || em_in == 2)) || (exit_ && (em_out == 1 || em_out == 2)))
-            return fail("full / dipole-only fringe models are not supported");
+        if ((entry && (em_in < -1 || em_in > 3)) || (exit_ && (em_out < -1 || em_out > 3)))
+            return fail("unknown edge model");
         if (e.slice == XTG_SLICE_ENTRY || e.slice == XTG_SLICE_EXIT) {
             if (e.cls == XTG_CLS_MULTIPOLE) return fail("Multipole has no entry/exit slices");
         }
@@ -433,6 +485,22 @@ void pack_magnet(const xtg_element& e, bool backtrack, bool exact, RecBuf* rb) {
             R()->exit_r21 = r21;
             R()->exit_r43 = r43;
         }
+    }
+    // nonlinear edges (full / dipole-only models): parameter blocks
+    R()->backtrack = backtrack ? 1 : 0;
+    if (m.edge_entry_active && (m.edge_entry_model == 1 || m.edge_entry_model == 2)) {
+        std::vector<double> fr = fringe_block(m, false, m.edge_entry_model, factor_edge);
+        rb->pad16();
+        int32_t off = rb->append(fr.data(), fr.size(), coef_base);
+        R()->edge_entry = EDGE_FRINGE;
+        R()->entry_fringe = off;
+    }
+    if (m.edge_exit_active && (m.edge_exit_model == 1 || m.edge_exit_model == 2)) {
+        std::vector<double> fr = fringe_block(m, true, m.edge_exit_model, factor_edge);
+        rb->pad16();
+        int32_t off = rb->append(fr.data(), fr.size(), coef_base);
+        R()->edge_exit = EDGE_FRINGE;
+        R()->exit_fringe = off;
     }
 
     if (m.body_active) {
@@ -836,6 +904,10 @@ double canonical_flops(const unsigned char* rec) {
         double f = 0;
         if (r->edge_entry == EDGE_LINEAR && (r->entry_r21 != 0 || r->entry_r43 != 0)) f += 4;
         if (r->edge_exit == EDGE_LINEAR && (r->exit_r21 != 0 || r->exit_r43 != 0)) f += 4;
+        // nonlinear edge: dipole fringe ~60, multipole fringe ~40 per order
+        const double* cf = reinterpret_cast<const double*>(rec + sizeof(MagnetRec));
+        if (r->edge_entry == EDGE_FRINGE) f += 60.0 + 40.0 * (4 + cf[r->entry_fringe + FR_KL_ORDER]);
+        if (r->edge_exit == EDGE_FRINGE) f += 60.0 + 40.0 * (4 + cf[r->exit_fringe + FR_KL_ORDER]);
         if (!r->body_active) return f;
         double const dr = (r->drift_model == 1) ? drift_exact : (r->drift_model == 0 ? drift_exp : 40.0);
         if (r->only_drift) return f + (r->drift_model < 0 ? 0 : dr);

@@ -484,9 +484,273 @@ XTG_DEV void magnet_kick(PState& p, const MagnetRec& r, const double* __restrict
     apply_kick<kExact>(p, kick_args(r, k), coefs);
 }
 
-// track_magnet_edge.h:16-80 with the linear model (track_dipole_edge_linear.h)
-XTG_DEV void magnet_edge(PState& p, int kind, bool is_exit, double r21, double r43) {
+// ---------------------------------------------------------------------------
+// Nonlinear edges: the "full" (1) and "dipole-only" (2) edge models of
+// track_magnet_edge.h:83-158. Cold code: two calls per magnet at most.
+// The parameters of one edge are a FringeRec block of doubles in the
+// record's coefficient area (layout: xtg_table.h, FR_*). The arithmetic
+// follows the reference expression by expression (this path is shared by
+// both arithmetic modes).
+// ---------------------------------------------------------------------------
+
+// local_particle_custom_api.h:20-33 (update_delta)
+XTG_DEV void set_delta_and_energy(PState& p, double new_delta) {
+    double const beta0 = p.beta0;
+    double const delta_beta0 = new_delta * beta0;
+    double const ptau_beta0 = sqrt(delta_beta0 * delta_beta0 + 2. * delta_beta0 * beta0 + 1.) - 1.;
+    p.delta = new_delta;
+    p.rvv = (1. + new_delta) / (1. + ptau_beta0);
+    p.rpp = 1. / (1. + new_delta);
+    p.ptau = ptau_beta0 / beta0;
+}
+
+// local_particle_custom_api.h:248-256
+XTG_DEV void kill_particle(PState& p, int64_t kill_state) {
+    p.x = 1e30;
+    p.px = 1e30;
+    p.y = 1e30;
+    p.py = 1e30;
+    p.zeta = 1e30;
+    set_delta_and_energy(p, -1.);
+    refresh_energy_cache(p);
+    p.state = kill_state;
+}
+
+// track_yrotation.h:13-48 (spin off)
+XTG_DEV void y_rotation(PState& p, double sin_a, double cos_a, double tan_a) {
+    double const beta0 = p.beta0;
+    double const x = p.x, y = p.y, px = p.px, py = p.py;
+    double const t = p.zeta / beta0;
+    double const pt = (p.ptau / beta0) * beta0;
+    double const pz = sqrt(1.0 + 2.0 * pt / beta0 + pt * pt - px * px - py * py);
+    double const ptt = 1.0 + tan_a * px / pz;
+    double const x_hat = x / (cos_a * ptt);
+    double const px_hat = cos_a * px - sin_a * pz;
+    double const y_hat = y - tan_a * x * py / (pz * ptt);
+    double const t_hat = t + tan_a * x * (1.0 / beta0 + pt) / (pz * ptt);
+    p.x = x_hat;
+    p.px = px_hat;
+    p.y = y_hat;
+    p.zeta = t_hat * beta0;
+}
+
+// track_dipole_fringe.h:16-82 (MAD-NG form)
+XTG_DEV void dipole_fringe(PState& p, double fint, double hgap, double k0) {
+    if (fabs(k0) < 10e-10) return;
+    double const beta0 = p.beta0;
+    double const x = p.x, px = p.px, y = p.y, py = p.py;
+    double const t = p.zeta / beta0;
+    double const pt = p.ptau;
+    double const delta = p.delta;
+    double const fh = hgap * fint;
+    double const fsad = (fh > 10e-10) ? 1. / (72 * fh) : 0;
+    double const b0 = k0 * p.chi;
+    double const inv_beta = 1. / beta0;
+    double const dpp = (1. + delta) * (1. + delta);
+    double const pz = sqrt(dpp - px * px - py * py);
+    double const ipz = 1. / pz;
+    double const relp = 1. / sqrt(dpp);
+    double const tfac = -(inv_beta + pt);
+    double const c2 = b0 * fh * 2;
+    double const c3 = b0 * b0 * fsad * relp;
+    double const xp = px / pz;
+    double const yp = py / pz;
+    double const xyp = xp * yp;
+    double const yp2 = 1. + yp * yp;
+    double const xp2 = xp * xp;
+    double const iyp2 = 1. / yp2;
+    double const fi0 = atan(xp * iyp2) - c2 * (1 + xp2 * (1 + yp2)) * ipz;
+    double const cf = cos(fi0);
+    double const co2 = b0 / (cf * cf);
+    double const xq = xp * iyp2;
+    double const co1 = co2 / (1 + xq * xq) * iyp2;
+    double const co3 = co2 * c2;
+    double const fi1 = co1 - co3 * 2 * xp * (1 + yp2) * ipz;
+    double const fi2 = -2 * co1 * xyp * iyp2 - co3 * 2 * xp * xyp * ipz;
+    double const fi3 = +co3 * (1 + xp2 * (1 + yp2)) * (ipz * ipz);
+    double const kx = fi1 * (1 + xp2) * ipz + fi2 * xyp * ipz - fi3 * xp;
+    double const ky = fi1 * xyp * ipz + fi2 * yp2 * ipz - fi3 * yp;
+    double const ipz2 = ipz * ipz;
+    double const kz = fi1 * tfac * xp * ipz2 + fi2 * tfac * yp * ipz2 - fi3 * tfac * ipz;
+    double const new_y = 2 * y / (1 + sqrt(1 - 2 * ky * y));
+    double const ny2 = new_y * new_y;
+    double const new_x = x + 0.5 * kx * ny2;
+    double const new_py = py - 4 * c3 * (ny2 * new_y) - b0 * tan(fi0) * new_y;
+    double const new_t = t + 0.5 * kz * ny2 + c3 * (new_y * new_y * new_y * new_y) * (relp * relp) * tfac;
+    p.x = new_x;
+    p.y = new_y;
+    p.py = new_py;
+    p.zeta = new_t * beta0;
+}
+
+// track_mult_fringe.h:12-128 with k_order = 3, min_order = 1
+XTG_DEV void mult_fringe(PState& p, const double* kn, const double* ks, const double* knl,
+                         const double* ksl, int64_t kl_order, double length, bool is_exit,
+                         bool backtrack) {
+    if (backtrack) {
+        kill_particle(p, -32);
+        return;
+    }
+    int64_t const k_order = 3;
+    double const beta0 = p.beta0;
+    double const direction = is_exit ? -1 : 1;
+    double const x = p.x, px = p.px, y = p.y, py = p.py;
+    double const t = p.zeta / beta0;
+    double const pt = p.ptau;
+    double const rpp = p.rpp;
+    double const chi = p.chi;
+    double rx = 1, ix = 0;
+    double fx = 0, fxx = 0, fxy = 0, fy = 0, fyx = 0, fyy = 0;
+    int64_t const order = (k_order > kl_order) ? k_order : kl_order;
+    double inv_factorial = 1;
+    for (int64_t ii = 0; ii <= order; ii++) {
+        if (ii > 1) inv_factorial /= ii;
+        double const component = ii + 1;
+        double const drx = rx, dix = ix;
+        rx = drx * x - dix * y;
+        ix = drx * y + dix * x;
+        double kn_total = 0, ks_total = 0;
+        if (ii >= 1) {
+            if (ii <= k_order) {
+                kn_total += kn[ii] * inv_factorial;
+                ks_total += ks[ii] * inv_factorial;
+            }
+            if (ii <= kl_order && length != 0.) {
+                kn_total += knl[ii] / length * inv_factorial;
+                ks_total += ksl[ii] / length * inv_factorial;
+            }
+        }
+        double const nj = -direction / (4 * (component + 1));
+        double const nf = (component + 2) / component;
+        double const kj = kn_total * chi;
+        double const ksj = ks_total * chi;
+        double u, v, du, dv;
+        if (ii == 0) {
+            u = nj * (-ksj * ix);
+            v = nj * (ksj * rx);
+            du = nj * (-ksj * dix);
+            dv = nj * (ksj * drx);
+        } else {
+            u = nj * (kj * rx - ksj * ix);
+            v = nj * (kj * ix + ksj * rx);
+            du = nj * (kj * drx - ksj * dix);
+            dv = nj * (kj * dix + ksj * drx);
+        }
+        double const dux = component * du;
+        double const dvx = component * dv;
+        double const duy = -component * dv;
+        double const dvy = component * du;
+        fx = fx + u * x + nf * v * y;
+        fy = fy + u * y - nf * v * x;
+        fxx = fxx + dux * x + nf * dvx * y + u;
+        fyy = fyy + duy * y - nf * dvy * x + u;
+        fxy = fxy + duy * x + nf * (dvy * y + v);
+        fyx = fyx + dux * y - nf * (dvx * x + v);
+    }
+    double const a = 1 - fxx * rpp;
+    double const b = -fyx * rpp;
+    double const c = -fxy * rpp;
+    double const d = 1 - fyy * rpp;
+    double const det = (a * d - b * c);
+    double const new_px = (d * px - b * py) / det;
+    double const new_py = (a * py - c * px) / det;
+    double const delta_t = (1 / beta0 + pt) * (new_px * fx + new_py * fy) * (rpp * rpp * rpp);
+    p.x = p.x + -fx * rpp;
+    p.y = p.y + -fy * rpp;
+    p.px = new_px;
+    p.py = new_py;
+    p.zeta = (t + delta_t) * beta0;
+}
+
+// track_wedge.h:14-58 (spin off); the trigonometric values of theta come
+// from the host
+XTG_DEV void wedge(PState& p, double theta, double sin_t, double cos_t, double tan_t,
+                   double sin_2t, double k0) {
+    double const b1 = k0 * p.chi;
+    if (fabs(b1) < 10e-10) {
+        y_rotation(p, -sin_t, cos_t, -tan_t);
+        return;
+    }
+    double const rvv = p.rvv;
+    double const x = p.x, px = p.px, py = p.py;
+    double const opd = p.delta + 1.0;
+    double const A = 1.0 / sqrt(opd * opd - py * py);
+    double const pz = sqrt(opd * opd - px * px - py * py);
+    double const new_px = px * cos_t + (pz - b1 * x) * sin_t;
+    double const new_pz = sqrt(opd * opd - new_px * new_px - py * py);
+    double const new_x = x * cos_t +
+                         (x * px * sin_2t + (sin_t * sin_t) * (2 * x * pz - b1 * (x * x))) /
+                             (new_pz + pz * cos_t - px * sin_t);
+    double const D = asin(A * px) - asin(A * new_px);
+    double const delta_y = py * (theta + D) / b1;
+    double const delta_ell = opd * (theta + D) / b1;
+    p.x = new_x;
+    p.y = p.y + delta_y;
+    p.px = new_px;
+    p.zeta = p.zeta + -delta_ell / rvv;
+}
+
+// track_wedge.h:60-82
+XTG_DEV void quad_wedge(PState& p, double theta, double k1) {
+    double const b2 = k1 * p.chi;
+    double const x = p.x, y = p.y, px = p.px, py = p.py;
+    double const new_px = px - b2 * x * x * theta + b2 * y * y / 2 * theta;
+    double const new_py = py + b2 * x * y * theta;
+    p.px = new_px;
+    p.py = new_py;
+}
+
+// track_magnet_edge.h:83-158 for one edge; the ax/ay reset of
+// track_magnet_edge.h:51-61 is done by the caller. The backtracking
+// variants kill the particle (state -32) as the reference does; the kill
+// leaves the particle with the kill values (the reference goes on
+// applying the map to them).
+XTG_COLD PState fringe_edge(PState p, const double* __restrict__ fr, bool backtrack) {
+    int const model = (int)fr[FR_MODEL];
+    bool const is_exit = fr[FR_IS_EXIT] != 0.;
+    if (backtrack) {
+        kill_particle(p, -32);
+        return p;
+    }
+    bool const rot = fr[FR_ROTATE] != 0.;
+    double const theta = -fr[FR_FACE_ANGLE];
+    const double* kn = fr + FR_KNORM;
+    const double* ks = fr + FR_KSKEW;
+    int64_t const kl_order = (int64_t)fr[FR_KL_ORDER];
+    const double* knl = fr + FR_KNL;
+    const double* ksl = knl + (kl_order + 1);
+    if (!is_exit) {
+        if (rot) y_rotation(p, -fr[FR_SIN], fr[FR_COS], -fr[FR_TAN]);
+        dipole_fringe(p, fr[FR_FINT], fr[FR_HGAP], fr[FR_K0]);
+        if (model == 1) mult_fringe(p, kn, ks, knl, ksl, kl_order, fr[FR_LENGTH], false, false);
+        if (model == 1 && rot) quad_wedge(p, theta, kn[1]);
+        if (rot) wedge(p, theta, fr[FR_WSIN], fr[FR_WCOS], fr[FR_WTAN], fr[FR_WSIN2], kn[0]);
+    } else {
+        if (rot) wedge(p, theta, fr[FR_WSIN], fr[FR_WCOS], fr[FR_WTAN], fr[FR_WSIN2], kn[0]);
+        if (model == 1 && rot) quad_wedge(p, theta, kn[1]);
+        if (model == 1) mult_fringe(p, kn, ks, knl, ksl, kl_order, fr[FR_LENGTH], true, false);
+        dipole_fringe(p, fr[FR_FINT], fr[FR_HGAP], fr[FR_K0]);
+        if (rot) y_rotation(p, -fr[FR_SIN], fr[FR_COS], -fr[FR_TAN]);
+    }
+    return p;
+}
+
+// track_magnet_edge.h:16-80 with the linear model (track_dipole_edge_linear.h);
+// the nonlinear models go to fringe_edge
+XTG_DEV void magnet_edge(PState& p, int kind, bool is_exit, double r21, double r43,
+                         const double* __restrict__ fringe, bool backtrack) {
     if (kind == EDGE_NONE) return;
+    if (kind == EDGE_FRINGE) {
+        if (is_exit) {
+            p.ax = 0.;
+            p.ay = 0.;
+        } else {
+            p.ax = (-0.5 * 0.0) * (p.y - 0.);
+            p.ay = (0.5 * 0.0) * (p.x - 0.);
+        }
+        p = fringe_edge(p, fringe, backtrack);
+        return;
+    }
     if (is_exit) {
         p.ax = 0.;
         p.ay = 0.;

@@ -73,7 +73,28 @@ struct ExactPass {
     double factor;
 };
 
-enum : int32_t { EDGE_NONE = 0, EDGE_AXAY = 1, EDGE_LINEAR = 2 };
+enum : int32_t { EDGE_NONE = 0, EDGE_AXAY = 1, EDGE_LINEAR = 2, EDGE_FRINGE = 3 };
+
+// Parameters of one nonlinear edge (full or dipole-only model,
+// track_magnet_edge.h:83-158): a block of doubles in the record's
+// coefficient area, at MagnetRec::entry_fringe / exit_fringe.
+enum : int32_t {
+    FR_MODEL = 0,        // 1 full, 2 dipole-only
+    FR_IS_EXIT = 1,
+    FR_K0 = 2,           // dipole strength of the fringe (sign flipped at the exit)
+    FR_FINT = 3,
+    FR_HGAP = 4,
+    FR_FACE_ANGLE = 5,
+    FR_ROTATE = 6,       // |face angle| > 1e-9
+    FR_SIN = 7, FR_COS = 8, FR_TAN = 9,            // of the face angle
+    FR_WSIN = 10, FR_WCOS = 11, FR_WTAN = 12,      // of theta = -face angle
+    FR_WSIN2 = 13,                                 // sin(2 theta)
+    FR_LENGTH = 14,      // length / factor_knl_ksl (multipole fringe)
+    FR_KL_ORDER = 15,
+    FR_KNORM = 16,       // k0..k3
+    FR_KSKEW = 20,       // k0s..k3s
+    FR_KNL = 24,         // knl[0..kl_order], then ksl[0..kl_order]
+};
 
 struct alignas(16) MagnetRec {
     RecHeader h;
@@ -107,6 +128,10 @@ struct alignas(16) MagnetRec {
     double htot, Q0, Q1;
     // --- linear edges ---
     double entry_r21, entry_r43, exit_r21, exit_r43;
+    // --- nonlinear edges: FringeRec offsets (doubles) in the coefficient area ---
+    int32_t entry_fringe, exit_fringe;
+    int32_t backtrack;        // the record belongs to a backtracking table
+    int32_t reserved_fr;
     // --- exact kick passes: knl, knl_rel, main strengths ---
     ExactPass pass[3];
     // coefficient area follows (doubles)

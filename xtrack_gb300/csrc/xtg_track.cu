@@ -270,9 +270,12 @@ __device__ __forceinline__ bool apply_record(PState& p, const unsigned char* __r
     case OP_MAGNET: {
         const MagnetRec& r = *reinterpret_cast<const MagnetRec*>(rec);
         const double* coefs = reinterpret_cast<const double*>(rec + sizeof(MagnetRec));
-        magnet_edge(p, r.edge_entry, false, r.entry_r21, r.entry_r43);
+        magnet_edge(p, r.edge_entry, false, r.entry_r21, r.entry_r43, coefs + r.entry_fringe,
+                    r.backtrack != 0);
+        if (p.state <= 0) break;   // killed by a nonlinear edge while backtracking
         if (r.body_active) magnet_body<kExact>(p, r, coefs);
-        magnet_edge(p, r.edge_exit, true, r.exit_r21, r.exit_r43);
+        magnet_edge(p, r.edge_exit, true, r.exit_r21, r.exit_r43, coefs + r.exit_fringe,
+                    r.backtrack != 0);
         break;
     }
     case OP_CAVITY: {
