@@ -350,15 +350,16 @@ def run_da_screen(args):
     train_lines = [workloads.thick_ring(seed=100 + s) for s in range(args.da_train_seeds)]
     test_lines = [workloads.thick_ring(seed=200 + s) for s in range(args.da_test_seeds)]
     t0 = time.perf_counter()
-    s_train = sc.build_scan(train_lines, counts(len(train_lines)), device=dev,
+    s_train = sc.build_scan(train_lines, counts(len(train_lines)), r_max=args.da_rmax, device=dev,
                             features=sg.seed_features)
-    s_test = sc.build_scan(test_lines, counts(len(test_lines)), device=dev,
+    s_test = sc.build_scan(test_lines, counts(len(test_lines)), r_max=args.da_rmax, device=dev,
                            features=sg.seed_features)
     t_setup = time.perf_counter() - t0
     bt_train = BatchTracker(train_lines, device=dev, arith=args.arith)
     bt_test = BatchTracker(test_lines, device=dev, arith=args.arith)
+    # small blocks keep a screened (small) particle set spread over the SMs
     for bt in (bt_train, bt_test):
-        bt.set_tuning(compact_every=max(1, turns // 10))
+        bt.set_tuning(compact_every=max(1, turns // 10), block_size=64, chunk_bytes=16384)
 
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
@@ -401,7 +402,7 @@ def run_da_screen(args):
            "unit": "x (plain time / screened time)", "higher_is_better": True, "n_gpus": 1,
            "dtype": "f64 tracking, bf16/f32 network", "data": "synthetic",
            "config": {"workload": "thick LHC-like ring seeds (6993 elements), polar grid "
-                                  "0-20 sigma x 11 angles x delta in {0, 2.7e-4}",
+                                  f"0-{args.da_rmax:g} sigma x 11 angles x delta in {{0, 2.7e-4}}",
                       "turns": turns, "train_seeds": len(train_lines),
                       "test_seeds": n_seeds, "train_particles": int(s_train.n),
                       "test_particles": int(s_test.n), "radial_step_sigma": grid_step,
@@ -446,6 +447,9 @@ def main():
                     help="record 6 coordinates per turn of the first N particles")
     ap.add_argument("--workload", default="thick_ring", choices=["thick_ring", "da_screen"])
     ap.add_argument("--da-turns", dest="da_turns", type=int, default=300)
+    ap.add_argument("--da-rmax", dest="da_rmax", type=float, default=80.0,
+                    help="largest amplitude of the grid (sigma); the synthetic ring at 7 TeV "
+                         "keeps everything within 20 sigma, its DA lies near the aperture")
     ap.add_argument("--da-particles", dest="da_particles", type=int, default=20000,
                     help="mean particles per seed (uniform in [n/2, 3n/2])")
     ap.add_argument("--da-train-seeds", dest="da_train_seeds", type=int, default=6)

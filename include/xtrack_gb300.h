@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define XTG_ABI_VERSION 1
+#define XTG_ABI_VERSION 2
 
 /* Maximum number of multipole coefficients per array (order <= 20). */
 #define XTG_MAX_KNL 21
@@ -56,7 +56,8 @@ extern "C" {
 #define XTG_CLS_CAVITY          7   /* cavity.py, cavity.h                   */
 #define XTG_CLS_LIMIT_ELLIPSE   8   /* limit_ellipse.py, limitellipse.h      */
 #define XTG_CLS_LIMIT_RECT      9   /* limit_rect.py, limitrect.h            */
-#define XTG_NUM_CLS            10
+#define XTG_CLS_MONITOR        10   /* monitors/*.py placed in the line      */
+#define XTG_NUM_CLS            11
 
 /* Slice kind of a record (slice classes of slice_elements_*.py). A slice
  * record carries its parent's parameters plus its own `weight`. */
@@ -116,6 +117,10 @@ typedef struct xtg_element {
     /* Misalignment fields (base_element.py:274-282); must all be zero. */
     double shift_x, shift_y, shift_s;
     double rot_x_rad, rot_y_rad, rot_s_rad, rot_s_rad_no_frame;
+    /* XTG_CLS_MONITOR: host address of an xtg_element_monitor, read by
+     * xtg_lattice_create (its buffers are device pointers kept by the
+     * caller for the lattice's lifetime); 0 for the other classes. */
+    uint64_t monitor;
 } xtg_element;
 
 /*
@@ -152,6 +157,39 @@ typedef struct xtg_monitor {
     int64_t n_records;
     xtg_particles data;
 } xtg_monitor;
+
+/*
+ * A monitor placed in the line as an element (monitors/*.py). kind:
+ *   XTG_MON_PARTICLES      ParticlesMonitor as an element: the records of
+ *                          `particles` (same layout as the turn-by-turn
+ *                          monitor), written each time a particle passes;
+ *   XTG_MON_LAST_TURNS     LastTurnsMonitor (last_turns_monitor.h): a
+ *                          rolling buffer of the last `n_last_turns` passes
+ *                          (every `every_n_turns` turns) of particles
+ *                          [particle_id_start, +num_particles), float32
+ *                          coordinates and uint32 ids/turns;
+ *   XTG_MON_BEAM_POSITION  BeamPositionMonitor (beam_position_monitor.h):
+ *                          per sample slot, the count and the sums of x and
+ *                          y of the particles that pass (atomic adds; the
+ *                          summation order is not fixed).
+ */
+#define XTG_MON_PARTICLES     1
+#define XTG_MON_LAST_TURNS    2
+#define XTG_MON_BEAM_POSITION 3
+
+typedef struct xtg_element_monitor {
+    int32_t kind;
+    int32_t reserved;
+    int64_t particle_id_start;      /* LAST_TURNS, BEAM_POSITION              */
+    int64_t num_particles;          /* BEAM_POSITION: -1 means all particles  */
+    int64_t n_last_turns, every_n_turns;          /* LAST_TURNS              */
+    int64_t start_at_turn, n_slots;               /* BEAM_POSITION           */
+    double frev, sampling_frequency;              /* BEAM_POSITION           */
+    uint32_t *lost_at_offset, *lt_particle_id, *lt_at_turn;   /* LAST_TURNS */
+    float *lt_x, *lt_px, *lt_y, *lt_py, *lt_delta, *lt_zeta;
+    double *count, *x_sum, *y_sum;                /* BEAM_POSITION           */
+    xtg_monitor particles;                        /* PARTICLES               */
+} xtg_element_monitor;
 
 /* Compile-time TrackerConfig equivalents (line.py:283-287). */
 typedef struct xtg_config {

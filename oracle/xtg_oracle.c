@@ -1258,13 +1258,78 @@ static void xto_fill_magnet(const xtg_element* e, xto_magnet* m) {
     }
 }
 
+static void xto_monitor(const xtg_monitor* m, const xto_part* p, const xtg_particles* src,
+                        int64_t isrc);
+
+/* last_turns_monitor.h:17-55 */
+static void xto_last_turns(const xtg_element_monitor* m, const xto_part* p) {
+    int64_t const particle_id_stop = m->particle_id_start + m->num_particles;
+    int64_t const particle_id = p->particle_id;
+    int64_t const at_turn = p->at_turn;
+    if (at_turn >= 0 && at_turn % m->every_n_turns == 0 && m->particle_id_start <= particle_id &&
+        particle_id < particle_id_stop) {
+        int64_t const offset = (at_turn / m->every_n_turns) % m->n_last_turns;
+        int64_t const ip = particle_id - m->particle_id_start;
+        int64_t const slot = m->n_last_turns * ip + offset;
+        m->lost_at_offset[ip] = (uint32_t)offset;
+        m->lt_particle_id[slot] = (uint32_t)particle_id;
+        m->lt_at_turn[slot] = (uint32_t)at_turn;
+        m->lt_x[slot] = (float)p->x;
+        m->lt_px[slot] = (float)p->px;
+        m->lt_y[slot] = (float)p->y;
+        m->lt_py[slot] = (float)p->py;
+        m->lt_delta[slot] = (float)p->delta;
+        m->lt_zeta[slot] = (float)p->zeta;
+    }
+}
+
+/* beam_position_monitor.h:16-58 (atomic sums, as the reference's atomicAdd) */
+static void xto_bpm(const xtg_element_monitor* m, const xto_part* p) {
+    int64_t const particle_id_stop = m->particle_id_start + m->num_particles;
+    int64_t const particle_id = p->particle_id;
+    if (particle_id_stop < 0 || (m->particle_id_start <= particle_id && particle_id < particle_id_stop)) {
+        double const zeta = p->zeta;
+        double const at_turn = (double)p->at_turn;
+        double const beta0 = p->beta0;
+        int64_t const slot = (int64_t)round(m->sampling_frequency *
+                                            ((at_turn - m->start_at_turn) / m->frev - zeta / beta0 / XTO_C_LIGHT));
+        if (slot >= 0 && slot < m->n_slots) {
+            double const x = p->x, y = p->y;
+#ifdef _OPENMP
+#pragma omp atomic
+#endif
+            m->count[slot] += 1.0;
+#ifdef _OPENMP
+#pragma omp atomic
+#endif
+            m->x_sum[slot] += x;
+#ifdef _OPENMP
+#pragma omp atomic
+#endif
+            m->y_sum[slot] += y;
+        }
+    }
+}
+
 /* Applies one element to one particle. Returns whether the class is
- * statically thick (global aperture check follows, tracker.py:681-689). */
-static int xto_apply(const xtg_element* e, const xtg_config* cfg, xto_part* p) {
+ * statically thick (global aperture check follows, tracker.py:681-689).
+ * `src`/`isrc` locate the particle in its arrays (monitors copy the fields
+ * the push does not carry). */
+static int xto_apply(const xtg_element* e, const xtg_config* cfg, xto_part* p,
+                     const xtg_particles* src, int64_t isrc) {
     int const backtrack = flag_set(p, XTG_FLAG_BACKTRACK);
     switch (e->cls) {
     case XTG_CLS_MARKER:
         return 0;
+    case XTG_CLS_MONITOR: {
+        /* monitors/*.py: get_backtrack_element is a Marker */
+        const xtg_element_monitor* m = (const xtg_element_monitor*)(uintptr_t)e->monitor;
+        if (backtrack) return 0;
+        if (m->kind == XTG_MON_PARTICLES) xto_monitor(&m->particles, p, src, isrc);
+        else if (m->kind == XTG_MON_LAST_TURNS) xto_last_turns(m, p);
+        else if (m->kind == XTG_MON_BEAM_POSITION) xto_bpm(m, p);
+        return 0;
+    }
     case XTG_CLS_DRIFT: {
         /* drift.h:13-37 */
         double length = e->length;
@@ -1423,6 +1488,8 @@ int32_t xto_validate(const xtg_element* els, int64_t n, char* msg, int64_t msg_l
         const xtg_element* e = &els[i];
         const char* why = NULL;
         if (e->cls < 0 || e->cls >= XTG_NUM_CLS) why = "unknown element class";
+        else if (e->cls == XTG_CLS_MONITOR && e->monitor == 0)
+            why = "monitor element without its descriptor";
         else if (e->slice < 0 || e->slice > XTG_SLICE_EXIT) why = "unknown slice kind";
         else if (e->order < 0 || e->order >= XTG_MAX_KNL) why = "multipole order out of range";
         else if (e->order_rel < -1 || e->order_rel >= 20) why = "relative multipole order out of range (0..19)";
@@ -1582,7 +1649,7 @@ static void xto_track_one(const xto_args* a, int64_t i) {
         }
         for (; (elem_idx >= a->ele_start) && (elem_idx < ele_stop); elem_idx += increm) {
             if (a->flag_monitor == 2) xto_monitor(a->mon, &p, a->P, i);
-            if (xto_apply(&a->els[elem_idx], a->cfg, &p)) xto_global_aperture(a->cfg, &p);
+            if (xto_apply(&a->els[elem_idx], a->cfg, &p, a->P, i)) xto_global_aperture(a->cfg, &p);
             isactive = p.state > 0;
             if (!isactive) break;
             p.at_element += backtrack ? -1 : 1;
@@ -1692,7 +1759,7 @@ static void xto_track_chunk_openmp(const xto_args* a, int64_t ipart, int64_t end
                 if (P->state[i] <= 0) continue;
                 xto_load(P, i, a->flags, a->line_length, &p);
                 if (a->flag_monitor == 2) xto_monitor(a->mon, &p, P, i);
-                if (xto_apply(e, a->cfg, &p)) xto_global_aperture(a->cfg, &p);
+                if (xto_apply(e, a->cfg, &p, P, i)) xto_global_aperture(a->cfg, &p);
                 xto_store(&p, P, i);
             }
             isactive = xto_check_is_active_range(P, ipart, endpart);
@@ -1729,6 +1796,9 @@ int32_t xto_abi_sizes(int64_t* out) {
     out[4] = (int64_t)offsetof(xtg_element, knl);
     out[5] = (int64_t)offsetof(xtg_element, shift_x);
     out[6] = (int64_t)offsetof(xtg_monitor, data);
+    out[7] = (int64_t)sizeof(xtg_element_monitor);
+    out[8] = (int64_t)offsetof(xtg_element_monitor, particles);
+    out[9] = (int64_t)offsetof(xtg_element, monitor);
     return 4;
 }
 

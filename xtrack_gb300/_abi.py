@@ -37,6 +37,7 @@ CLS_OCTUPOLE = 6
 CLS_CAVITY = 7
 CLS_LIMIT_ELLIPSE = 8
 CLS_LIMIT_RECT = 9
+CLS_MONITOR = 10
 
 SLICE_NONE = 0
 SLICE_THICK = 1
@@ -95,6 +96,7 @@ class XtgElement(ctypes.Structure):
         ("shift_x", ctypes.c_double), ("shift_y", ctypes.c_double), ("shift_s", ctypes.c_double),
         ("rot_x_rad", ctypes.c_double), ("rot_y_rad", ctypes.c_double),
         ("rot_s_rad", ctypes.c_double), ("rot_s_rad_no_frame", ctypes.c_double),
+        ("monitor", ctypes.c_uint64),
     ]
 
 
@@ -132,6 +134,27 @@ class XtgMonitor(ctypes.Structure):
         ("n_repetitions", ctypes.c_int64), ("repetition_period", ctypes.c_int64),
         ("n_records", ctypes.c_int64),
         ("data", XtgParticles),
+    ]
+
+
+MON_PARTICLES = 1
+MON_LAST_TURNS = 2
+MON_BEAM_POSITION = 3
+
+
+class XtgElementMonitor(ctypes.Structure):
+    _fields_ = [
+        ("kind", ctypes.c_int32), ("reserved", ctypes.c_int32),
+        ("particle_id_start", ctypes.c_int64), ("num_particles", ctypes.c_int64),
+        ("n_last_turns", ctypes.c_int64), ("every_n_turns", ctypes.c_int64),
+        ("start_at_turn", ctypes.c_int64), ("n_slots", ctypes.c_int64),
+        ("frev", ctypes.c_double), ("sampling_frequency", ctypes.c_double),
+        ("lost_at_offset", ctypes.c_void_p), ("lt_particle_id", ctypes.c_void_p),
+        ("lt_at_turn", ctypes.c_void_p),
+        ("lt_x", ctypes.c_void_p), ("lt_px", ctypes.c_void_p), ("lt_y", ctypes.c_void_p),
+        ("lt_py", ctypes.c_void_p), ("lt_delta", ctypes.c_void_p), ("lt_zeta", ctypes.c_void_p),
+        ("count", ctypes.c_void_p), ("x_sum", ctypes.c_void_p), ("y_sum", ctypes.c_void_p),
+        ("particles", XtgMonitor),
     ]
 
 
@@ -256,7 +279,7 @@ def load_library(path=None):
     lib.xtg_launch_count.restype = c.c_int64
     lib.xtg_measure_fp64_peak.argtypes = [c.POINTER(c.c_double)]
     lib.xtg_measure_fp64_peak.restype = c.c_int32
-    if lib.xtg_abi_version() != 1:
+    if lib.xtg_abi_version() != 2:
         raise RuntimeError("xtrack_gb300: ABI version mismatch")
     if path == LIB_PATH:
         _lib = lib

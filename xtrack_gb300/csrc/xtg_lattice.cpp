@@ -411,6 +411,28 @@ int32_t validate_element(const xtg_element& e, int64_t idx, std::string* why) {
     } else if (e.slice != XTG_SLICE_NONE) {
         return fail("slice kind not valid for this class");
     }
+    if (e.cls == XTG_CLS_MONITOR) {
+        const xtg_element_monitor* m = reinterpret_cast<const xtg_element_monitor*>(e.monitor);
+        if (!m) return fail("monitor element without its descriptor");
+        if (m->kind == XTG_MON_LAST_TURNS) {
+            if (m->n_last_turns < 1 || m->every_n_turns < 1 || m->num_particles < 0)
+                return fail("LastTurnsMonitor needs n_last_turns >= 1, every_n_turns >= 1");
+            if (m->num_particles > 0 && (!m->lost_at_offset || !m->lt_particle_id || !m->lt_at_turn ||
+                                         !m->lt_x || !m->lt_px || !m->lt_y || !m->lt_py ||
+                                         !m->lt_delta || !m->lt_zeta))
+                return fail("LastTurnsMonitor with a NULL buffer");
+        } else if (m->kind == XTG_MON_BEAM_POSITION) {
+            if (m->n_slots < 0) return fail("BeamPositionMonitor with a negative size");
+            if (m->n_slots > 0 && (!m->count || !m->x_sum || !m->y_sum))
+                return fail("BeamPositionMonitor with a NULL buffer");
+        } else if (m->kind == XTG_MON_PARTICLES) {
+            if (m->particles.n_records < 0) return fail("ParticlesMonitor with a negative size");
+            if (m->particles.n_repetitions > 1 && m->particles.repetition_period <= 0)
+                return fail("ParticlesMonitor repetition_period must be > 0");
+        } else {
+            return fail("unknown monitor kind");
+        }
+    }
     return XTG_OK;
 }
 
@@ -825,6 +847,51 @@ int32_t pack_lattice(const xtg_element* els, int64_t n, const xtg_config& cfg,
             r->a_squ = e.a_squ;
             r->b_squ = e.b_squ;
             r->a_b_squ = e.a_b_squ;
+            break;
+        }
+        case XTG_CLS_MONITOR: {
+            // monitors are replaced by markers in backtracking tables
+            // (get_backtrack_element of monitors/*.py)
+            const xtg_element_monitor* m = reinterpret_cast<const xtg_element_monitor*>(e.monitor);
+            if (backtrack) {
+                rb.init(sizeof(RecHeader));
+                rb.head<RecHeader>()->op = OP_NOP;
+            } else if (m->kind == XTG_MON_PARTICLES) {
+                rb.init(sizeof(MonParticlesRec));
+                MonParticlesRec* r = rb.head<MonParticlesRec>();
+                r->h.op = OP_MON_PARTICLES;
+                r->m = m->particles;
+            } else if (m->kind == XTG_MON_LAST_TURNS) {
+                rb.init(sizeof(MonLastTurnsRec));
+                MonLastTurnsRec* r = rb.head<MonLastTurnsRec>();
+                r->h.op = OP_MON_LAST_TURNS;
+                r->particle_id_start = m->particle_id_start;
+                r->particle_id_stop = m->particle_id_start + m->num_particles;
+                r->n_last_turns = m->n_last_turns;
+                r->every_n_turns = m->every_n_turns;
+                r->lost_at_offset = m->lost_at_offset;
+                r->particle_id = m->lt_particle_id;
+                r->at_turn = m->lt_at_turn;
+                r->x = m->lt_x;
+                r->px = m->lt_px;
+                r->y = m->lt_y;
+                r->py = m->lt_py;
+                r->delta = m->lt_delta;
+                r->zeta = m->lt_zeta;
+            } else {
+                rb.init(sizeof(MonBpmRec));
+                MonBpmRec* r = rb.head<MonBpmRec>();
+                r->h.op = OP_MON_BPM;
+                r->particle_id_start = m->particle_id_start;
+                r->particle_id_stop = m->particle_id_start + m->num_particles;
+                r->start_at_turn = m->start_at_turn;
+                r->n_slots = m->n_slots;
+                r->frev = m->frev;
+                r->sampling_frequency = m->sampling_frequency;
+                r->count = m->count;
+                r->x_sum = m->x_sum;
+                r->y_sum = m->y_sum;
+            }
             break;
         }
         case XTG_CLS_LIMIT_RECT: {

@@ -13,6 +13,8 @@
 #pragma once
 #include <stdint.h>
 
+#include "../../include/xtrack_gb300.h"
+
 namespace xtg {
 
 enum Op : int32_t {
@@ -25,6 +27,9 @@ enum Op : int32_t {
     OP_LIMIT_RECT = 5,
     OP_KICK = 6,          // a magnet that is a single kick with no edges (thin
                           // multipoles, thin slices): compact form of OP_MAGNET
+    OP_MON_PARTICLES = 7, // monitors placed in the line (monitors/*.h)
+    OP_MON_LAST_TURNS = 8,
+    OP_MON_BPM = 9,
 };
 
 // RecHeader.flags
@@ -166,6 +171,28 @@ struct alignas(16) CavityRec {
     double phase;
     double phi_const;         // DEG2RAD*lag + phase (valid when phase0 == 0)
     double w_freq;            // (2*pi/c)*frequency (valid when harmonic == 0)
+};
+
+// ParticlesMonitor as a line element (particles_monitor.h:12-77).
+struct alignas(16) MonParticlesRec {
+    RecHeader h;
+    xtg_monitor m;
+};
+
+// LastTurnsMonitor (last_turns_monitor.h:17-55).
+struct alignas(16) MonLastTurnsRec {
+    RecHeader h;
+    int64_t particle_id_start, particle_id_stop, n_last_turns, every_n_turns;
+    uint32_t *lost_at_offset, *particle_id, *at_turn;
+    float *x, *px, *y, *py, *delta, *zeta;
+};
+
+// BeamPositionMonitor (beam_position_monitor.h:16-58).
+struct alignas(16) MonBpmRec {
+    RecHeader h;
+    int64_t particle_id_start, particle_id_stop, start_at_turn, n_slots;
+    double frev, sampling_frequency;
+    double *count, *x_sum, *y_sum;
 };
 
 // Header of an uploaded table.

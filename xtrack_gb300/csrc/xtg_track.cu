@@ -31,6 +31,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <deque>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -94,6 +95,7 @@ struct TrackArgs {
     int32_t chunk_bytes;                       // 0: read records from global memory
     int32_t smem_bytes;                        // dynamic shared memory of the block
     int32_t flag_monitor;
+    int32_t load_pid;                          // a monitor needs particle_id
     int32_t flag_end_turn_actions;
     int32_t flag_reset_s;
     int32_t backtrack;
@@ -189,9 +191,9 @@ __device__ __forceinline__ void issue_copy(void* dst, const void* src, uint32_t 
 // ---------------------------------------------------------------------------
 // monitor (particles_monitor.h:12-77)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void monitor_store(const TrackArgs& a, const PState& p, int64_t i, int64_t k) {
-    const xtg_particles& D = a.M.data;
-    const xtg_particles& S = a.P;
+__device__ __forceinline__ void monitor_store(const xtg_monitor& M, const xtg_particles& S, const PState& p,
+                                              int64_t i, int64_t k) {
+    const xtg_particles& D = M.data;
     if (D.x) D.x[k] = p.x;
     if (D.px) D.px[k] = p.px;
     if (D.y) D.y[k] = p.y;
@@ -218,13 +220,13 @@ __device__ __forceinline__ void monitor_store(const TrackArgs& a, const PState& 
     if (D.parent_particle_id) D.parent_particle_id[k] = S.parent_particle_id ? S.parent_particle_id[i] : 0;
 }
 
-__device__ __forceinline__ void monitor(const TrackArgs& a, const PState& p, int64_t i, int64_t pid) {
-    const xtg_monitor& m = a.M;
+__device__ __forceinline__ void monitor_into(const xtg_monitor& m, const xtg_particles& S, const PState& p,
+                                             int64_t i, int64_t pid, bool backtrack) {
     int64_t at_turn;
     if (m.ebe_mode) {
         at_turn = p.at_element;
     } else {
-        if (a.backtrack) return;
+        if (backtrack) return;
         at_turn = p.at_turn;
     }
     int64_t const n_turns_record = m.stop_at_turn - m.start_at_turn;
@@ -232,7 +234,7 @@ __device__ __forceinline__ void monitor(const TrackArgs& a, const PState& p, int
         if (at_turn >= m.start_at_turn && at_turn < m.stop_at_turn && pid < m.part_id_end &&
             pid >= m.part_id_start) {
             int64_t const store_at = n_turns_record * (pid - m.part_id_start) + at_turn - m.start_at_turn;
-            if (store_at >= 0 && store_at < m.n_records) monitor_store(a, p, i, store_at);
+            if (store_at >= 0 && store_at < m.n_records) monitor_store(m, S, p, i, store_at);
         }
     } else if (m.n_repetitions > 1) {
         if (at_turn < m.start_at_turn) return;
@@ -243,7 +245,47 @@ __device__ __forceinline__ void monitor(const TrackArgs& a, const PState& p, int
             int64_t const store_at = n_turns_record * (m.part_id_end - m.part_id_start) * i_frame +
                                      n_turns_record * (pid - m.part_id_start) +
                                      (at_turn - i_frame * m.repetition_period) - m.start_at_turn;
-            if (store_at >= 0 && store_at < m.n_records) monitor_store(a, p, i, store_at);
+            if (store_at >= 0 && store_at < m.n_records) monitor_store(m, S, p, i, store_at);
+        }
+    }
+}
+
+__device__ __forceinline__ void monitor(const TrackArgs& a, const PState& p, int64_t i, int64_t pid) {
+    monitor_into(a.M, a.P, p, i, pid, a.backtrack != 0);
+}
+
+// LastTurnsMonitor in the line (last_turns_monitor.h:17-55): tracking of a
+// particle stops at its loss, so every pass stores the slot offset and the
+// last one stored is that of the last pass before the loss
+__device__ __noinline__ void monitor_last_turns(const MonLastTurnsRec& r, const PState& p, int64_t pid) {
+    int64_t const at_turn = p.at_turn;
+    if (at_turn >= 0 && at_turn % r.every_n_turns == 0 && r.particle_id_start <= pid &&
+        pid < r.particle_id_stop) {
+        int64_t const offset = (at_turn / r.every_n_turns) % r.n_last_turns;
+        int64_t const ip = pid - r.particle_id_start;
+        int64_t const slot = r.n_last_turns * ip + offset;
+        r.lost_at_offset[ip] = (uint32_t)offset;
+        r.particle_id[slot] = (uint32_t)pid;
+        r.at_turn[slot] = (uint32_t)at_turn;
+        r.x[slot] = (float)p.x;
+        r.px[slot] = (float)p.px;
+        r.y[slot] = (float)p.y;
+        r.py[slot] = (float)p.py;
+        r.delta[slot] = (float)p.delta;
+        r.zeta[slot] = (float)p.zeta;
+    }
+}
+
+// BeamPositionMonitor in the line (beam_position_monitor.h:16-58)
+__device__ __noinline__ void monitor_bpm(const MonBpmRec& r, const PState& p, int64_t pid) {
+    if (r.particle_id_stop < 0 || (r.particle_id_start <= pid && pid < r.particle_id_stop)) {
+        double const at_turn = (double)p.at_turn;
+        int64_t const slot = (int64_t)round(
+            r.sampling_frequency * ((at_turn - r.start_at_turn) / r.frev - p.zeta / p.beta0 / kCLightD));
+        if (slot >= 0 && slot < r.n_slots) {
+            atomicAdd(r.count + slot, 1.0);
+            atomicAdd(r.x_sum + slot, p.x);
+            atomicAdd(r.y_sum + slot, p.y);
         }
     }
 }
@@ -253,7 +295,7 @@ __device__ __forceinline__ void monitor(const TrackArgs& a, const PState& p, int
 // ---------------------------------------------------------------------------
 template <bool kExact>
 __device__ __forceinline__ bool apply_record(PState& p, const unsigned char* __restrict__ rec,
-                                             const TrackArgs& a, const RfCtx& rf) {
+                                             const TrackArgs& a, const RfCtx& rf, int64_t i, int64_t pid) {
     const RecHeader& h = *reinterpret_cast<const RecHeader*>(rec);
     switch (h.op) {
     case OP_DRIFT: {
@@ -301,6 +343,17 @@ __device__ __forceinline__ bool apply_record(PState& p, const unsigned char* __r
         }
         break;
     }
+    case OP_MON_PARTICLES: {
+        const MonParticlesRec& r = *reinterpret_cast<const MonParticlesRec*>(rec);
+        monitor_into(r.m, a.P, p, i, pid, a.backtrack != 0);
+        break;
+    }
+    case OP_MON_LAST_TURNS:
+        monitor_last_turns(*reinterpret_cast<const MonLastTurnsRec*>(rec), p, pid);
+        break;
+    case OP_MON_BPM:
+        monitor_bpm(*reinterpret_cast<const MonBpmRec*>(rec), p, pid);
+        break;
     default:
         break;
     }
@@ -315,7 +368,7 @@ __device__ __forceinline__ void walk(PState& p, bool& active, const unsigned cha
     int64_t const incr = a.backtrack ? -1 : 1;
     while (active && rec < rec_end) {
         if (a.flag_monitor == 2) monitor(a, p, i, pid);
-        bool const thick = apply_record<kExact>(p, rec, a, rf);
+        bool const thick = apply_record<kExact>(p, rec, a, rf, i, pid);
         if (thick && !ignore_global) {
             // local_particle_custom_api.h:259-287
             double const lim = a.global_lim;
@@ -422,7 +475,7 @@ __global__ void __launch_bounds__(256, kExact ? 1 : XTG_FAST_MIN_BLOCKS) track_k
             p.at_turn = P.at_turn[i];
             p.chi_one = (p.chi == 1.0);
             refresh_energy_cache(p);
-            if (a.flag_monitor != 0) pid = P.particle_id[i];
+            if (a.load_pid) pid = P.particle_id[i];
         }
         bool const touched = active;
 
@@ -694,6 +747,8 @@ static void free_ws(Workspace* w) {
 
 struct ExecCtx {
     std::vector<std::vector<xtg_element>> lattices;
+    std::deque<xtg_element_monitor> monitors;  // owned copies of the monitor descriptors
+    bool has_monitors = false;
     xtg_config config;
     int device = 0;
     DevTables fwd, bwd;
@@ -721,6 +776,19 @@ struct xtg_lattice {
 struct xtg_batch {
     ExecCtx ctx;
 };
+
+// Copies the monitor descriptors the elements point at into the context,
+// so that the tables can be packed again later (backtracking) without the
+// caller's descriptors.
+static void own_monitors(ExecCtx* C) {
+    for (auto& els : C->lattices)
+        for (auto& e : els)
+            if (e.cls == XTG_CLS_MONITOR && e.monitor) {
+                C->monitors.push_back(*reinterpret_cast<const xtg_element_monitor*>(e.monitor));
+                e.monitor = reinterpret_cast<uint64_t>(&C->monitors.back());
+                C->has_monitors = true;
+            }
+}
 
 static int32_t build_tables(ExecCtx* C, bool backtrack, DevTables* T) {
     std::vector<unsigned char> bytes;
@@ -1007,6 +1075,7 @@ static int32_t track_impl(ExecCtx* C, const xtg_particles* particles, const int3
     a.rec_count = num_ele_track;
     a.chunk_bytes = chunk;
     a.flag_monitor = flag_monitor;
+    a.load_pid = (flag_monitor != 0 || C->has_monitors) ? 1 : 0;
     a.flag_end_turn_actions = flag_end_turn_actions;
     a.flag_reset_s = flag_reset_s_at_end_turn;
     a.backtrack = backtrack ? 1 : 0;
@@ -1159,6 +1228,7 @@ int32_t xtg_lattice_create(const xtg_element* elements, int64_t n_elements, cons
     }
     std::unique_ptr<xtg_lattice> L(new xtg_lattice());
     L->ctx.lattices.emplace_back(elements, elements + n_elements);
+    own_monitors(&L->ctx);
     L->ctx.config = *config;
     XTG_CUDA_CHECK(cudaGetDevice(&L->ctx.device));
     int32_t st = build_tables(&L->ctx, false, &L->ctx.fwd);
@@ -1283,6 +1353,7 @@ int32_t xtg_track_noalloc(const xtg_lattice* lattice, const xtg_particles* parti
     a.rec_first = rec_first;
     a.rec_count = num_ele_track;
     a.flag_monitor = flag_monitor;
+    a.load_pid = (flag_monitor != 0 || C->has_monitors) ? 1 : 0;
     a.flag_end_turn_actions = flag_end_turn_actions;
     a.flag_reset_s = flag_reset_s_at_end_turn;
     a.backtrack = backtrack ? 1 : 0;
@@ -1321,6 +1392,7 @@ int32_t xtg_batch_create(const xtg_lattice* const* lattices, int32_t n_lattices,
         }
         B->ctx.lattices.push_back(c.lattices[0]);
     }
+    own_monitors(&B->ctx);
     int32_t st = build_tables(&B->ctx, false, &B->ctx.fwd);
     if (st != XTG_OK) return st;
     *out = B.release();

@@ -1,4 +1,10 @@
-"""Turn-by-turn ParticlesMonitor (xtrack/monitors/particles_monitor.py).
+"""Monitors: the turn-by-turn ParticlesMonitor
+(xtrack/monitors/particles_monitor.py), usable as the tracker's
+``turn_by_turn_monitor`` or placed in the line as an element, and the
+LastTurnsMonitor and BeamPositionMonitor elements
+(xtrack/monitors/last_turns_monitor.py, beam_position_monitor.py).
+
+ParticlesMonitor:
 
 Record layout and reshaping follow the reference: ``n_records =
 (stop_at_turn-start_at_turn) * (part_id_end-part_id_start) * n_repetitions``
@@ -11,6 +17,8 @@ turn is written by the push at the start of that turn
 ``fields`` selects the recorded arrays (default: all of them, as the
 reference does); unrecorded fields read back as zeros.
 """
+import ctypes
+
 import numpy as np
 import torch
 
@@ -20,7 +28,34 @@ from .particles import DOUBLE_FIELDS, INT_FIELDS, default_device
 _RECORDABLE = _abi.PARTICLE_DOUBLE_FIELDS + _abi.PARTICLE_INT_FIELDS
 
 
-class ParticlesMonitor:
+class _MonitorElement:
+    """Line-element side of a monitor: the record carries the address of an
+    xtg_element_monitor descriptor (kept alive by the element) whose buffers
+    live on the monitor's device."""
+    isthick = False
+    _cls = _abi.CLS_MONITOR
+
+    def _descriptor(self):
+        raise NotImplementedError
+
+    def to_record(self):
+        rec = np.zeros(1, dtype=_abi.ELEMENT_DTYPE)[0]
+        rec["weight"] = 1.0
+        rec["order_rel"] = -1
+        rec["cls"] = _abi.CLS_MONITOR
+        desc = self._descriptor()
+        # every descriptor handed out stays alive with the element: records
+        # built earlier keep pointing at valid memory
+        self.__dict__.setdefault("_descs", []).append(desc)
+        rec["monitor"] = ctypes.addressof(desc)
+        return rec
+
+    def copy(self):
+        import copy
+        return copy.deepcopy(self)
+
+
+class ParticlesMonitor(_MonitorElement):
     def __init__(self, start_at_turn=0, stop_at_turn=1, num_particles=None,
                  particle_id_range=None, n_repetitions=None, repetition_period=None,
                  auto_to_numpy=True, fields=None, device=None, ebe_mode=0):
@@ -60,6 +95,12 @@ class ParticlesMonitor:
             dtype = torch.int64 if f in INT_FIELDS else torch.float64
             self.data[f] = torch.zeros(self.n_records, dtype=dtype, device=self.device)
 
+    def _descriptor(self):
+        d = _abi.XtgElementMonitor()
+        d.kind = _abi.MON_PARTICLES
+        d.particles = self._xtg_struct()
+        return d
+
     def _xtg_struct(self):
         m = _abi.XtgMonitor()
         m.start_at_turn = self.start_at_turn
@@ -94,3 +135,120 @@ class ParticlesMonitor:
         if name in DOUBLE_FIELDS or name in INT_FIELDS:
             return self._get(name)
         raise AttributeError(name)
+
+
+class LastTurnsMonitor(_MonitorElement):
+    """Rolling buffer of the last ``n_last_turns`` passes (every
+    ``every_n_turns`` turns) of the particles with ids in
+    ``particle_id_range`` (last_turns_monitor.py:31-111). ``x``, ``px``,
+    ``y``, ``py``, ``delta``, ``zeta`` (float32), ``particle_id`` and
+    ``at_turn`` (uint32 in the buffers) read back as arrays of shape
+    (num_particles, n_last_turns), oldest pass first."""
+    properties = ("particle_id", "at_turn", "x", "px", "y", "py", "delta", "zeta")
+
+    def __init__(self, *, n_last_turns=None, num_particles=None, particle_id_range=None,
+                 every_n_turns=1, device=None):
+        if num_particles is not None and particle_id_range is None:
+            particle_id_start = 0
+        elif particle_id_range is not None and num_particles is None:
+            particle_id_start = particle_id_range[0]
+            num_particles = particle_id_range[1] - particle_id_range[0]
+        else:
+            raise ValueError("Exactly one of `num_particles` or `particle_id_range` parameters "
+                             "must be specified")
+        if n_last_turns is None or n_last_turns < 1:
+            raise ValueError("n_last_turns must be >= 1")
+        self.n_last_turns = int(n_last_turns)
+        self.particle_id_start = int(particle_id_start)
+        self.num_particles = int(num_particles)
+        self.every_n_turns = int(every_n_turns)
+        self.device = torch.device(device) if device is not None else default_device()
+        size = self.num_particles * self.n_last_turns
+        # uint32 in the reference; torch keeps them as int32 bit patterns
+        self._buf = {f: torch.zeros(size, dtype=torch.int32 if f in ("particle_id", "at_turn")
+                                    else torch.float32, device=self.device)
+                     for f in self.properties}
+        self._buf["lost_at_offset"] = torch.zeros(self.num_particles, dtype=torch.int32,
+                                                  device=self.device)
+
+    def _descriptor(self):
+        d = _abi.XtgElementMonitor()
+        d.kind = _abi.MON_LAST_TURNS
+        d.particle_id_start = self.particle_id_start
+        d.num_particles = self.num_particles
+        d.n_last_turns = self.n_last_turns
+        d.every_n_turns = self.every_n_turns
+        b = self._buf
+        d.lost_at_offset = b["lost_at_offset"].data_ptr()
+        d.lt_particle_id = b["particle_id"].data_ptr()
+        d.lt_at_turn = b["at_turn"].data_ptr()
+        for f in ("x", "px", "y", "py", "delta", "zeta"):
+            setattr(d, "lt_" + f, b[f].data_ptr())
+        return d
+
+    def __getattr__(self, attr):
+        if attr in LastTurnsMonitor.properties:
+            val = self._buf[attr].cpu().numpy()
+            if attr in ("particle_id", "at_turn"):
+                val = val.view(np.uint32)
+            val = val.reshape(self.num_particles, self.n_last_turns)
+            off = self._buf["lost_at_offset"].cpu().numpy().view(np.uint32).astype(np.int64) + 1
+            r, c = np.ogrid[:val.shape[0], :val.shape[1]]
+            c = (c + off[:, np.newaxis]) % val.shape[1]
+            return val[r, c]
+        raise AttributeError(attr)
+
+
+class BeamPositionMonitor(_MonitorElement):
+    """Centroid recorder (beam_position_monitor.py:25-137): per sample slot
+    i = round(sampling_frequency * ((at_turn - start_at_turn)/frev -
+    zeta/beta0/c)), the count and the sums of x and y of the particles that
+    pass; ``x_mean`` / ``y_mean`` are sum / count."""
+    properties = ("count", "x_sum", "y_sum")
+
+    def __init__(self, *, particle_id_range=None, particle_id_start=None, num_particles=None,
+                 start_at_turn=None, stop_at_turn=None, frev=None, sampling_frequency=None,
+                 device=None):
+        if particle_id_range is None:
+            particle_id_start = 0 if particle_id_start is None else particle_id_start
+            num_particles = -1 if num_particles is None else num_particles
+        elif particle_id_start is None and num_particles is None:
+            particle_id_start = particle_id_range[0]
+            num_particles = particle_id_range[1] - particle_id_range[0]
+        else:
+            raise ValueError("Parameter `particle_id_range` must not be used together with "
+                             "`num_particles` and/or `particle_id_start`")
+        self.particle_id_start = int(particle_id_start)
+        self.num_particles = int(num_particles)
+        self.start_at_turn = int(start_at_turn or 0)
+        self.stop_at_turn = int(stop_at_turn or 0)
+        self.frev = float(frev or 1)
+        self.sampling_frequency = float(sampling_frequency or 1)
+        self.device = torch.device(device) if device is not None else default_device()
+        size = int(round((self.stop_at_turn - self.start_at_turn) * self.sampling_frequency
+                         / self.frev))
+        self.n_slots = size
+        self._buf = {f: torch.zeros(size, dtype=torch.float64, device=self.device)
+                     for f in self.properties}
+
+    def _descriptor(self):
+        d = _abi.XtgElementMonitor()
+        d.kind = _abi.MON_BEAM_POSITION
+        d.particle_id_start = self.particle_id_start
+        d.num_particles = self.num_particles
+        d.start_at_turn = self.start_at_turn
+        d.n_slots = self.n_slots
+        d.frev = self.frev
+        d.sampling_frequency = self.sampling_frequency
+        d.count = self._buf["count"].data_ptr()
+        d.x_sum = self._buf["x_sum"].data_ptr()
+        d.y_sum = self._buf["y_sum"].data_ptr()
+        return d
+
+    def __getattr__(self, attr):
+        if attr in BeamPositionMonitor.properties:
+            return self._buf[attr].cpu().numpy()
+        if attr in ("x_mean", "y_mean", "x_cen", "y_cen", "x_centroid", "y_centroid"):
+            with np.errstate(invalid="ignore", divide="ignore"):
+                return self._buf[attr[0] + "_sum"].cpu().numpy() / self._buf["count"].cpu().numpy()
+        raise AttributeError(attr)
