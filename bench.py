@@ -339,8 +339,8 @@ def run_da_screen(args):
     turns = args.da_turns
     rng = np.random.default_rng(7)
 
-    def counts(n):
-        return rng.integers(args.da_particles // 2, args.da_particles * 3 // 2 + 1, size=n)
+    def counts(n, mean):
+        return rng.integers(mean // 2, mean * 3 // 2 + 1, size=n)
 
     def features(scan):
         d = scan.deltas[scan.delta_index]
@@ -350,10 +350,10 @@ def run_da_screen(args):
     train_lines = [workloads.thick_ring(seed=100 + s) for s in range(args.da_train_seeds)]
     test_lines = [workloads.thick_ring(seed=200 + s) for s in range(args.da_test_seeds)]
     t0 = time.perf_counter()
-    s_train = sc.build_scan(train_lines, counts(len(train_lines)), r_max=args.da_rmax, device=dev,
-                            features=sg.seed_features)
-    s_test = sc.build_scan(test_lines, counts(len(test_lines)), r_max=args.da_rmax, device=dev,
-                           features=sg.seed_features)
+    s_train = sc.build_scan(train_lines, counts(len(train_lines), args.da_train_particles),
+                            r_max=args.da_rmax, device=dev, features=sg.seed_features)
+    s_test = sc.build_scan(test_lines, counts(len(test_lines), args.da_particles),
+                           r_max=args.da_rmax, device=dev, features=sg.seed_features)
     t_setup = time.perf_counter() - t0
     bt_train = BatchTracker(train_lines, device=dev, arith=args.arith)
     bt_test = BatchTracker(test_lines, device=dev, arith=args.arith)
@@ -368,7 +368,7 @@ def run_da_screen(args):
     surv, lt = sg.targets(st, at, turns)
     net = sg.SurvivalMLP(seed=0, device=dev)
     t0 = time.perf_counter()
-    hist = net.fit(features(s_train), surv, lt, epochs=args.da_epochs, batch=2048, lr=2e-3)
+    hist = net.fit(features(s_train), surv, lt, epochs=args.da_epochs, batch=4096, lr=3e-3)
     torch.cuda.synchronize(dev)
     t_fit = time.perf_counter() - t0
 
@@ -383,12 +383,12 @@ def run_da_screen(args):
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
     p, _ = net.predict(features(s_test))
-    track, audit = sg.screen(p, 0.05, 0.95, 0.02, seed=1)
+    track, audit = sg.screen(p, args.da_lo, args.da_hi, 0.02, seed=1)
     st_s, at_s, _ = sc.run_scan(bt_test, s_test, turns, select=track, device=dev)
     torch.cuda.synchronize(dev)
     t_screen = time.perf_counter() - t0
     surv_tracked = sg.targets(st_s, at_s, turns)[0] > 0
-    surv_screen = sg.screened_outcome(p, track, surv_tracked)
+    surv_screen = sg.screened_outcome(p, track, surv_tracked, hi=args.da_hi)
 
     n_seeds = len(test_lines)
     da_plain = sc.da_table(s_test, surv_plain, n_seeds)
@@ -403,7 +403,8 @@ def run_da_screen(args):
            "dtype": "f64 tracking, bf16/f32 network", "data": "synthetic",
            "config": {"workload": "thick LHC-like ring seeds (6993 elements), polar grid "
                                   f"0-{args.da_rmax:g} sigma x 11 angles x delta in {{0, 2.7e-4}}",
-                      "turns": turns, "train_seeds": len(train_lines),
+                      "turns": turns, "screen_band": [args.da_lo, args.da_hi],
+                      "train_seeds": len(train_lines),
                       "test_seeds": n_seeds, "train_particles": int(s_train.n),
                       "test_particles": int(s_test.n), "radial_step_sigma": grid_step,
                       "arith": args.arith},
@@ -446,15 +447,18 @@ def main():
     ap.add_argument("--monitor-first", dest="monitor_first", type=int, default=0,
                     help="record 6 coordinates per turn of the first N particles")
     ap.add_argument("--workload", default="thick_ring", choices=["thick_ring", "da_screen"])
-    ap.add_argument("--da-turns", dest="da_turns", type=int, default=300)
+    ap.add_argument("--da-turns", dest="da_turns", type=int, default=100)
+    ap.add_argument("--da-train-particles", dest="da_train_particles", type=int, default=50000)
+    ap.add_argument("--da-lo", dest="da_lo", type=float, default=0.02)
+    ap.add_argument("--da-hi", dest="da_hi", type=float, default=0.98)
     ap.add_argument("--da-rmax", dest="da_rmax", type=float, default=80.0,
                     help="largest amplitude of the grid (sigma); the synthetic ring at 7 TeV "
                          "keeps everything within 20 sigma, its DA lies near the aperture")
-    ap.add_argument("--da-particles", dest="da_particles", type=int, default=20000,
+    ap.add_argument("--da-particles", dest="da_particles", type=int, default=100000,
                     help="mean particles per seed (uniform in [n/2, 3n/2])")
     ap.add_argument("--da-train-seeds", dest="da_train_seeds", type=int, default=6)
     ap.add_argument("--da-test-seeds", dest="da_test_seeds", type=int, default=4)
-    ap.add_argument("--da-epochs", dest="da_epochs", type=int, default=6)
+    ap.add_argument("--da-epochs", dest="da_epochs", type=int, default=30)
     args = ap.parse_args()
     if args.workload == "da_screen":
         run_da_screen(args)

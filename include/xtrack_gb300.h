@@ -176,6 +176,10 @@ typedef struct xtg_monitor {
 #define XTG_MON_PARTICLES     1
 #define XTG_MON_LAST_TURNS    2
 #define XTG_MON_BEAM_POSITION 3
+#define XTG_MON_BEAM_SIZE     4   /* beam_size_monitor.h: BEAM_POSITION plus
+                                     the sums of x^2 and y^2 per slot     */
+#define XTG_MON_BEAM_PROFILE  5   /* beam_profile_monitor.h: per sample, the
+                                     counts of x and y in nx / ny bins    */
 
 typedef struct xtg_element_monitor {
     int32_t kind;
@@ -187,7 +191,11 @@ typedef struct xtg_element_monitor {
     double frev, sampling_frequency;              /* BEAM_POSITION           */
     uint32_t *lost_at_offset, *lt_particle_id, *lt_at_turn;   /* LAST_TURNS */
     float *lt_x, *lt_px, *lt_y, *lt_py, *lt_delta, *lt_zeta;
-    double *count, *x_sum, *y_sum;                /* BEAM_POSITION           */
+    double *count, *x_sum, *y_sum;                /* BEAM_POSITION, BEAM_SIZE */
+    double *x2_sum, *y2_sum;                      /* BEAM_SIZE               */
+    int64_t nx, ny;                               /* BEAM_PROFILE: bins;     */
+    double x_min, dx, y_min, dy;                  /*   n_slots = sample_size */
+    double *counts_x, *counts_y;                  /*   n_slots*nx, *ny       */
     xtg_monitor particles;                        /* PARTICLES               */
 } xtg_element_monitor;
 

@@ -1307,6 +1307,46 @@ static void xto_bpm(const xtg_element_monitor* m, const xto_part* p) {
 #pragma omp atomic
 #endif
             m->y_sum[slot] += y;
+            if (m->kind == XTG_MON_BEAM_SIZE) {
+                /* beam_size_monitor.h:16-64 */
+#ifdef _OPENMP
+#pragma omp atomic
+#endif
+                m->x2_sum[slot] += x * x;
+#ifdef _OPENMP
+#pragma omp atomic
+#endif
+                m->y2_sum[slot] += y * y;
+            }
+        }
+    }
+}
+
+/* beam_profile_monitor.h:16-80 */
+static void xto_profile(const xtg_element_monitor* m, const xto_part* p) {
+    int64_t const particle_id_stop = m->particle_id_start + m->num_particles;
+    int64_t const particle_id = p->particle_id;
+    if (particle_id_stop < 0 || (m->particle_id_start <= particle_id && particle_id < particle_id_stop)) {
+        double const zeta = p->zeta;
+        double const at_turn = (double)p->at_turn;
+        double const beta0 = p->beta0;
+        int64_t const sample = (int64_t)round(m->sampling_frequency *
+                                              ((at_turn - m->start_at_turn) / m->frev - zeta / beta0 / XTO_C_LIGHT));
+        if (sample >= 0 && sample < m->n_slots) {
+            int64_t const bin_x = (int64_t)floor((p->x - m->x_min) / m->dx);
+            int64_t const bin_y = (int64_t)floor((p->y - m->y_min) / m->dy);
+            if (bin_x >= 0 && bin_x < m->nx) {
+#ifdef _OPENMP
+#pragma omp atomic
+#endif
+                m->counts_x[sample * m->nx + bin_x] += 1.;
+            }
+            if (bin_y >= 0 && bin_y < m->ny) {
+#ifdef _OPENMP
+#pragma omp atomic
+#endif
+                m->counts_y[sample * m->ny + bin_y] += 1.;
+            }
         }
     }
 }
@@ -1327,7 +1367,8 @@ static int xto_apply(const xtg_element* e, const xtg_config* cfg, xto_part* p,
         if (backtrack) return 0;
         if (m->kind == XTG_MON_PARTICLES) xto_monitor(&m->particles, p, src, isrc);
         else if (m->kind == XTG_MON_LAST_TURNS) xto_last_turns(m, p);
-        else if (m->kind == XTG_MON_BEAM_POSITION) xto_bpm(m, p);
+        else if (m->kind == XTG_MON_BEAM_POSITION || m->kind == XTG_MON_BEAM_SIZE) xto_bpm(m, p);
+        else if (m->kind == XTG_MON_BEAM_PROFILE) xto_profile(m, p);
         return 0;
     }
     case XTG_CLS_DRIFT: {

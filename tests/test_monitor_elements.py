@@ -147,3 +147,112 @@ def test_particles_monitor_element_equals_turn_by_turn_monitor():
     # the BPM saw every pass of every alive particle
     alive_per_turn = (tbt.state > 0).sum(axis=0)
     assert np.array_equal(bpm.count, alive_per_turn.astype(float))
+
+
+def _size_scenario(device, turn_fn):
+    npart = 512
+    x = np.linspace(-0.1, 0.1, npart + 4) ** 2
+    p = xt.Particles(p0c=6.5e12, x=x, y=10 * x,
+                     zeta=-2.99792458e8 * np.tile([0.0, 0.5], (npart + 4) // 2), device=device)
+    mon = xt.BeamSizeMonitor(num_particles=npart, start_at_turn=0, stop_at_turn=10, frev=1,
+                             sampling_frequency=2, device=device)
+    line = xt.Line(elements=[mon], element_names=["bsm"])
+    if device != "cpu":
+        line.build_tracker(device=device)
+    for turn in range(11):
+        p.x[0] += 0.005
+        p.y[0] += 0.05
+        if turn == 8:
+            p.state[256:] = 0
+        if turn == 9:
+            p.state[:] = 0
+        turn_fn(line, p)
+    return mon, x, npart
+
+
+def _check_size(mon, x, npart):
+    expected_count = np.tile([npart // 2, npart // 2], 10).astype(float)
+    expected_count[16:18] = 128
+    expected_count[18:20] = 0
+    assert np.array_equal(mon.count, expected_count)
+    xr = x[:npart].reshape((-1, 2))
+    ex = np.tile(np.sum(xr, axis=0), 10)
+    ex[0::2] += 0.005 * np.arange(1, 11)
+    ex[16:18] -= np.sum(xr[128:, :], axis=0)
+    ex[18:20] = 0
+    assert np.allclose(mon.x_sum, ex, rtol=1e-10, atol=1e-15)
+    assert np.allclose(mon.y_sum, 10 * ex, rtol=1e-10, atol=1e-14)
+    ex2 = np.tile(np.sum(xr ** 2, axis=0), 10)
+    ex2[0::2] += 2 * xr[0, 0] * 0.005 * np.arange(1, 11) + (0.005 * np.arange(1, 11)) ** 2
+    ex2[16:18] -= np.sum(xr[128:, :] ** 2, axis=0)
+    ex2[18:20] = 0
+    assert np.allclose(mon.x2_sum, ex2, rtol=1e-10, atol=1e-16)
+    assert np.allclose(mon.y2_sum, 100 * ex2, rtol=1e-10, atol=1e-14)
+    mean = ex[:18] / expected_count[:18]
+    var = ex2[:18] / expected_count[:18] - mean ** 2
+    assert np.allclose(mon.x_var[:18], var, rtol=1e-6, atol=1e-15)
+    assert np.all(np.isnan(mon.x_std[18:]))
+
+
+def _profile_scenario(device, turn_fn):
+    gen = np.random.default_rng(seed=38715345)
+    npart = 512
+    x = gen.normal(size=npart + 4)
+    y = gen.normal(size=npart + 4)
+    p = xt.Particles(p0c=6.5e12, x=x, y=y, zeta=-2.99792458e8 * np.tile([0.0, 0.5], x.size // 2),
+                     device=device)
+    mon = xt.BeamProfileMonitor(num_particles=npart, start_at_turn=0, stop_at_turn=10, frev=1,
+                                sampling_frequency=2, n=100, x_range=5, y_range=(-4, 2),
+                                device=device)
+    line = xt.Line(elements=[mon], element_names=["bpf"])
+    if device != "cpu":
+        line.build_tracker(device=device)
+    for turn in range(11):
+        p.x[0] += 0.1
+        p.y[0] -= 0.1
+        if turn == 8:
+            p.state[256:] = 0
+        if turn == 9:
+            p.state[:] = 0
+        turn_fn(line, p)
+    return mon, x, y, npart
+
+
+def _check_profile(mon, x, y, npart):
+    nb = 100
+    ex_x = np.zeros((20, nb))
+    ex_y = np.zeros((20, nb))
+    for turn in range(10):
+        for sub in range(2):
+            lim = {8: 256, 9: 0}.get(turn, npart)
+            xs = np.copy(x[:lim][sub::2])
+            ys = np.copy(y[:lim][sub::2])
+            if sub == 0 and lim > 0:
+                xs[0] += 0.1 * (turn + 1)
+                ys[0] -= 0.1 * (turn + 1)
+            hx, edges_x = np.histogram(xs, bins=nb, range=(-2.5, 2.5))
+            hy, edges_y = np.histogram(ys, bins=nb, range=(-4, 2))
+            ex_x[2 * turn + sub] = hx
+            ex_y[2 * turn + sub] = hy
+    assert np.allclose(mon.x_edges, edges_x)
+    assert np.allclose(mon.y_grid, 0.5 * (edges_y[1:] + edges_y[:-1]))
+    assert np.array_equal(mon.x_intensity, ex_x)
+    assert np.array_equal(mon.y_intensity, ex_y)
+
+
+def test_beam_size_monitor_oracle():
+    _check_size(*_size_scenario("cpu", _oracle_turn))
+
+
+def test_beam_profile_monitor_oracle():
+    _check_profile(*_profile_scenario("cpu", _oracle_turn))
+
+
+@pytest.mark.gpu
+def test_beam_size_monitor_gpu():
+    _check_size(*_size_scenario("cuda", _gpu_turn))
+
+
+@pytest.mark.gpu
+def test_beam_profile_monitor_gpu():
+    _check_profile(*_profile_scenario("cuda", _gpu_turn))

@@ -9,7 +9,8 @@ from .particles import Particles, PROTON_MASS_EV, ELECTRON_MASS_EV, LAST_INVALID
 from .elements import (Marker, Drift, Multipole, Bend, Quadrupole, Sextupole, Octupole,
                        Cavity, LimitEllipse, LimitRect, BeamElement)
 from .elements import *  # noqa: F401,F403  (slice classes)
-from .monitors import ParticlesMonitor, LastTurnsMonitor, BeamPositionMonitor
+from .monitors import (ParticlesMonitor, LastTurnsMonitor, BeamPositionMonitor, BeamSizeMonitor,
+                       BeamProfileMonitor)
 from .slicing import Strategy, Teapot, Uniform
 from .line import Line, TrackerConfig
 from .tracker import Tracker, TrackFlags

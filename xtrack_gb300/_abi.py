@@ -140,6 +140,8 @@ class XtgMonitor(ctypes.Structure):
 MON_PARTICLES = 1
 MON_LAST_TURNS = 2
 MON_BEAM_POSITION = 3
+MON_BEAM_SIZE = 4
+MON_BEAM_PROFILE = 5
 
 
 class XtgElementMonitor(ctypes.Structure):
@@ -154,6 +156,11 @@ class XtgElementMonitor(ctypes.Structure):
         ("lt_x", ctypes.c_void_p), ("lt_px", ctypes.c_void_p), ("lt_y", ctypes.c_void_p),
         ("lt_py", ctypes.c_void_p), ("lt_delta", ctypes.c_void_p), ("lt_zeta", ctypes.c_void_p),
         ("count", ctypes.c_void_p), ("x_sum", ctypes.c_void_p), ("y_sum", ctypes.c_void_p),
+        ("x2_sum", ctypes.c_void_p), ("y2_sum", ctypes.c_void_p),
+        ("nx", ctypes.c_int64), ("ny", ctypes.c_int64),
+        ("x_min", ctypes.c_double), ("dx", ctypes.c_double),
+        ("y_min", ctypes.c_double), ("dy", ctypes.c_double),
+        ("counts_x", ctypes.c_void_p), ("counts_y", ctypes.c_void_p),
         ("particles", XtgMonitor),
     ]
 

@@ -421,10 +421,17 @@ int32_t validate_element(const xtg_element& e, int64_t idx, std::string* why) {
                                          !m->lt_x || !m->lt_px || !m->lt_y || !m->lt_py ||
                                          !m->lt_delta || !m->lt_zeta))
                 return fail("LastTurnsMonitor with a NULL buffer");
-        } else if (m->kind == XTG_MON_BEAM_POSITION) {
-            if (m->n_slots < 0) return fail("BeamPositionMonitor with a negative size");
+        } else if (m->kind == XTG_MON_BEAM_POSITION || m->kind == XTG_MON_BEAM_SIZE) {
+            if (m->n_slots < 0) return fail("beam position/size monitor with a negative size");
             if (m->n_slots > 0 && (!m->count || !m->x_sum || !m->y_sum))
-                return fail("BeamPositionMonitor with a NULL buffer");
+                return fail("beam position/size monitor with a NULL buffer");
+            if (m->kind == XTG_MON_BEAM_SIZE && m->n_slots > 0 && (!m->x2_sum || !m->y2_sum))
+                return fail("BeamSizeMonitor with a NULL buffer");
+        } else if (m->kind == XTG_MON_BEAM_PROFILE) {
+            if (m->n_slots < 0 || m->nx < 0 || m->ny < 0)
+                return fail("BeamProfileMonitor with a negative size");
+            if (m->n_slots > 0 && ((m->nx > 0 && !m->counts_x) || (m->ny > 0 && !m->counts_y)))
+                return fail("BeamProfileMonitor with a NULL buffer");
         } else if (m->kind == XTG_MON_PARTICLES) {
             if (m->particles.n_records < 0) return fail("ParticlesMonitor with a negative size");
             if (m->particles.n_repetitions > 1 && m->particles.repetition_period <= 0)
@@ -878,10 +885,32 @@ int32_t pack_lattice(const xtg_element* els, int64_t n, const xtg_config& cfg,
                 r->py = m->lt_py;
                 r->delta = m->lt_delta;
                 r->zeta = m->lt_zeta;
+            } else if (m->kind == XTG_MON_BEAM_PROFILE) {
+                rb.init(sizeof(MonProfileRec));
+                MonProfileRec* r = rb.head<MonProfileRec>();
+                r->h.op = OP_MON_PROFILE;
+                r->particle_id_start = m->particle_id_start;
+                r->particle_id_stop = m->particle_id_start + m->num_particles;
+                r->start_at_turn = m->start_at_turn;
+                r->sample_size = m->n_slots;
+                r->frev = m->frev;
+                r->sampling_frequency = m->sampling_frequency;
+                r->nx = m->nx;
+                r->ny = m->ny;
+                r->x_min = m->x_min;
+                r->dx = m->dx;
+                r->y_min = m->y_min;
+                r->dy = m->dy;
+                r->counts_x = m->counts_x;
+                r->counts_y = m->counts_y;
             } else {
                 rb.init(sizeof(MonBpmRec));
                 MonBpmRec* r = rb.head<MonBpmRec>();
                 r->h.op = OP_MON_BPM;
+                if (m->kind == XTG_MON_BEAM_SIZE) {
+                    r->x2_sum = m->x2_sum;
+                    r->y2_sum = m->y2_sum;
+                }
                 r->particle_id_start = m->particle_id_start;
                 r->particle_id_stop = m->particle_id_start + m->num_particles;
                 r->start_at_turn = m->start_at_turn;

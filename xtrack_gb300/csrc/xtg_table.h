@@ -29,7 +29,8 @@ enum Op : int32_t {
                           // multipoles, thin slices): compact form of OP_MAGNET
     OP_MON_PARTICLES = 7, // monitors placed in the line (monitors/*.h)
     OP_MON_LAST_TURNS = 8,
-    OP_MON_BPM = 9,
+    OP_MON_BPM = 9,       // beam position and beam size monitors
+    OP_MON_PROFILE = 10,
 };
 
 // RecHeader.flags
@@ -193,6 +194,17 @@ struct alignas(16) MonBpmRec {
     int64_t particle_id_start, particle_id_stop, start_at_turn, n_slots;
     double frev, sampling_frequency;
     double *count, *x_sum, *y_sum;
+    double *x2_sum, *y2_sum;      // beam size monitor (NULL for beam position)
+};
+
+// BeamProfileMonitor (beam_profile_monitor.h:16-80).
+struct alignas(16) MonProfileRec {
+    RecHeader h;
+    int64_t particle_id_start, particle_id_stop, start_at_turn, sample_size;
+    double frev, sampling_frequency;
+    int64_t nx, ny;
+    double x_min, dx, y_min, dy;
+    double *counts_x, *counts_y;
 };
 
 // Header of an uploaded table.

@@ -286,6 +286,26 @@ __device__ __noinline__ void monitor_bpm(const MonBpmRec& r, const PState& p, in
             atomicAdd(r.count + slot, 1.0);
             atomicAdd(r.x_sum + slot, p.x);
             atomicAdd(r.y_sum + slot, p.y);
+            if (r.x2_sum) {
+                // beam_size_monitor.h:16-64
+                atomicAdd(r.x2_sum + slot, p.x * p.x);
+                atomicAdd(r.y2_sum + slot, p.y * p.y);
+            }
+        }
+    }
+}
+
+// BeamProfileMonitor in the line (beam_profile_monitor.h:16-80)
+__device__ __noinline__ void monitor_profile(const MonProfileRec& r, const PState& p, int64_t pid) {
+    if (r.particle_id_stop < 0 || (r.particle_id_start <= pid && pid < r.particle_id_stop)) {
+        double const at_turn = (double)p.at_turn;
+        int64_t const sample = (int64_t)round(
+            r.sampling_frequency * ((at_turn - r.start_at_turn) / r.frev - p.zeta / p.beta0 / kCLightD));
+        if (sample >= 0 && sample < r.sample_size) {
+            int64_t const bin_x = (int64_t)floor((p.x - r.x_min) / r.dx);
+            int64_t const bin_y = (int64_t)floor((p.y - r.y_min) / r.dy);
+            if (bin_x >= 0 && bin_x < r.nx) atomicAdd(r.counts_x + sample * r.nx + bin_x, 1.);
+            if (bin_y >= 0 && bin_y < r.ny) atomicAdd(r.counts_y + sample * r.ny + bin_y, 1.);
         }
     }
 }
@@ -353,6 +373,9 @@ __device__ __forceinline__ bool apply_record(PState& p, const unsigned char* __r
         break;
     case OP_MON_BPM:
         monitor_bpm(*reinterpret_cast<const MonBpmRec*>(rec), p, pid);
+        break;
+    case OP_MON_PROFILE:
+        monitor_profile(*reinterpret_cast<const MonProfileRec*>(rec), p, pid);
         break;
     default:
         break;

@@ -199,6 +199,16 @@ class LastTurnsMonitor(_MonitorElement):
         raise AttributeError(attr)
 
 
+def _id_range(particle_id_range, particle_id_start, num_particles):
+    if particle_id_range is None:
+        return (0 if particle_id_start is None else int(particle_id_start),
+                -1 if num_particles is None else int(num_particles))
+    if particle_id_start is None and num_particles is None:
+        return int(particle_id_range[0]), int(particle_id_range[1] - particle_id_range[0])
+    raise ValueError("Parameter `particle_id_range` must not be used together with "
+                     "`num_particles` and/or `particle_id_start`")
+
+
 class BeamPositionMonitor(_MonitorElement):
     """Centroid recorder (beam_position_monitor.py:25-137): per sample slot
     i = round(sampling_frequency * ((at_turn - start_at_turn)/frev -
@@ -251,4 +261,104 @@ class BeamPositionMonitor(_MonitorElement):
         if attr in ("x_mean", "y_mean", "x_cen", "y_cen", "x_centroid", "y_centroid"):
             with np.errstate(invalid="ignore", divide="ignore"):
                 return self._buf[attr[0] + "_sum"].cpu().numpy() / self._buf["count"].cpu().numpy()
+        raise AttributeError(attr)
+
+
+class BeamSizeMonitor(BeamPositionMonitor):
+    """Beam size recorder (beam_size_monitor.py): the beam position
+    monitor's sums plus those of x^2 and y^2 per sample slot; ``x_std`` /
+    ``y_std`` from them."""
+    properties = ("count", "x_sum", "y_sum", "x2_sum", "y2_sum")
+
+    def __init__(self, **kwargs):
+        super().__init__(**kwargs)
+        for f in ("x2_sum", "y2_sum"):
+            self._buf[f] = torch.zeros(self.n_slots, dtype=torch.float64, device=self.device)
+
+    def _descriptor(self):
+        d = super()._descriptor()
+        d.kind = _abi.MON_BEAM_SIZE
+        d.x2_sum = self._buf["x2_sum"].data_ptr()
+        d.y2_sum = self._buf["y2_sum"].data_ptr()
+        return d
+
+    def __getattr__(self, attr):
+        if attr in BeamSizeMonitor.properties:
+            return self._buf[attr].cpu().numpy()
+        if attr in ("x_var", "y_var", "x_std", "y_std"):
+            c = attr[0]
+            with np.errstate(invalid="ignore", divide="ignore"):
+                n = self._buf["count"].cpu().numpy()
+                mean = self._buf[c + "_sum"].cpu().numpy() / n
+                var = self._buf[c + "2_sum"].cpu().numpy() / n - mean ** 2
+            return var if attr.endswith("var") else np.sqrt(var)
+        return super().__getattr__(attr)
+
+
+class BeamProfileMonitor(_MonitorElement):
+    """Transverse profile recorder (beam_profile_monitor.py): per sample,
+    particle counts in ``nx`` bins over ``x_range`` and ``ny`` bins over
+    ``y_range``; ``x_intensity`` / ``y_intensity`` have shape
+    (sample_size, n)."""
+    properties = ("counts_x", "counts_y")
+
+    def __init__(self, *, particle_id_range=None, particle_id_start=None, num_particles=None,
+                 start_at_turn=None, stop_at_turn=None, frev=None, sampling_frequency=None,
+                 nx=None, x_range=None, ny=None, y_range=None, n=None, range=None, device=None):
+        self.particle_id_start, self.num_particles = _id_range(particle_id_range,
+                                                               particle_id_start, num_particles)
+        self.start_at_turn = int(start_at_turn or 0)
+        self.stop_at_turn = int(stop_at_turn or 0)
+        self.frev = float(frev or 1)
+        self.sampling_frequency = float(sampling_frequency or 1)
+
+        def axis(nv, rv):
+            nv = int(nv if nv is not None else (n or 128))
+            if rv is None:
+                if range is None:
+                    raise ValueError("Either `x_range`/`y_range` or `range` must be provided")
+                rv = range
+            if np.isscalar(rv):
+                rv = (-rv / 2, rv / 2)
+            return nv, float(rv[0]), (rv[1] - rv[0]) / nv
+
+        self.nx, self.x_min, self.dx = axis(nx, x_range)
+        self.ny, self.y_min, self.dy = axis(ny, y_range)
+        self.sample_size = int(round((self.stop_at_turn - self.start_at_turn)
+                                     * self.sampling_frequency / self.frev))
+        self.device = torch.device(device) if device is not None else default_device()
+        self._buf = {"counts_x": torch.zeros(self.sample_size * self.nx, dtype=torch.float64,
+                                             device=self.device),
+                     "counts_y": torch.zeros(self.sample_size * self.ny, dtype=torch.float64,
+                                             device=self.device)}
+
+    def _descriptor(self):
+        d = _abi.XtgElementMonitor()
+        d.kind = _abi.MON_BEAM_PROFILE
+        d.particle_id_start = self.particle_id_start
+        d.num_particles = self.num_particles
+        d.start_at_turn = self.start_at_turn
+        d.n_slots = self.sample_size
+        d.frev = self.frev
+        d.sampling_frequency = self.sampling_frequency
+        d.nx, d.ny = self.nx, self.ny
+        d.x_min, d.dx, d.y_min, d.dy = self.x_min, self.dx, self.y_min, self.dy
+        d.counts_x = self._buf["counts_x"].data_ptr()
+        d.counts_y = self._buf["counts_y"].data_ptr()
+        return d
+
+    def __getattr__(self, attr):
+        if attr in BeamProfileMonitor.properties:
+            return self._buf[attr].cpu().numpy()
+        if attr in ("x_intensity", "y_intensity"):
+            c = attr[0]
+            nb = self.nx if c == "x" else self.ny
+            return self._buf["counts_" + c].cpu().numpy().reshape(self.sample_size, nb)
+        if attr in ("x_edges", "y_edges"):
+            c = attr[0]
+            nb, lo, d = (self.nx, self.x_min, self.dx) if c == "x" else (self.ny, self.y_min, self.dy)
+            return lo + d * np.arange(nb + 1)
+        if attr in ("x_grid", "y_grid"):
+            e = self.__getattr__(attr[0] + "_edges")
+            return 0.5 * (e[1:] + e[:-1])
         raise AttributeError(attr)
