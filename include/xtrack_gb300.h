@@ -285,6 +285,30 @@ int32_t xtg_track_noalloc(const xtg_lattice* lattice, const xtg_particles* parti
                           int32_t flag_monitor, int32_t num_ele_line, double line_length,
                           const xtg_monitor* monitor, uint64_t track_flags, void* stream);
 
+/*
+ * Multi-element monitor (monitors/multi_element_monitor.h:10-65; the
+ * tracker's `multi_element_monitor_at`, tracker.py:1482-1525): before each
+ * element whose index maps to an observation point, the 7 coordinates
+ * x, px, y, py, zeta, delta, s of particles [part_id_start, part_id_end)
+ * in turns [start_at_turn, stop_at_turn) are stored at
+ * data[((turn - start) * n_particles + (id - part_id_start)) * 7 + coord)
+ *      * n_obs + obs].
+ * `at_element_mapping` (device, mapping_len entries) gives the observation
+ * index of each element or -1. Set on a lattice it applies to every later
+ * xtg_track / xtg_track_noalloc call on it until cleared with NULL; the
+ * struct is copied, its device buffers are the caller's.
+ */
+typedef struct xtg_multi_element_monitor {
+    int64_t start_at_turn, stop_at_turn;
+    int64_t part_id_start, part_id_end;
+    int64_t mapping_len, n_obs;
+    const int64_t* at_element_mapping;
+    double* data;
+} xtg_multi_element_monitor;
+
+int32_t xtg_set_multi_element_monitor(xtg_lattice* lattice,
+                                      const xtg_multi_element_monitor* monitor);
+
 /* Launch tuning of the push. Results do not depend on it. */
 typedef struct xtg_tuning {
     int32_t block_size;      /* threads per block: 64, 128 or 256            */

@@ -189,6 +189,28 @@ def track(records, arrs, q0=1.0, mass0=938272088.16, t_sim=0.0, num_turns=1, ele
     return arrs
 
 
+class _MultiMon(ctypes.Structure):
+    _fields_ = [("start_at_turn", ctypes.c_int64), ("stop_at_turn", ctypes.c_int64),
+                ("part_id_start", ctypes.c_int64), ("part_id_end", ctypes.c_int64),
+                ("mapping_len", ctypes.c_int64), ("n_obs", ctypes.c_int64),
+                ("at_element_mapping", ctypes.c_void_p), ("data", ctypes.c_void_p)]
+
+
+def set_multi_element_monitor(mapping, data, start_at_turn, stop_at_turn, part_id_start,
+                              part_id_end, which="oracle"):
+    """Multi-element monitor for the following track() calls of the oracle
+    (host numpy buffers: int64 mapping, float64 data of shape
+    (turns, particles, 7, n_obs)); mapping=None clears it."""
+    lib = _load(ORACLE_LIB if which == "oracle" else ORACLE_FMA_LIB, "oracle")
+    lib.xto_set_multi_element_monitor.argtypes = [ctypes.POINTER(_MultiMon)]
+    if mapping is None:
+        lib.xto_set_multi_element_monitor(None)
+        return
+    m = _MultiMon(start_at_turn, stop_at_turn, part_id_start, part_id_end, len(mapping),
+                  data.shape[-1], mapping.ctypes.data, data.ctypes.data)
+    lib.xto_set_multi_element_monitor(ctypes.byref(m))
+
+
 def validate(records):
     ensure_built(with_ref=False)
     lib = _load(ORACLE_LIB, "oracle")

@@ -1651,6 +1651,41 @@ static void xto_monitor(const xtg_monitor* m, const xto_part* p,
     }
 }
 
+/* multi_element_monitor.h:10-65 (set for the next calls by
+ * xto_set_multi_element_monitor) */
+static xtg_multi_element_monitor xto_mem;
+static int xto_mem_on = 0;
+
+static void xto_multi_element_monitor(const xto_part* p) {
+    const xtg_multi_element_monitor* E = &xto_mem;
+    int64_t const at_turn = p->at_turn;
+    int64_t const particle_id = p->particle_id;
+    if ((at_turn >= E->start_at_turn && at_turn < E->stop_at_turn) &&
+        (particle_id >= E->part_id_start && particle_id < E->part_id_end)) {
+        int64_t const at_element = p->at_element;
+        int64_t store_at = -1;
+        if (at_element < E->mapping_len) store_at = E->at_element_mapping[at_element];
+        if (store_at >= 0) {
+            int64_t const turn_index = at_turn - E->start_at_turn;
+            int64_t const particle_index = particle_id - E->part_id_start;
+            int64_t const n_part = E->part_id_end - E->part_id_start;
+            double const v[7] = {p->x, p->px, p->y, p->py, p->zeta, p->delta, p->s};
+            for (int c = 0; c < 7; c++)
+                E->data[((turn_index * n_part + particle_index) * 7 + c) * E->n_obs + store_at] = v[c];
+        }
+    }
+}
+
+int32_t xto_set_multi_element_monitor(const xtg_multi_element_monitor* m) {
+    if (m) {
+        xto_mem = *m;
+        xto_mem_on = 1;
+    } else {
+        xto_mem_on = 0;
+    }
+    return XTG_OK;
+}
+
 /* ---------------------------------------------------------------------- */
 /* track_line, per-particle semantics: tracker.py:594-736                  */
 /* ---------------------------------------------------------------------- */
@@ -1690,6 +1725,7 @@ static void xto_track_one(const xto_args* a, int64_t i) {
         }
         for (; (elem_idx >= a->ele_start) && (elem_idx < ele_stop); elem_idx += increm) {
             if (a->flag_monitor == 2) xto_monitor(a->mon, &p, a->P, i);
+            if (xto_mem_on) xto_multi_element_monitor(&p);
             if (xto_apply(&a->els[elem_idx], a->cfg, &p, a->P, i)) xto_global_aperture(a->cfg, &p);
             isactive = p.state > 0;
             if (!isactive) break;
@@ -1800,6 +1836,7 @@ static void xto_track_chunk_openmp(const xto_args* a, int64_t ipart, int64_t end
                 if (P->state[i] <= 0) continue;
                 xto_load(P, i, a->flags, a->line_length, &p);
                 if (a->flag_monitor == 2) xto_monitor(a->mon, &p, P, i);
+                if (xto_mem_on) xto_multi_element_monitor(&p);
                 if (xto_apply(e, a->cfg, &p, P, i)) xto_global_aperture(a->cfg, &p);
                 xto_store(&p, P, i);
             }

@@ -48,6 +48,10 @@ int32_t xto_track(const xtg_element* elements, int64_t n_elements,
  * offset of particles, element.monitor offset. */
 int32_t xto_abi_sizes(int64_t* out);
 
+/* Multi-element monitor applied by the following xto_track calls (NULL
+ * clears it); host buffers. */
+int32_t xto_set_multi_element_monitor(const xtg_multi_element_monitor* m);
+
 /* Threads the OpenMP runtime would use (1 when built without OpenMP). */
 int32_t xto_max_threads(void);
 

@@ -256,3 +256,58 @@ def test_beam_size_monitor_gpu():
 @pytest.mark.gpu
 def test_beam_profile_monitor_gpu():
     _check_profile(*_profile_scenario("cuda", _gpu_turn))
+
+
+def _multi_element_oracle(line, kw, names, turns):
+    """The oracle's multi-element monitor over the same observation points."""
+    import pyoracle as po
+    recs = line._element_records()
+    p = xt.Particles(device="cpu", **kw)
+    arrs = po.host_arrays(p.to_numpy())
+    elnames = list(line.element_names)
+    obs = [elnames.index(n) for n in names]
+    mapping = np.full(len(elnames) + 1, -1, dtype=np.int64)
+    mapping[obs] = np.arange(len(obs))
+    data = np.zeros((turns, len(arrs["x"]), 7, len(obs)))
+    po.set_multi_element_monitor(mapping, data, 0, turns, 0, len(arrs["x"]))
+    try:
+        po.track(recs, arrs, num_turns=turns, line_length=line.get_length())
+    finally:
+        po.set_multi_element_monitor(None, None, 0, 0, 0, 0)
+    return data
+
+
+def test_multi_element_monitor_oracle_records_before_elements():
+    from xtrack_gb300 import workloads
+    line = workloads.toy_ring()
+    n = 16
+    rng = np.random.default_rng(4)
+    kw = dict(p0c=450e9, x=rng.normal(0, 1e-3, n), px=rng.normal(0, 1e-5, n))
+    names = [line.element_names[k] for k in (0, 3, 250, 500)]
+    data = _multi_element_oracle(line, kw, names, 3)
+    # before the first element of turn 0: the initial coordinates
+    assert np.array_equal(data[0, :, 0, 0], kw["x"])
+    assert np.all(data[:, :, 6, 0] == 0.0)       # s at the start of each turn
+    assert np.all(np.diff(data[0, :, 6, :], axis=1) > 0)
+
+
+@pytest.mark.gpu
+def test_multi_element_monitor_gpu_matches_oracle():
+    from xtrack_gb300 import workloads
+    line = workloads.toy_ring()
+    n = 300
+    rng = np.random.default_rng(5)
+    kw = dict(p0c=450e9, x=rng.normal(0, 3e-3, n), px=rng.normal(0, 3e-5, n),
+              y=rng.normal(0, 3e-3, n), zeta=rng.normal(0, 0.1, n), delta=rng.normal(0, 1e-4, n))
+    names = [line.element_names[k] for k in (0, 1, 3, 17, 250, 499, 500)]
+    ref = _multi_element_oracle(line, kw, names, 5)
+    line.build_tracker(device="cuda")
+    p = xt.Particles(device="cuda", **kw)
+    line.track(p, num_turns=5, multi_element_monitor_at=names)
+    mem = line.record_multi_element_last_track
+    got = mem.data
+    assert got.shape == ref.shape
+    scale = np.max(np.abs(ref), axis=(0, 1, 3), keepdims=True)
+    scale[scale == 0] = 1
+    assert np.max(np.abs(got - ref) / scale) <= 5e-14
+    assert np.array_equal(mem.get("x", obs_name=names[0], particle_id=3, turn=0), kw["x"][3])

@@ -10,7 +10,7 @@ from .elements import (Marker, Drift, Multipole, Bend, Quadrupole, Sextupole, Oc
                        Cavity, LimitEllipse, LimitRect, BeamElement)
 from .elements import *  # noqa: F401,F403  (slice classes)
 from .monitors import (ParticlesMonitor, LastTurnsMonitor, BeamPositionMonitor, BeamSizeMonitor,
-                       BeamProfileMonitor)
+                       BeamProfileMonitor, MultiElementMonitor)
 from .slicing import Strategy, Teapot, Uniform
 from .line import Line, TrackerConfig
 from .tracker import Tracker, TrackFlags

@@ -165,6 +165,15 @@ class XtgElementMonitor(ctypes.Structure):
     ]
 
 
+class XtgMultiElementMonitor(ctypes.Structure):
+    _fields_ = [
+        ("start_at_turn", ctypes.c_int64), ("stop_at_turn", ctypes.c_int64),
+        ("part_id_start", ctypes.c_int64), ("part_id_end", ctypes.c_int64),
+        ("mapping_len", ctypes.c_int64), ("n_obs", ctypes.c_int64),
+        ("at_element_mapping", ctypes.c_void_p), ("data", ctypes.c_void_p),
+    ]
+
+
 class XtgTuning(ctypes.Structure):
     _fields_ = [
         ("block_size", ctypes.c_int32),
@@ -203,7 +212,8 @@ LIB_PATH = os.path.join(_PKG_DIR, "libxtrack_gb300.so")
 
 EXPORTED_SYMBOLS = (
     "xtg_abi_version", "xtg_get_last_error", "xtg_lattice_create", "xtg_lattice_destroy",
-    "xtg_lattice_info", "xtg_track", "xtg_track_noalloc", "xtg_get_tuning", "xtg_set_tuning", "xtg_device_status",
+    "xtg_lattice_info", "xtg_track", "xtg_track_noalloc", "xtg_set_multi_element_monitor",
+    "xtg_get_tuning", "xtg_set_tuning", "xtg_device_status",
     "xtg_batch_create", "xtg_batch_destroy", "xtg_batch_get_tuning", "xtg_batch_set_tuning", "xtg_batch_device_status",
     "xtg_track_batch", "xtg_sync", "xtg_launch_count", "xtg_measure_fp64_peak",
     "xtg_mlp_gemm", "xtg_mlp_act_backward", "xtg_mlp_colsum", "xtg_mlp_loss", "xtg_mlp_adam",
@@ -245,6 +255,8 @@ def load_library(path=None):
     lib.xtg_track.restype = c.c_int32
     lib.xtg_track_noalloc.argtypes = lib.xtg_track.argtypes
     lib.xtg_track_noalloc.restype = c.c_int32
+    lib.xtg_set_multi_element_monitor.argtypes = [c.c_void_p, c.POINTER(XtgMultiElementMonitor)]
+    lib.xtg_set_multi_element_monitor.restype = c.c_int32
     lib.xtg_get_tuning.argtypes = [c.c_void_p, c.POINTER(XtgTuning)]
     lib.xtg_get_tuning.restype = c.c_int32
     lib.xtg_set_tuning.argtypes = [c.c_void_p, c.POINTER(XtgTuning)]

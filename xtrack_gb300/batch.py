@@ -106,6 +106,8 @@ class BatchTracker(Tracker):
         """Tracks ``particles``; particle slot i through lattice
         ``lattice_index[i]`` (the seed's position in ``lines``). Takes the
         keyword arguments of ``Line.track``."""
+        if kwargs.get("multi_element_monitor_at"):
+            raise NotImplementedError("multi_element_monitor_at is not supported for batches")
         idx = torch.as_tensor(lattice_index, dtype=torch.int32, device=particles.device)
         if idx.dim() != 1 or idx.numel() != particles._capacity:
             raise ValueError("lattice_index needs one entry per particle slot "

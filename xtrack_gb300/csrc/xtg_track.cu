@@ -112,6 +112,7 @@ struct TrackArgs {
     int32_t* err;
     xtg_particles P;
     xtg_monitor M;
+    xtg_multi_element_monitor E;               // E.data == NULL: none
 };
 
 __device__ __forceinline__ bool flag_on(uint64_t flags, int bit) { return (flags >> bit) & 1u; }
@@ -313,6 +314,25 @@ __device__ __noinline__ void monitor_profile(const MonProfileRec& r, const PStat
 // ---------------------------------------------------------------------------
 // one element record
 // ---------------------------------------------------------------------------
+
+// multi_element_monitor.h:10-65, before an element
+__device__ __noinline__ void multi_element_monitor(const xtg_multi_element_monitor& E, const PState& p,
+                                                   int64_t pid) {
+    int64_t const at_turn = p.at_turn;
+    if (at_turn >= E.start_at_turn && at_turn < E.stop_at_turn && pid >= E.part_id_start &&
+        pid < E.part_id_end) {
+        int64_t const at_element = p.at_element;
+        int64_t store_at = -1;
+        if (at_element >= 0 && at_element < E.mapping_len) store_at = E.at_element_mapping[at_element];
+        if (store_at >= 0) {
+            int64_t const n_part = E.part_id_end - E.part_id_start;
+            int64_t const base =
+                (((at_turn - E.start_at_turn) * n_part + (pid - E.part_id_start)) * 7) * E.n_obs + store_at;
+            double const v[7] = {p.x, p.px, p.y, p.py, p.zeta, p.delta, p.s};
+            for (int c = 0; c < 7; c++) E.data[base + (int64_t)c * E.n_obs] = v[c];
+        }
+    }
+}
 template <bool kExact>
 __device__ __forceinline__ bool apply_record(PState& p, const unsigned char* __restrict__ rec,
                                              const TrackArgs& a, const RfCtx& rf, int64_t i, int64_t pid) {
@@ -391,6 +411,7 @@ __device__ __forceinline__ void walk(PState& p, bool& active, const unsigned cha
     int64_t const incr = a.backtrack ? -1 : 1;
     while (active && rec < rec_end) {
         if (a.flag_monitor == 2) monitor(a, p, i, pid);
+        if (a.E.data) multi_element_monitor(a.E, p, pid);
         bool const thick = apply_record<kExact>(p, rec, a, rf, i, pid);
         if (thick && !ignore_global) {
             // local_particle_custom_api.h:259-287
@@ -772,6 +793,7 @@ struct ExecCtx {
     std::vector<std::vector<xtg_element>> lattices;
     std::deque<xtg_element_monitor> monitors;  // owned copies of the monitor descriptors
     bool has_monitors = false;
+    xtg_multi_element_monitor multi_mon;       // data == NULL: none
     xtg_config config;
     int device = 0;
     DevTables fwd, bwd;
@@ -780,6 +802,7 @@ struct ExecCtx {
     std::vector<double> flops;                 // per element (first lattice)
     std::mutex mu;
     ExecCtx() {
+        memset(&multi_mon, 0, sizeof(multi_mon));
         tune.block_size = 256;
         tune.compact_every = 0;
         tune.chunk_bytes = 49152;
@@ -1098,7 +1121,8 @@ static int32_t track_impl(ExecCtx* C, const xtg_particles* particles, const int3
     a.rec_count = num_ele_track;
     a.chunk_bytes = chunk;
     a.flag_monitor = flag_monitor;
-    a.load_pid = (flag_monitor != 0 || C->has_monitors) ? 1 : 0;
+    a.load_pid = (flag_monitor != 0 || C->has_monitors || C->multi_mon.data) ? 1 : 0;
+    a.E = C->multi_mon;
     a.flag_end_turn_actions = flag_end_turn_actions;
     a.flag_reset_s = flag_reset_s_at_end_turn;
     a.backtrack = backtrack ? 1 : 0;
@@ -1280,6 +1304,21 @@ int32_t xtg_lattice_info(const xtg_lattice* L, int64_t* n_elements, int64_t ele_
     return XTG_OK;
 }
 
+int32_t xtg_set_multi_element_monitor(xtg_lattice* L, const xtg_multi_element_monitor* m) {
+    if (!L) return set_error(XTG_E_NULL, "xtg_set_multi_element_monitor: NULL lattice");
+    if (!m) {
+        memset(&L->ctx.multi_mon, 0, sizeof(L->ctx.multi_mon));
+        return XTG_OK;
+    }
+    if (!m->data || !m->at_element_mapping)
+        return set_error(XTG_E_NULL, "xtg_set_multi_element_monitor: NULL buffer");
+    if (m->mapping_len < 0 || m->n_obs < 1 || m->part_id_end < m->part_id_start ||
+        m->stop_at_turn < m->start_at_turn)
+        return set_error(XTG_E_VALUE, "xtg_set_multi_element_monitor: inconsistent sizes");
+    L->ctx.multi_mon = *m;
+    return XTG_OK;
+}
+
 int32_t xtg_get_tuning(const xtg_lattice* L, xtg_tuning* out) {
     if (!L || !out) return set_error(XTG_E_NULL, "xtg_get_tuning: NULL argument");
     *out = L->ctx.tune;
@@ -1376,7 +1415,8 @@ int32_t xtg_track_noalloc(const xtg_lattice* lattice, const xtg_particles* parti
     a.rec_first = rec_first;
     a.rec_count = num_ele_track;
     a.flag_monitor = flag_monitor;
-    a.load_pid = (flag_monitor != 0 || C->has_monitors) ? 1 : 0;
+    a.load_pid = (flag_monitor != 0 || C->has_monitors || C->multi_mon.data) ? 1 : 0;
+    a.E = C->multi_mon;
     a.flag_end_turn_actions = flag_end_turn_actions;
     a.flag_reset_s = flag_reset_s_at_end_turn;
     a.backtrack = backtrack ? 1 : 0;

@@ -139,16 +139,22 @@ class Line:
     def track(self, particles, ele_start=0, ele_stop=None, num_elements=None, num_turns=None,
               turn_by_turn_monitor=None, freeze_longitudinal=False, time=False,
               with_progress=False, backtrack=False, **kwargs):
-        """Tracks ``particles`` in place (line.py:1902-1994)."""
-        if kwargs.get("multi_element_monitor_at"):
-            raise NotImplementedError("multi_element_monitor_at is not supported")
+        """Tracks ``particles`` in place (line.py:1902-1994).
+        ``multi_element_monitor_at``: element names (or '_all_') at which
+        x, px, y, py, zeta, delta, s are recorded before the element, every
+        turn (tracker.py:1482-1525); the record is
+        ``line.record_multi_element_last_track``."""
+        unknown = set(kwargs) - {"multi_element_monitor_at"}
+        if unknown:
+            raise TypeError(f"unexpected arguments {unknown}")
         if not self._has_valid_tracker():
             self.build_tracker(device=particles.device)
         return self.tracker._track(particles, ele_start=ele_start, ele_stop=ele_stop,
                                    num_elements=num_elements, num_turns=num_turns,
                                    turn_by_turn_monitor=turn_by_turn_monitor,
                                    freeze_longitudinal=freeze_longitudinal, time=time,
-                                   with_progress=with_progress, backtrack=backtrack)
+                                   with_progress=with_progress, backtrack=backtrack,
+                                   multi_element_monitor_at=kwargs.get("multi_element_monitor_at"))
 
     @property
     def record_last_track(self):
@@ -157,6 +163,10 @@ class Line:
     @property
     def time_last_track(self):
         return self.tracker.time_last_track if self.tracker else None
+
+    @property
+    def record_multi_element_last_track(self):
+        return self.tracker.record_multi_element_last_track if self.tracker else None
 
     @property
     def track_flags(self):

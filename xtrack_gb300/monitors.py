@@ -362,3 +362,54 @@ class BeamProfileMonitor(_MonitorElement):
             e = self.__getattr__(attr[0] + "_edges")
             return 0.5 * (e[1:] + e[:-1])
         raise AttributeError(attr)
+
+
+class MultiElementMonitor:
+    """Coordinates at several elements of the line, every turn
+    (multi_element_monitor.py): ``data[turn, particle, coordinate, obs]``
+    with coordinates x, px, y, py, zeta, delta, s, filled before each
+    observed element. Built by ``Line.track(..., multi_element_monitor_at=
+    [...])``."""
+    _coord_name_to_index = {"x": 0, "px": 1, "y": 2, "py": 3, "zeta": 4, "delta": 5, "s": 6}
+
+    def __init__(self, start_at_turn, stop_at_turn, part_id_start, part_id_end,
+                 at_element_mapping, obs_names, device=None):
+        self.start_at_turn = int(start_at_turn)
+        self.stop_at_turn = int(stop_at_turn)
+        self.part_id_start = int(part_id_start)
+        self.part_id_end = int(part_id_end)
+        self.obs_names = list(obs_names)
+        self._name_to_index = {n: k for k, n in enumerate(self.obs_names)}
+        self.device = torch.device(device) if device is not None else default_device()
+        self._mapping = torch.as_tensor(np.asarray(at_element_mapping, dtype=np.int64),
+                                        device=self.device)
+        shape = (self.stop_at_turn - self.start_at_turn, self.part_id_end - self.part_id_start,
+                 7, len(self.obs_names))
+        self._data = torch.zeros(shape, dtype=torch.float64, device=self.device)
+
+    def _xtg_struct(self):
+        m = _abi.XtgMultiElementMonitor()
+        m.start_at_turn = self.start_at_turn
+        m.stop_at_turn = self.stop_at_turn
+        m.part_id_start = self.part_id_start
+        m.part_id_end = self.part_id_end
+        m.mapping_len = self._mapping.numel()
+        m.n_obs = len(self.obs_names)
+        m.at_element_mapping = self._mapping.data_ptr()
+        m.data = self._data.data_ptr()
+        return m
+
+    @property
+    def data(self):
+        return self._data.cpu().numpy()
+
+    def get(self, coordinate, obs_name=None, particle_id=None, turn=None):
+        c = self._coord_name_to_index[coordinate]
+        o = slice(None) if obs_name is None else self._name_to_index[obs_name]
+        pi = slice(None) if particle_id is None else particle_id - self.part_id_start
+        ti = slice(None) if turn is None else turn - self.start_at_turn
+        return self.data[ti, pi, c, o]
+
+    def __repr__(self):
+        names = self.obs_names if len(self.obs_names) < 5 else self.obs_names[:5] + ["..."]
+        return f"MultiElementMonitor(obs_names=[{', '.join(names)}])"

@@ -13,7 +13,7 @@ import numpy as np
 import torch
 
 from . import _abi
-from .monitors import ParticlesMonitor
+from .monitors import MultiElementMonitor, ParticlesMonitor
 
 ARITH = {"exact": _abi.ARITH_EXACT, "fast": _abi.ARITH_FAST}
 
@@ -80,6 +80,7 @@ class Tracker:
                 ctypes.byref(self._cfg), ctypes.byref(handle)), self._lib)
         self._handle = handle
         self.record_last_track = None
+        self.record_multi_element_last_track = None
         self.time_last_track = None
 
     def __del__(self):
@@ -142,6 +143,11 @@ class Tracker:
             return (2 if turn_by_turn_monitor.ebe_mode == 1 else 1), turn_by_turn_monitor
         raise ValueError("Please provide a valid monitor object")
 
+    def _set_multi_element_monitor(self, mem):
+        st = self._lib.xtg_set_multi_element_monitor(
+            self._handle, ctypes.byref(mem._xtg_struct()) if mem is not None else None)
+        _abi.check(st, self._lib)
+
     def _launch(self, pstruct, num_turns, ele_start, num_ele_track, flag_end, flag_monitor,
                 mstruct, flags, stream):
         st = self._lib.xtg_track(
@@ -152,9 +158,32 @@ class Tracker:
             int(flags), ctypes.c_void_p(stream))
         _abi.check(st, self._lib)
 
+    def _get_multi_element_monitor(self, multi_element_monitor_at, particles, num_turns):
+        """tracker.py:1482-1525."""
+        if multi_element_monitor_at is None or len(multi_element_monitor_at) == 0:
+            return None
+        names = list(self.line.element_names)
+        if isinstance(multi_element_monitor_at, str):
+            if multi_element_monitor_at != "_all_":
+                raise ValueError("multi_element_monitor_at must be a list of names or '_all_'")
+            multi_element_monitor_at = names
+        index = {n: i for i, n in reversed(list(enumerate(names)))}
+        missing = [n for n in multi_element_monitor_at if n not in index]
+        if missing:
+            raise ValueError(f"Elements not found in line: {set(missing)}")
+        obs = [index[n] for n in multi_element_monitor_at]
+        mapping = np.full(len(names) + 1, -1, dtype=np.int64)
+        mapping[obs] = np.arange(len(obs), dtype=np.int64)
+        start, end = particles.get_active_particle_id_range()
+        return MultiElementMonitor(start_at_turn=0, stop_at_turn=num_turns or 1,
+                                   part_id_start=start, part_id_end=end,
+                                   at_element_mapping=mapping,
+                                   obs_names=[names[i] for i in obs], device=particles.device)
+
     def _track(self, particles, ele_start=0, ele_stop=None, num_elements=None, num_turns=None,
                turn_by_turn_monitor=None, freeze_longitudinal=False, time=False,
-               with_progress=False, backtrack=False, _force_no_end_turn_actions=False):
+               with_progress=False, backtrack=False, _force_no_end_turn_actions=False,
+               multi_element_monitor_at=None):
         if freeze_longitudinal:
             raise NotImplementedError("freeze_longitudinal is not supported")
         if particles.device.type != "cuda":
@@ -235,19 +264,27 @@ class Tracker:
         if backtrack:
             flags = np.uint64(int(flags) | (1 << _abi.FLAG_BACKTRACK))
 
+        mem = self._get_multi_element_monitor(multi_element_monitor_at, particles, monitor_turns)
         pstruct = particles._xtg_struct()
         stream = torch.cuda.current_stream(particles.device).cuda_stream
         with torch.cuda.device(particles.device):
-            self._launch(pstruct, 1, ele_start, num_elements_first_turn, flag_end_first,
-                         flag_monitor, mstruct, flags, stream)
-            if num_middle_turns > 0:
-                self._launch(pstruct, num_middle_turns, 0, L, flag_end_middle, flag_monitor,
-                             mstruct, flags, stream)
-            if num_elements_last_turn > 0:
-                self._launch(pstruct, 1, 0, num_elements_last_turn, False, flag_monitor,
-                             mstruct, flags, stream)
+            if mem is not None:
+                self._set_multi_element_monitor(mem)
+            try:
+                self._launch(pstruct, 1, ele_start, num_elements_first_turn, flag_end_first,
+                             flag_monitor, mstruct, flags, stream)
+                if num_middle_turns > 0:
+                    self._launch(pstruct, num_middle_turns, 0, L, flag_end_middle, flag_monitor,
+                                 mstruct, flags, stream)
+                if num_elements_last_turn > 0:
+                    self._launch(pstruct, 1, 0, num_elements_last_turn, False, flag_monitor,
+                                 mstruct, flags, stream)
+            finally:
+                if mem is not None:
+                    self._set_multi_element_monitor(None)
 
         self.record_last_track = monitor
+        self.record_multi_element_last_track = mem
         if time:
             torch.cuda.synchronize(particles.device)
             self.time_last_track = _time.perf_counter() - t0
