@@ -343,9 +343,13 @@ def run_da_screen(args):
         return rng.integers(mean // 2, mean * 3 // 2 + 1, size=n)
 
     def features(scan):
+        # coordinates, the seed's multipole-error summary and its linear
+        # tunes (the tunes set the resonances that bound the DA; the error
+        # RMS over hundreds of magnets barely differs between seeds)
         d = scan.deltas[scan.delta_index]
         return np.concatenate([sg.coord_features(scan.r, scan.theta, d),
-                               scan.seed_features[scan.lattice_index]], axis=1)
+                               scan.seed_features[scan.lattice_index],
+                               scan.tunes[scan.lattice_index][:, :2]], axis=1)
 
     train_lines = [workloads.thick_ring(seed=100 + s) for s in range(args.da_train_seeds)]
     test_lines = [workloads.thick_ring(seed=200 + s) for s in range(args.da_test_seeds)]
@@ -366,7 +370,7 @@ def run_da_screen(args):
     st, at, _ = sc.run_scan(bt_train, s_train, turns, device=dev)
     t_train_scan = time.perf_counter() - t0
     surv, lt = sg.targets(st, at, turns)
-    net = sg.SurvivalMLP(seed=0, device=dev)
+    net = sg.SurvivalMLP(n_in=sg.N_COORD_FEATURES + sg.N_SEED_FEATURES + 2, seed=0, device=dev)
     t0 = time.perf_counter()
     hist = net.fit(features(s_train), surv, lt, epochs=args.da_epochs, batch=4096, lr=3e-3)
     torch.cuda.synchronize(dev)
@@ -458,7 +462,7 @@ def main():
                     help="mean particles per seed (uniform in [n/2, 3n/2])")
     ap.add_argument("--da-train-seeds", dest="da_train_seeds", type=int, default=6)
     ap.add_argument("--da-test-seeds", dest="da_test_seeds", type=int, default=4)
-    ap.add_argument("--da-epochs", dest="da_epochs", type=int, default=30)
+    ap.add_argument("--da-epochs", dest="da_epochs", type=int, default=40)
     args = ap.parse_args()
     if args.workload == "da_screen":
         run_da_screen(args)

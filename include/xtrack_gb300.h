@@ -57,7 +57,8 @@ extern "C" {
 #define XTG_CLS_LIMIT_ELLIPSE   8   /* limit_ellipse.py, limitellipse.h      */
 #define XTG_CLS_LIMIT_RECT      9   /* limit_rect.py, limitrect.h            */
 #define XTG_CLS_MONITOR        10   /* monitors/*.py placed in the line      */
-#define XTG_NUM_CLS            11
+#define XTG_CLS_LIMIT_POLYGON  11   /* limit_polygon.py, limitpolygon.h      */
+#define XTG_NUM_CLS            12
 
 /* Slice kind of a record (slice classes of slice_elements_*.py). A slice
  * record carries its parent's parameters plus its own `weight`. */
@@ -117,11 +118,21 @@ typedef struct xtg_element {
     /* Misalignment fields (base_element.py:274-282); must all be zero. */
     double shift_x, shift_y, shift_s;
     double rot_x_rad, rot_y_rad, rot_s_rad, rot_s_rad_no_frame;
-    /* XTG_CLS_MONITOR: host address of an xtg_element_monitor, read by
-     * xtg_lattice_create (its buffers are device pointers kept by the
-     * caller for the lattice's lifetime); 0 for the other classes. */
-    uint64_t monitor;
+    /* Host address of the class's extra description, read by
+     * xtg_lattice_create, 0 for the other classes:
+     *   XTG_CLS_MONITOR        an xtg_element_monitor (its buffers are
+     *                          device pointers kept by the caller for the
+     *                          lattice's lifetime);
+     *   XTG_CLS_LIMIT_POLYGON  an xtg_polygon (vertices copied). */
+    uint64_t aux;
 } xtg_element;
+
+/* Vertices of a LimitPolygon aperture (limit_polygon.py), host arrays. */
+typedef struct xtg_polygon {
+    int64_t n_vertices;
+    const double* x_vertices;
+    const double* y_vertices;
+} xtg_polygon;
 
 /*
  * Particles structure-of-arrays (particles.py:26-83). Pointers are device

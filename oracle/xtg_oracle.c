@@ -1363,7 +1363,7 @@ static int xto_apply(const xtg_element* e, const xtg_config* cfg, xto_part* p,
         return 0;
     case XTG_CLS_MONITOR: {
         /* monitors/*.py: get_backtrack_element is a Marker */
-        const xtg_element_monitor* m = (const xtg_element_monitor*)(uintptr_t)e->monitor;
+        const xtg_element_monitor* m = (const xtg_element_monitor*)(uintptr_t)e->aux;
         if (backtrack) return 0;
         if (m->kind == XTG_MON_PARTICLES) xto_monitor(&m->particles, p, src, isrc);
         else if (m->kind == XTG_MON_LAST_TURNS) xto_last_turns(m, p);
@@ -1392,6 +1392,49 @@ static int xto_apply(const xtg_element* e, const xtg_config* cfg, xto_part* p,
         double const temp = x * x * e->b_squ + y * y * e->a_squ;
         int64_t const is_alive = (int64_t)(temp <= e->a_b_squ);
         if (!is_alive) p->state = 0;
+        return 0;
+    }
+    case XTG_CLS_LIMIT_POLYGON: {
+        /* limitpolygon.h:13-90 (CPU build: inscribed-circle shortcut) */
+        if (flag_set(p, XTG_FLAG_IGNORE_LOCAL_APERTURE)) return 0;
+        const xtg_polygon* pg = (const xtg_polygon*)(uintptr_t)e->aux;
+        int64_t const N_edg = pg->n_vertices;
+        double inner_radius_sq = 0.0;
+        for (int64_t ii = 0; ii < N_edg; ii++) {
+            int64_t const jj = (ii + 1) % N_edg;
+            double const x0 = pg->x_vertices[ii], y0 = pg->y_vertices[ii];
+            double const x1 = pg->x_vertices[jj], y1 = pg->y_vertices[jj];
+            double const dx = x1 - x0;
+            double const dy = y1 - y0;
+            double const seg_len_sq = dx * dx + dy * dy;
+            double dist_sq;
+            if (seg_len_sq > 0.0) {
+                double t = -(x0 * dx + y0 * dy) / seg_len_sq;
+                if (t < 0.0) t = 0.0;
+                else if (t > 1.0) t = 1.0;
+                double const x_proj = x0 + t * dx;
+                double const y_proj = y0 + t * dy;
+                dist_sq = x_proj * x_proj + y_proj * y_proj;
+            } else {
+                dist_sq = x0 * x0 + y0 * y0;
+            }
+            if (ii == 0 || dist_sq < inner_radius_sq) inner_radius_sq = dist_sq;
+        }
+        double const x = p->x, y = p->y;
+        if (x * x + y * y > inner_radius_sq) {
+            int64_t ii = 0, jj = N_edg - 1;
+            int64_t is_alive = 0;
+            while (ii < N_edg) {
+                double const Vx_ii = pg->x_vertices[ii], Vx_jj = pg->x_vertices[jj];
+                double const Vy_ii = pg->y_vertices[ii], Vy_jj = pg->y_vertices[jj];
+                if (((Vy_ii > y) != (Vy_jj > y)) &&
+                    (x < (Vx_jj - Vx_ii) * (y - Vy_ii) / (Vy_jj - Vy_ii) + Vx_ii))
+                    is_alive = !is_alive;
+                jj = ii;
+                ii++;
+            }
+            if (!is_alive) p->state = 0;
+        }
         return 0;
     }
     case XTG_CLS_LIMIT_RECT: {
@@ -1529,8 +1572,11 @@ int32_t xto_validate(const xtg_element* els, int64_t n, char* msg, int64_t msg_l
         const xtg_element* e = &els[i];
         const char* why = NULL;
         if (e->cls < 0 || e->cls >= XTG_NUM_CLS) why = "unknown element class";
-        else if (e->cls == XTG_CLS_MONITOR && e->monitor == 0)
+        else if (e->cls == XTG_CLS_MONITOR && e->aux == 0)
             why = "monitor element without its descriptor";
+        else if (e->cls == XTG_CLS_LIMIT_POLYGON &&
+                 (e->aux == 0 || ((const xtg_polygon*)(uintptr_t)e->aux)->n_vertices < 3))
+            why = "LimitPolygon needs at least 3 vertices";
         else if (e->slice < 0 || e->slice > XTG_SLICE_EXIT) why = "unknown slice kind";
         else if (e->order < 0 || e->order >= XTG_MAX_KNL) why = "multipole order out of range";
         else if (e->order_rel < -1 || e->order_rel >= 20) why = "relative multipole order out of range (0..19)";
@@ -1876,7 +1922,7 @@ int32_t xto_abi_sizes(int64_t* out) {
     out[6] = (int64_t)offsetof(xtg_monitor, data);
     out[7] = (int64_t)sizeof(xtg_element_monitor);
     out[8] = (int64_t)offsetof(xtg_element_monitor, particles);
-    out[9] = (int64_t)offsetof(xtg_element, monitor);
+    out[9] = (int64_t)offsetof(xtg_element, aux);
     return 4;
 }
 

@@ -52,7 +52,7 @@ def test_ctypes_layout_matches_c():
     assert out[6] == _abi.XtgMonitor.data.offset
     assert out[7] == ctypes.sizeof(_abi.XtgElementMonitor)
     assert out[8] == _abi.XtgElementMonitor.particles.offset
-    assert out[9] == _abi.XtgElement.monitor.offset
+    assert out[9] == _abi.XtgElement.aux.offset
 
 
 @pytest.mark.parametrize("element,msg", [

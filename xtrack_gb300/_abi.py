@@ -38,6 +38,7 @@ CLS_CAVITY = 7
 CLS_LIMIT_ELLIPSE = 8
 CLS_LIMIT_RECT = 9
 CLS_MONITOR = 10
+CLS_LIMIT_POLYGON = 11
 
 SLICE_NONE = 0
 SLICE_THICK = 1
@@ -96,7 +97,7 @@ class XtgElement(ctypes.Structure):
         ("shift_x", ctypes.c_double), ("shift_y", ctypes.c_double), ("shift_s", ctypes.c_double),
         ("rot_x_rad", ctypes.c_double), ("rot_y_rad", ctypes.c_double),
         ("rot_s_rad", ctypes.c_double), ("rot_s_rad_no_frame", ctypes.c_double),
-        ("monitor", ctypes.c_uint64),
+        ("aux", ctypes.c_uint64),
     ]
 
 
@@ -135,6 +136,11 @@ class XtgMonitor(ctypes.Structure):
         ("n_records", ctypes.c_int64),
         ("data", XtgParticles),
     ]
+
+
+class XtgPolygon(ctypes.Structure):
+    _fields_ = [("n_vertices", ctypes.c_int64), ("x_vertices", ctypes.c_void_p),
+                ("y_vertices", ctypes.c_void_p)]
 
 
 MON_PARTICLES = 1

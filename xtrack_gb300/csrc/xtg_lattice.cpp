@@ -411,8 +411,14 @@ int32_t validate_element(const xtg_element& e, int64_t idx, std::string* why) {
     } else if (e.slice != XTG_SLICE_NONE) {
         return fail("slice kind not valid for this class");
     }
+    if (e.cls == XTG_CLS_LIMIT_POLYGON) {
+        const xtg_polygon* pg = reinterpret_cast<const xtg_polygon*>(e.aux);
+        if (!pg) return fail("LimitPolygon without its vertices");
+        if (pg->n_vertices < 3 || !pg->x_vertices || !pg->y_vertices)
+            return fail("LimitPolygon needs at least 3 vertices");
+    }
     if (e.cls == XTG_CLS_MONITOR) {
-        const xtg_element_monitor* m = reinterpret_cast<const xtg_element_monitor*>(e.monitor);
+        const xtg_element_monitor* m = reinterpret_cast<const xtg_element_monitor*>(e.aux);
         if (!m) return fail("monitor element without its descriptor");
         if (m->kind == XTG_MON_LAST_TURNS) {
             if (m->n_last_turns < 1 || m->every_n_turns < 1 || m->num_particles < 0)
@@ -859,7 +865,7 @@ int32_t pack_lattice(const xtg_element* els, int64_t n, const xtg_config& cfg,
         case XTG_CLS_MONITOR: {
             // monitors are replaced by markers in backtracking tables
             // (get_backtrack_element of monitors/*.py)
-            const xtg_element_monitor* m = reinterpret_cast<const xtg_element_monitor*>(e.monitor);
+            const xtg_element_monitor* m = reinterpret_cast<const xtg_element_monitor*>(e.aux);
             if (backtrack) {
                 rb.init(sizeof(RecHeader));
                 rb.head<RecHeader>()->op = OP_NOP;
@@ -921,6 +927,42 @@ int32_t pack_lattice(const xtg_element* els, int64_t n, const xtg_config& cfg,
                 r->x_sum = m->x_sum;
                 r->y_sum = m->y_sum;
             }
+            break;
+        }
+        case XTG_CLS_LIMIT_POLYGON: {
+            // limitpolygon.h:13-90; the inscribed-circle radius of the CPU
+            // build is computed here once (limitpolygon.h:27-62)
+            const xtg_polygon* pg = reinterpret_cast<const xtg_polygon*>(e.aux);
+            int64_t const nv = pg->n_vertices;
+            double inner_radius_sq = 0.0;
+            for (int64_t ii = 0; ii < nv; ii++) {
+                int64_t const jj = (ii + 1) % nv;
+                double const x0 = pg->x_vertices[ii], y0 = pg->y_vertices[ii];
+                double const x1 = pg->x_vertices[jj], y1 = pg->y_vertices[jj];
+                double const dx = x1 - x0;
+                double const dy = y1 - y0;
+                double const seg_len_sq = dx * dx + dy * dy;
+                double dist_sq;
+                if (seg_len_sq > 0.0) {
+                    double t = -(x0 * dx + y0 * dy) / seg_len_sq;
+                    if (t < 0.0) t = 0.0;
+                    else if (t > 1.0) t = 1.0;
+                    double const xp = x0 + t * dx;
+                    double const yp = y0 + t * dy;
+                    dist_sq = xp * xp + yp * yp;
+                } else {
+                    dist_sq = x0 * x0 + y0 * y0;
+                }
+                if (ii == 0 || dist_sq < inner_radius_sq) inner_radius_sq = dist_sq;
+            }
+            rb.init(sizeof(LimitPolygonRec));
+            LimitPolygonRec* r = rb.head<LimitPolygonRec>();
+            r->h.op = OP_LIMIT_POLYGON;
+            r->n = nv;
+            r->inner_radius_sq = inner_radius_sq;
+            rb.append(pg->x_vertices, (size_t)nv, sizeof(LimitPolygonRec));
+            rb.append(pg->y_vertices, (size_t)nv, sizeof(LimitPolygonRec));
+            rb.pad16();
             break;
         }
         case XTG_CLS_LIMIT_RECT: {

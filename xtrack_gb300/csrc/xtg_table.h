@@ -31,6 +31,7 @@ enum Op : int32_t {
     OP_MON_LAST_TURNS = 8,
     OP_MON_BPM = 9,       // beam position and beam size monitors
     OP_MON_PROFILE = 10,
+    OP_LIMIT_POLYGON = 11,
 };
 
 // RecHeader.flags
@@ -60,6 +61,13 @@ struct alignas(16) LimitEllipseRec {
 struct alignas(16) LimitRectRec {
     RecHeader h;
     double min_x, max_x, min_y, max_y;
+};
+
+// LimitPolygon (limitpolygon.h:13-90): x vertices then y vertices follow.
+struct alignas(16) LimitPolygonRec {
+    RecHeader h;
+    int64_t n;
+    double inner_radius_sq;   // points inside this circle skip the test
 };
 
 // Integrators (reference numbering, _common.py:40-47)

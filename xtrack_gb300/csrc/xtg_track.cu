@@ -383,6 +383,29 @@ __device__ __forceinline__ bool apply_record(PState& p, const unsigned char* __r
         }
         break;
     }
+    case OP_LIMIT_POLYGON: {
+        // limitpolygon.h:64-90 (crossing-number test)
+        if (!flag_on(a.track_flags, XTG_FLAG_IGNORE_LOCAL_APERTURE)) {
+            const LimitPolygonRec& r = *reinterpret_cast<const LimitPolygonRec*>(rec);
+            const double* vx = reinterpret_cast<const double*>(rec + sizeof(LimitPolygonRec));
+            const double* vy = vx + r.n;
+            double const x = p.x, y = p.y;
+            if (x * x + y * y > r.inner_radius_sq) {
+                int64_t ii = 0, jj = r.n - 1;
+                bool alive = false;
+                while (ii < r.n) {
+                    double const vx_ii = vx[ii], vx_jj = vx[jj], vy_ii = vy[ii], vy_jj = vy[jj];
+                    if (((vy_ii > y) != (vy_jj > y)) &&
+                        (x < (vx_jj - vx_ii) * (y - vy_ii) / (vy_jj - vy_ii) + vx_ii))
+                        alive = !alive;
+                    jj = ii;
+                    ii++;
+                }
+                if (!alive) p.state = 0;
+            }
+        }
+        break;
+    }
     case OP_MON_PARTICLES: {
         const MonParticlesRec& r = *reinterpret_cast<const MonParticlesRec*>(rec);
         monitor_into(r.m, a.P, p, i, pid, a.backtrack != 0);
@@ -829,9 +852,9 @@ struct xtg_batch {
 static void own_monitors(ExecCtx* C) {
     for (auto& els : C->lattices)
         for (auto& e : els)
-            if (e.cls == XTG_CLS_MONITOR && e.monitor) {
-                C->monitors.push_back(*reinterpret_cast<const xtg_element_monitor*>(e.monitor));
-                e.monitor = reinterpret_cast<uint64_t>(&C->monitors.back());
+            if (e.cls == XTG_CLS_MONITOR && e.aux) {
+                C->monitors.push_back(*reinterpret_cast<const xtg_element_monitor*>(e.aux));
+                e.aux = reinterpret_cast<uint64_t>(&C->monitors.back());
                 C->has_monitors = true;
             }
 }

@@ -508,6 +508,97 @@ class LimitRect(BeamElement):
                 ("min_y", self.min_y), ("max_y", self.max_y)]
 
 
+class LimitPolygon(BeamElement):
+    """Polygonal aperture (limit_polygon.py): a particle survives when the
+    crossing-number test puts (x, y) inside the closed polygon of the
+    vertices (limitpolygon.h:13-90)."""
+    _cls = _abi.CLS_LIMIT_POLYGON
+
+    def __init__(self, x_vertices=None, y_vertices=None):
+        x = np.ascontiguousarray(x_vertices, dtype=np.float64)
+        y = np.ascontiguousarray(y_vertices, dtype=np.float64)
+        if x.shape != y.shape or x.ndim != 1 or len(x) < 3:
+            raise ValueError("LimitPolygon needs matching x/y vertex arrays of length >= 3")
+        xc, yc = np.append(x, x[0]), np.append(y, y[0])
+        if not np.all(np.hypot(np.diff(xc), np.diff(yc)) > 0):
+            raise ValueError("LimitPolygon has repeated consecutive vertices")
+        self.x_vertices = x
+        self.y_vertices = y
+
+    @property
+    def x_closed(self):
+        return np.append(self.x_vertices, self.x_vertices[0])
+
+    @property
+    def y_closed(self):
+        return np.append(self.y_vertices, self.y_vertices[0])
+
+    def get_area(self, signed=False):
+        """Shoelace formula."""
+        x, y = self.x_closed, self.y_closed
+        a = 0.5 * np.sum(x[:-1] * y[1:] - x[1:] * y[:-1])
+        return a if signed else abs(a)
+
+    @property
+    def area(self):
+        return self.get_area()
+
+    def impact_point_and_normal(self, x_in, y_in, z_in, x_out, y_out, z_out):
+        """First crossing of each segment (in -> out) with the polygon's
+        boundary and the unit normal of the edge crossed, with the
+        reference's orientation (limit_polygon.py: (-dy, dx) along the edge
+        of a counter-clockwise polygon, i.e. pointing inwards): returns x, y,
+        z of the crossings, Nx, Ny, and the index of the edge."""
+        x_in, y_in, z_in = (np.atleast_1d(np.asarray(v, dtype=np.float64)) for v in (x_in, y_in, z_in))
+        x_out, y_out, z_out = (np.atleast_1d(np.asarray(v, dtype=np.float64))
+                               for v in (x_out, y_out, z_out))
+        xc, yc = self.x_closed, self.y_closed
+        ex, ey = np.diff(xc), np.diff(yc)
+        nx, ny = -ey, ex
+        if self.get_area(signed=True) < 0:
+            nx, ny = -nx, -ny
+        norm = np.hypot(nx, ny)
+        nx, ny = nx / norm, ny / norm
+        n = len(x_in)
+        out = [np.zeros(n) for _ in range(5)]
+        found = np.full(n, -1, dtype=np.int64)
+        for k in range(n):
+            dx, dy = x_out[k] - x_in[k], y_out[k] - y_in[k]
+            best = np.inf
+            for i in range(len(ex)):
+                den = dx * ey[i] - dy * ex[i]
+                if den == 0:
+                    continue
+                wx, wy = xc[i] - x_in[k], yc[i] - y_in[k]
+                t = (wx * ey[i] - wy * ex[i]) / den      # along the segment
+                u = (wx * dy - wy * dx) / den            # along the edge
+                if 0 <= t <= 1 and 0 <= u <= 1 and t < best:
+                    best = t
+                    found[k] = i
+            if found[k] >= 0:
+                t = best
+                i = found[k]
+                out[0][k] = x_in[k] + t * dx
+                out[1][k] = y_in[k] + t * dy
+                out[2][k] = z_in[k] + t * (z_out[k] - z_in[k])
+                out[3][k] = nx[i]
+                out[4][k] = ny[i]
+        if np.any(found < 0):
+            raise ValueError("a segment does not cross the polygon")
+        return out[0], out[1], out[2], out[3], out[4], found
+
+    def _fill(self, rec):
+        import ctypes
+        rec["cls"] = self._cls
+        desc = _abi.XtgPolygon(len(self.x_vertices), self.x_vertices.ctypes.data,
+                               self.y_vertices.ctypes.data)
+        self.__dict__.setdefault("_descs", []).append(desc)
+        rec["aux"] = ctypes.addressof(desc)
+
+    def _repr_items(self):
+        return [("n_vertices", len(self.x_vertices))]
+
+
 # ---------------------------------------------------------------------------
 # Slices (slice_elements_thick.py, slice_elements_thin.py,
 # slice_elements_drift.py, slice_elements_edge.py): a slice refers to its

@@ -15,11 +15,12 @@ Both steps run on the GPU push: the backtracking uses the line's own
 tracker with the backtracking flag, the forward pass a tracker of the
 short line.
 
-Built here: the reference's "replicate" mode, used when the two apertures
-are identical (same class and parameters; misalignments are not supported
-by the push at all). Consecutive apertures that differ use polygon
-interpolation in the reference (LimitPolygon, outside the push's element
-set): ``refine_loss_location`` raises NotImplementedError for them.
+Both of the reference's modes are built: "replicate" when the two
+apertures are identical (misalignments are not supported by the push at
+all), and polygon interpolation otherwise: each aperture is characterised
+as a convex polygon by tracking test particles on rays through it, and the
+apertures inserted along the gap are LimitPolygons whose vertices move
+linearly in s from one polygon to the other.
 """
 import numpy as np
 import torch
@@ -71,6 +72,10 @@ def apertures_are_identical(a, b):
     """loss_location_refinement.py:243-292 for the aperture classes of the push."""
     if type(a) is not type(b):
         return False
+    if isinstance(a, el.LimitPolygon):
+        return (len(a.x_vertices) == len(b.x_vertices)
+                and np.allclose(a.x_vertices, b.x_vertices, rtol=0, atol=1e-15)
+                and np.allclose(a.y_vertices, b.y_vertices, rtol=0, atol=1e-15))
     fields = {"LimitRect": ("min_x", "max_x", "min_y", "max_y"),
               "LimitEllipse": ("a_squ", "b_squ", "a_b_squ")}[type(a).__name__]
     return all(abs(getattr(a, f) - getattr(b, f)) <= 1e-15 for f in fields)
@@ -113,13 +118,26 @@ def _cut(e, pieces):
     raise NotImplementedError(f"cannot cut {type(e).__name__} for loss refinement")
 
 
-def build_interp_line(line, i_end_thin_0, i_start_thin_1, s0, s_vect, aperture):
-    """The short line: an aperture copy, the elements between the thick
-    neighbours of the two apertures with aperture copies at ``s_vect``
-    (cutting thick elements there), and a final aperture copy
-    (loss_location_refinement.py:493-530)."""
+def build_interp_line(line, i_end_thin_0, i_start_thin_1, s0, s_vect, aperture,
+                      aper_0=None, aper_1=None, aper_interp=None):
+    """The short line: the first aperture, the elements between the thick
+    neighbours of the two apertures with an aperture at each of ``s_vect``
+    (cutting thick elements there), and the last aperture
+    (loss_location_refinement.py:493-530). Copies of ``aperture`` serve
+    where ``aper_0`` / ``aper_1`` / ``aper_interp`` are not given."""
     from .line import Line, _element_length
-    elems = [aperture.copy()]
+    if aper_interp is None:
+        aper_interp = [aperture.copy() for _ in s_vect]
+    aper_iter = iter(aper_interp)
+
+    class _Next:
+        def copy(self):
+            return next(aper_iter)
+
+    first = aper_0 if aper_0 is not None else aperture.copy()
+    last = aper_1 if aper_1 is not None else aperture.copy()
+    aperture = _Next()
+    elems = [first]
     s = s0
     cuts = list(s_vect)
     ci = 0
@@ -164,7 +182,7 @@ def build_interp_line(line, i_end_thin_0, i_start_thin_1, s0, s_vect, aperture):
     while ci < len(cuts):
         elems.append(aperture.copy())
         ci += 1
-    elems.append(aperture.copy())
+    elems.append(last)
     names = [f"_interp_{k}" for k in range(len(elems))]
     out = Line(elements=elems, element_names=names)
     out.config.XTRACK_GLOBAL_XY_LIMIT = line.config.XTRACK_GLOBAL_XY_LIMIT
@@ -173,11 +191,95 @@ def build_interp_line(line, i_end_thin_0, i_start_thin_1, s0, s_vect, aperture):
     return out
 
 
+def _convex_hull_polygon(x, y):
+    """LimitPolygon through the convex hull of the points, vertices in
+    their original (angle) order (loss_location_refinement.py:449-455)."""
+    from scipy.spatial import ConvexHull
+    hull = ConvexHull(np.array([x, y]).T)
+    i_hull = np.sort(hull.vertices)
+    return el.LimitPolygon(x_vertices=x[i_hull], y_vertices=y[i_hull])
+
+
+def characterize_aperture(line, i_aperture, n_theta, r_max, dr, coming_from="upstream"):
+    """Polygon approximating the aperture seen from its thick neighbour
+    (loss_location_refinement.py:573-658): test particles on n_theta rays
+    are tracked from the thick neighbour through the aperture (two passes,
+    coarse then at step ``dr``); the first lost point of each ray gives a
+    vertex; the convex hull of these is resampled at every ray angle.
+    Returns (polygon, index of the first thin element)."""
+    assert coming_from in ("upstream", "downstream")
+    if coming_from == "upstream":
+        i_start = find_adjacent_thick(line, i_aperture, "upstream") + 1
+        i_stop = i_aperture + 1
+        backtrack = False
+        index_start_thin = i_start
+    else:
+        i_stop = find_adjacent_thick(line, i_aperture, "downstream")
+        i_start = i_aperture
+        backtrack = True
+        index_start_thin = i_stop - 1
+    theta = np.linspace(0, 2 * np.pi, n_theta + 1)[:-1]
+    rmin, rmax = 0.0, r_max
+    step = (rmax - rmin) / 100.
+    rmin_theta = 0 * theta
+    tr = line.tracker
+    for iteration in range(2):
+        r_vect = np.arange(rmin, rmax, step)
+        RR, TT = np.meshgrid(r_vect, theta)
+        RR += np.atleast_2d(rmin_theta).T
+        x_test = RR.flatten() * np.cos(TT.flatten())
+        y_test = RR.flatten() * np.sin(TT.flatten())
+        ptest = Particles(p0c=1, x=x_test.copy(), y=y_test.copy(), device=tr.device)
+        flags = tr.track_flags
+        old = flags.XS_FLAG_IGNORE_GLOBAL_APERTURE
+        flags.XS_FLAG_IGNORE_GLOBAL_APERTURE = True
+        try:
+            tr._track(ptest, ele_start=i_start, ele_stop=i_stop, backtrack=backtrack,
+                      _force_no_end_turn_actions=True)
+        finally:
+            flags.XS_FLAG_IGNORE_GLOBAL_APERTURE = old
+        pid = ptest.particle_id.cpu().numpy()
+        state = ptest.state.cpu().numpy()[np.argsort(pid)]
+        state_mat = state.reshape(RR.shape)
+        i_r_aper = np.argmin(state_mat > 0, axis=1)
+        rmin_theta = r_vect[i_r_aper - 1]
+        rmin, rmax = 0.0, 2 * step
+        step = dr
+    x_mat = x_test.reshape(RR.shape)
+    y_mat = y_test.reshape(RR.shape)
+    xv = np.array([x_mat[k, i_r_aper[k]] for k in range(n_theta)])
+    yv = np.array([y_mat[k, i_r_aper[k]] for k in range(n_theta)])
+    temp = _convex_hull_polygon(xv, yv)
+    r_out = 1.0
+    res = temp.impact_point_and_normal(x_in=0 * theta, y_in=0 * theta, z_in=0 * theta,
+                                       x_out=r_out * np.cos(theta), y_out=r_out * np.sin(theta),
+                                       z_out=0 * theta)
+    return el.LimitPolygon(x_vertices=res[0], y_vertices=res[1]), index_start_thin
+
+
+def interp_aperture_using_polygons(line, i_aper_0, i_aper_1, n_theta, r_max, dr, ds, s_elements):
+    """loss_location_refinement.py:419-463."""
+    polygon_1, i_start_thin_1 = characterize_aperture(line, i_aper_1, n_theta, r_max, dr,
+                                                      coming_from="upstream")
+    polygon_0, i_end_thin_0 = characterize_aperture(line, i_aper_0, n_theta, r_max, dr,
+                                                    coming_from="downstream")
+    s0, s1, s_vect = interp_aperture_locations(s_elements, i_aper_0, i_aper_1, ds)
+    delta_s = s1 - s0
+    interp = []
+    for ss in s_vect:
+        xn = polygon_1.x_vertices * (ss - s0) / delta_s + polygon_0.x_vertices * (s1 - ss) / delta_s
+        yn = polygon_1.y_vertices * (ss - s0) / delta_s + polygon_0.y_vertices * (s1 - ss) / delta_s
+        interp.append(_convex_hull_polygon(xn, yn))
+    interp_line = build_interp_line(line, i_end_thin_0, i_start_thin_1, s0, s_vect, None,
+                                    aper_0=polygon_0, aper_1=polygon_1, aper_interp=interp)
+    return interp_line, i_end_thin_0, i_start_thin_1, s0, s1
+
+
 class LossLocationRefinement:
     """Refines the loss location of particles lost at apertures of ``line``
     (loss_location_refinement.py:29-108). ``ds``: spacing of the inserted
-    apertures [m]. ``n_theta``, ``r_max`` and ``dr`` belong to the polygon
-    mode, which is not built; they are accepted and ignored."""
+    apertures [m]. ``n_theta`` (rays), ``r_max`` and ``dr`` [m] set the
+    characterisation of differing apertures (polygon mode)."""
 
     def __init__(self, line, backtrack_line=None, n_theta=None, r_max=None, dr=None, ds=None,
                  save_refine_lines=False, allowed_backtrack_types=()):
@@ -226,13 +328,18 @@ class LossLocationRefinement:
                 continue
             a0 = self.line[self.line.element_names[i_aper_0]]
             a1 = self.line[self.line.element_names[i_aper_1]]
-            if not apertures_are_identical(a0, a1):
-                raise NotImplementedError(
-                    f"apertures {i_aper_0} and {i_aper_1} differ: the polygon interpolation "
-                    "mode is not built")
-            i_start_thin_1 = find_adjacent_thick(self.line, i_aper_1, "upstream") + 1
-            i_end_thin_0 = find_adjacent_thick(self.line, i_aper_0, "downstream") - 1
-            interp = build_interp_line(self.line, i_end_thin_0, i_start_thin_1, s0, s_vect, a1)
+            if apertures_are_identical(a0, a1):
+                i_start_thin_1 = find_adjacent_thick(self.line, i_aper_1, "upstream") + 1
+                i_end_thin_0 = find_adjacent_thick(self.line, i_aper_0, "downstream") - 1
+                interp = build_interp_line(self.line, i_end_thin_0, i_start_thin_1, s0, s_vect,
+                                           a1)
+            else:
+                if self.n_theta is None or self.r_max is None or self.dr is None:
+                    raise ValueError("apertures differ: n_theta, r_max and dr are needed for "
+                                     "the polygon interpolation")
+                interp, i_end_thin_0, i_start_thin_1, s0, s1 = interp_aperture_using_polygons(
+                    self.line, i_aper_0, i_aper_1, self.n_theta, self.r_max, self.dr, self.ds,
+                    self._s)
             self._refine_single(particles, mask, i_aper_1, i_end_thin_0, interp)
             if self.save_refine_lines:
                 interp.i_start_thin_0 = i_end_thin_0

@@ -47,7 +47,7 @@ class _MonitorElement:
         # every descriptor handed out stays alive with the element: records
         # built earlier keep pointing at valid memory
         self.__dict__.setdefault("_descs", []).append(desc)
-        rec["monitor"] = ctypes.addressof(desc)
+        rec["aux"] = ctypes.addressof(desc)
         return rec
 
     def copy(self):

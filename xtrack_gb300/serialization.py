@@ -24,10 +24,11 @@ from . import elements as el
 _NEUTRAL = {
     "radiation_flag": 0, "delta_taper": 0.0, "hyl": 0.0, "lag_taper": 0.0, "phase_taper": 0.0,
     "shift_x": 0.0, "shift_y": 0.0, "shift_s": 0.0, "rot_x_rad": 0.0, "rot_y_rad": 0.0,
-    "rot_s_rad": 0.0, "rot_s_rad_no_frame": 0.0, "rot_shift_anchor": 0.0,
+    "rot_s_rad": 0.0, "rot_s_rad_no_frame": 0.0, "rot_shift_anchor": 0.0, "resc_fac": 1.0,
 }
 # derived fields that are recomputed, not read
-_DERIVED = {"inv_factorial_order", "h", "k0_from_h", "_isthick", "prototype"}
+_DERIVED = {"inv_factorial_order", "h", "k0_from_h", "_isthick", "prototype", "x_normal",
+            "y_normal", "svg"}
 
 _MAGNET_KEYS = ("knl", "ksl", "order", "knl_rel", "ksl_rel", "model", "integrator",
                 "num_multipole_kicks")
@@ -51,6 +52,7 @@ _ACCEPT = {
                "num_kicks", "model", "integrator"),
     "LimitEllipse": ("a_squ", "b_squ", "a_b_squ", "a", "b"),
     "LimitRect": ("min_x", "max_x", "min_y", "max_y"),
+    "LimitPolygon": ("x_vertices", "y_vertices"),
 }
 
 
@@ -116,6 +118,9 @@ def element_to_dict(e):
         return out
     if isinstance(e, el.LimitRect):
         out.update(min_x=e.min_x, max_x=e.max_x, min_y=e.min_y, max_y=e.max_y)
+        return out
+    if isinstance(e, el.LimitPolygon):
+        out.update(x_vertices=e.x_vertices.tolist(), y_vertices=e.y_vertices.tolist())
         return out
     # magnets
     out.update(knl=e.knl.tolist(), ksl=e.ksl.tolist(), order=e.order,
