@@ -343,13 +343,18 @@ def run_da_screen(args):
         return rng.integers(mean // 2, mean * 3 // 2 + 1, size=n)
 
     def features(scan):
-        # coordinates, the seed's multipole-error summary and its linear
-        # tunes (the tunes set the resonances that bound the DA; the error
-        # RMS over hundreds of magnets barely differs between seeds)
+        # coordinates, the seed's multipole-error summary, its linear tunes
+        # and the extremes of its closed orbit around the ring (in mm): the
+        # orbit eats into the aperture, which bounds the DA on this ring,
+        # and the error RMS over hundreds of magnets barely differs
+        # between seeds
         d = scan.deltas[scan.delta_index]
-        return np.concatenate([sg.coord_features(scan.r, scan.theta, d),
-                               scan.seed_features[scan.lattice_index],
-                               scan.tunes[scan.lattice_index][:, :2]], axis=1)
+        li = scan.lattice_index
+        parts = [sg.coord_features(scan.r, scan.theta, d), scan.tunes[li][:, :2],
+                 1e3 * scan.co_extremes[li]]
+        if args.da_features == "all":
+            parts.append(scan.seed_features[li])
+        return np.concatenate(parts, axis=1)
 
     train_lines = [workloads.thick_ring(seed=100 + s) for s in range(args.da_train_seeds)]
     test_lines = [workloads.thick_ring(seed=200 + s) for s in range(args.da_test_seeds)]
@@ -370,9 +375,11 @@ def run_da_screen(args):
     st, at, _ = sc.run_scan(bt_train, s_train, turns, device=dev)
     t_train_scan = time.perf_counter() - t0
     surv, lt = sg.targets(st, at, turns)
-    net = sg.SurvivalMLP(n_in=sg.N_COORD_FEATURES + sg.N_SEED_FEATURES + 2, seed=0, device=dev)
+    n_in = sg.N_COORD_FEATURES + 6 + (sg.N_SEED_FEATURES if args.da_features == "all" else 0)
+    net = sg.SurvivalMLP(n_in=n_in, seed=0, device=dev)
     t0 = time.perf_counter()
-    hist = net.fit(features(s_train), surv, lt, epochs=args.da_epochs, batch=4096, lr=3e-3)
+    hist = net.fit(features(s_train), surv, lt, epochs=args.da_epochs, batch=4096, lr=3e-3,
+                   weight_decay=args.da_weight_decay)
     torch.cuda.synchronize(dev)
     t_fit = time.perf_counter() - t0
 
@@ -387,12 +394,17 @@ def run_da_screen(args):
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
     p, _ = net.predict(features(s_test))
-    track, audit = sg.screen(p, args.da_lo, args.da_hi, 0.02, seed=1)
+    # rays of the scan: seed x momentum offset x angle
+    angles = np.unique(s_test.theta)
+    ray = ((s_test.lattice_index.astype(np.int64) * len(s_test.deltas) + s_test.delta_index)
+           * len(angles) + np.searchsorted(angles, s_test.theta))
+    track, audit = sg.screen_rays(p, s_test.r, ray, args.da_lo, args.da_hi, 0.02, seed=1)
     st_s, at_s, _ = sc.run_scan(bt_test, s_test, turns, select=track, device=dev)
     torch.cuda.synchronize(dev)
     t_screen = time.perf_counter() - t0
     surv_tracked = sg.targets(st_s, at_s, turns)[0] > 0
-    surv_screen = sg.screened_outcome(p, track, surv_tracked, hi=args.da_hi)
+    surv_screen = sg.ray_outcome(p, s_test.r, ray, track, surv_tracked, hi=args.da_hi,
+                                 audit_mask=audit)
 
     n_seeds = len(test_lines)
     da_plain = sc.da_table(s_test, surv_plain, n_seeds)
@@ -412,6 +424,7 @@ def run_da_screen(args):
                       "test_seeds": n_seeds, "train_particles": int(s_train.n),
                       "test_particles": int(s_test.n), "radial_step_sigma": grid_step,
                       "arith": args.arith},
+           "features": args.da_features, "weight_decay": args.da_weight_decay,
            "plain_s": t_plain, "screened_s": t_screen, "tracked_fraction": float(track.mean()),
            "audit_fraction": float(audit.mean()), "da_error_sigma": da_err,
            "da_plain_mean_sigma": float(da_plain.mean()),
@@ -452,7 +465,7 @@ def main():
                     help="record 6 coordinates per turn of the first N particles")
     ap.add_argument("--workload", default="thick_ring", choices=["thick_ring", "da_screen"])
     ap.add_argument("--da-turns", dest="da_turns", type=int, default=100)
-    ap.add_argument("--da-train-particles", dest="da_train_particles", type=int, default=50000)
+    ap.add_argument("--da-train-particles", dest="da_train_particles", type=int, default=16000)
     ap.add_argument("--da-lo", dest="da_lo", type=float, default=0.02)
     ap.add_argument("--da-hi", dest="da_hi", type=float, default=0.98)
     ap.add_argument("--da-rmax", dest="da_rmax", type=float, default=80.0,
@@ -460,9 +473,13 @@ def main():
                          "keeps everything within 20 sigma, its DA lies near the aperture")
     ap.add_argument("--da-particles", dest="da_particles", type=int, default=100000,
                     help="mean particles per seed (uniform in [n/2, 3n/2])")
-    ap.add_argument("--da-train-seeds", dest="da_train_seeds", type=int, default=6)
+    ap.add_argument("--da-train-seeds", dest="da_train_seeds", type=int, default=24)
     ap.add_argument("--da-test-seeds", dest="da_test_seeds", type=int, default=4)
     ap.add_argument("--da-epochs", dest="da_epochs", type=int, default=40)
+    ap.add_argument("--da-features", dest="da_features", default="all", choices=["all", "physics"],
+                    help="all: coordinates, tunes, orbit extremes and the 32 multipole-error "
+                         "statistics; physics: without the error statistics")
+    ap.add_argument("--da-weight-decay", dest="da_weight_decay", type=float, default=0.0)
     args = ap.parse_args()
     if args.workload == "da_screen":
         run_da_screen(args)

@@ -171,3 +171,21 @@ def test_training_learns_a_stability_boundary():
     assert acc >= 0.95, acc
     track, _ = sg.screen(p, audit=0.0)
     assert track.mean() < 0.3
+
+
+def test_ray_screening_band_and_outcome():
+    # two rays; the network is sure up to r = 3, unsure on [3, 5], sure lost after
+    r = np.tile(np.arange(1.0, 9.0), 2)
+    ray = np.repeat([0, 1], 8)
+    p = np.tile([1.0, 1.0, 0.99, 0.5, 0.3, 0.01, 0.0, 0.0], 2)
+    track, audit = sg.screen_rays(p, r, ray, lo=0.02, hi=0.98, audit=0.0)
+    assert track.tolist() == [False, False, False, True, True, True, False, False] * 2
+    truth = np.tile([True, True, True, True, False, False, False, False], 2)
+    out = sg.ray_outcome(p, r, ray, track, truth[track], hi=0.98)
+    assert np.array_equal(out, truth)
+    # an audited particle below the band does not move the band
+    aud = np.zeros_like(track)
+    aud[0] = True
+    t2 = track | aud
+    out2 = sg.ray_outcome(p, r, ray, t2, truth[t2], hi=0.98, audit_mask=aud)
+    assert np.array_equal(out2, truth)

@@ -1025,14 +1025,16 @@ static int32_t run_rounds(ExecCtx* C, TrackArgs a, const int32_t* lat, int64_t c
     if (C->tune.use_graph && full > 1) {
         // capture one round on a side stream and replay it `full` times
         cudaStream_t cs = nullptr;
-        cudaEvent_t ev = nullptr;
         cudaGraph_t g = nullptr;
         cudaGraphExec_t ex = nullptr;
         XTG_CUDA_CHECK(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
-        XTG_CUDA_CHECK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
-        XTG_CUDA_CHECK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+        cudaError_t ce = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+        if (ce != cudaSuccess) {
+            cudaStreamDestroy(cs);
+            return set_error(XTG_E_CUDA, "graph capture failed: %s", cudaGetErrorString(ce));
+        }
         st = launch_round<kExact>(C, a, lat, cap, block, grid, smem, cs);
-        cudaError_t ce = cudaStreamEndCapture(cs, &g);
+        ce = cudaStreamEndCapture(cs, &g);
         if (st == XTG_OK && ce == cudaSuccess) ce = cudaGraphInstantiate(&ex, g, 0);
         if (g) cudaGraphDestroy(g);
         if (st == XTG_OK && ce == cudaSuccess) {
@@ -1044,7 +1046,6 @@ static int32_t run_rounds(ExecCtx* C, TrackArgs a, const int32_t* lat, int64_t c
         }
         if (ex) cudaGraphExecDestroy(ex);
         cudaStreamDestroy(cs);
-        cudaEventDestroy(ev);
         if (st != XTG_OK) return st;
         if (ce != cudaSuccess) return set_error(XTG_E_CUDA, "graph replay failed: %s", cudaGetErrorString(ce));
     } else {

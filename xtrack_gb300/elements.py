@@ -572,7 +572,9 @@ class LimitPolygon(BeamElement):
                 wx, wy = xc[i] - x_in[k], yc[i] - y_in[k]
                 t = (wx * ey[i] - wy * ex[i]) / den      # along the segment
                 u = (wx * dy - wy * dx) / den            # along the edge
-                if 0 <= t <= 1 and 0 <= u <= 1 and t < best:
+                # rays through a vertex hit both neighbouring edges at
+                # their ends: accept the end points within rounding
+                if -1e-12 <= t <= 1 + 1e-12 and -1e-12 <= u <= 1 + 1e-12 and t < best:
                     best = t
                     found[k] = i
             if found[k] >= 0:

@@ -28,6 +28,7 @@ class Scan:
         self.deltas = None
         self.seed_features = None  # (n_seeds, k)
         self.tunes = None
+        self.co_extremes = None   # (n_seeds, 4): max x, min x, max y, min y of the orbit
 
     @property
     def n(self):
@@ -40,6 +41,19 @@ def seed_normal_form(tracker, particle_ref_kwargs, device="cuda"):
     R, _ = da.one_turn_matrix(fn, co)
     W, tunes = da.linear_normal_form(R)
     return co, W, tunes
+
+
+def closed_orbit_extremes(tracker, co, particle_ref_kwargs, device="cuda"):
+    """Largest and smallest x and y of the closed orbit over the ring's
+    elements [m], from one element-by-element turn of the closed-orbit
+    particle (ONE_TURN_EBE monitor)."""
+    p = Particles(device=device, x=[co[0]], px=[co[1]], y=[co[2]], py=[co[3]], zeta=[co[4]],
+                  delta=[co[5]], **particle_ref_kwargs)
+    tracker._track(p, num_turns=1, turn_by_turn_monitor="ONE_TURN_EBE")
+    mon = tracker.record_last_track
+    x = np.asarray(mon.x).ravel()
+    y = np.asarray(mon.y).ravel()
+    return np.array([x.max(), x.min(), y.max(), y.min()])
 
 
 def build_scan(lines, counts, r_max=20.0, n_angles=11, deltas=(0.0, 2.7e-4), nemitt=2.5e-6,
@@ -56,10 +70,12 @@ def build_scan(lines, counts, r_max=20.0, n_angles=11, deltas=(0.0, 2.7e-4), nem
     out.deltas = np.asarray(deltas, dtype=np.float64)
     parts = {k: [] for k in ("coords", "lat", "r", "theta", "di")}
     tunes = []
+    co_ext = []
     for s, line in enumerate(lines):
         tr = line.build_tracker(device=device, arith=arith)
         co, W, q = seed_normal_form(tr, ref_kw, device=device)
         tunes.append(q)
+        co_ext.append(closed_orbit_extremes(tr, co, ref_kw, device=device))
         n_rays = n_angles * len(deltas)
         per_ray = max(1, int(counts[s]) // n_rays)
         r = np.tile(np.linspace(r_max / per_ray, r_max, per_ray), n_rays)
@@ -79,6 +95,7 @@ def build_scan(lines, counts, r_max=20.0, n_angles=11, deltas=(0.0, 2.7e-4), nem
     out.theta = np.concatenate(parts["theta"])
     out.delta_index = np.concatenate(parts["di"])
     out.tunes = np.array(tunes)
+    out.co_extremes = np.array(co_ext)
     out.ref_kw = ref_kw
     if features is not None:
         out.seed_features = np.stack([features(line) for line in lines])

@@ -10,11 +10,13 @@ accumulation for forward and backward passes, a fixed-order bias-gradient
 reduction and an Adam step on FP32 master weights (include/xtrack_gb300.h,
 ``xtg_mlp_*``). Torch only holds the device memory.
 
-``screened_scan`` then tracks only the particles the network is unsure
-about (P(survive) between two thresholds) plus a random audit fraction and
-takes the network's answer for the rest; plain tracking of every particle
-stays the reference the screened result is judged against (DA error in
-beam sigma, misclassification rate on the audit).
+``screen`` then tracks only the particles the network is unsure about
+(P(survive) between two thresholds) plus a random audit fraction and takes
+the network's answer for the rest; ``screen_rays`` does the same per ray
+of a DA scan, tracking the band from the first uncertain amplitude to the
+first confidently lost one. Plain tracking of every particle stays the
+reference the screened result is judged against (DA error in beam sigma,
+misclassification rate on the audit).
 
 No reference counterpart: xtrack has no learned component.
 """
@@ -164,7 +166,8 @@ class SurvivalMLP:
                 self.b[l].numel(), lr, beta1, beta2, eps, 0.0, self.step_count, st), self._lib)
 
     # ------------------------------------------------------------------
-    def fit(self, X, survive, logturn, epochs=10, batch=4096, lr=1e-3, seed=0, lr_final=None):
+    def fit(self, X, survive, logturn, epochs=10, batch=4096, lr=1e-3, seed=0, lr_final=None,
+            weight_decay=0.0):
         """Adam training on (X, survive, logturn); returns the mean loss of
         each epoch. ``lr`` decays linearly to ``lr_final`` (default lr/10)."""
         X = torch.as_tensor(X, dtype=torch.float32, device=self.device)
@@ -189,7 +192,7 @@ class SurvivalMLP:
                                                         t.index_select(0, idx).contiguous())
                 self.backward(dout, dout16)
                 cur = lr + (lr_final - lr) * k / max(1, steps_total - 1)
-                self.adam_step(lr=cur)
+                self.adam_step(lr=cur, weight_decay=weight_decay)
                 tot += loss.double().sum()
                 k += 1
             hist.append(float(tot.item()) / n)
@@ -257,6 +260,58 @@ def screen(p_survive, lo=0.05, hi=0.95, audit=0.02, seed=0):
     rng = np.random.default_rng(seed)
     aud = (~unsure) & (rng.random(p.shape) < audit)
     return unsure | aud, aud
+
+
+def screen_rays(p_survive, r, ray_id, lo=0.05, hi=0.95, audit=0.02, seed=0):
+    """Boolean masks (track, audit) for a DA scan on rays: on each ray the
+    particles from the first amplitude the network is unsure about
+    (P < hi) up to the first amplitude it calls lost (P <= lo) are
+    tracked; below that band the particles are taken to survive, above it
+    to be lost (they cannot change the ray's DA, the smallest lost
+    amplitude), plus a random ``audit`` fraction of the rest."""
+    p = np.asarray(p_survive)
+    r = np.asarray(r)
+    ray_id = np.asarray(ray_id)
+    track = np.zeros(p.shape, dtype=bool)
+    order = np.lexsort((r, ray_id))
+    rid = ray_id[order]
+    starts = np.flatnonzero(np.r_[True, rid[1:] != rid[:-1]])
+    ends = np.r_[starts[1:], len(order)]
+    for a, b in zip(starts, ends):
+        idx = order[a:b]
+        pr = p[idx]
+        unsure = np.flatnonzero(pr < hi)
+        if unsure.size == 0:
+            continue
+        first = unsure[0]
+        lost = np.flatnonzero(pr[first:] <= lo)
+        last = first + lost[0] if lost.size else len(idx) - 1
+        track[idx[first:last + 1]] = True
+    rng = np.random.default_rng(seed)
+    aud = (~track) & (rng.random(p.shape) < audit)
+    return track | aud, aud
+
+
+def ray_outcome(p_survive, r, ray_id, tracked_mask, tracked_survive, hi=0.95, audit_mask=None):
+    """Survival map of a ray-screened scan: tracked particles their tracked
+    outcome; untracked ones below their ray's tracked band survive, above
+    it are lost (audited particles are tracked but not part of the band)."""
+    p = np.asarray(p_survive)
+    r = np.asarray(r)
+    ray_id = np.asarray(ray_id)
+    out = np.zeros(p.shape, dtype=bool)
+    out[tracked_mask] = np.asarray(tracked_survive, dtype=bool)
+    in_band = tracked_mask if audit_mask is None else tracked_mask & ~np.asarray(audit_mask)
+    for rid in np.unique(ray_id):
+        on = ray_id == rid
+        band = on & in_band
+        untracked = on & ~tracked_mask
+        if band.any():
+            r_band_lo = r[band].min()
+            out[untracked] = r[untracked] < r_band_lo
+        else:
+            out[untracked] = p[untracked] >= hi
+    return out
 
 
 def screened_outcome(p_survive, tracked_mask, tracked_survive, hi=0.95):
