@@ -144,8 +144,12 @@ def run_reference(args):
     out = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": "thick ring 6993 elements, 1e6 protons 7 TeV (CPU sample)",
-                      "particles": base["sample"]},
+           "config": {"workload": "thick LHC-like ring, 8x23 FODO cells, 6993 elements, "
+                                  f"{args.particles:.3g} protons 7 TeV, 1 turn per step",
+                      "particles_per_gpu": args.particles, "elements": 6993,
+                      "turns_per_step": 1,
+                      "sample": "each step times a bounded sample of the beam on the host "
+                                "cores: " + base["sample"]},
            "cpu_baseline": base,
            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
@@ -390,26 +394,35 @@ def run_da_screen(args):
     t_plain = time.perf_counter() - t0
     surv_plain = sg.targets(st_p, at_p, turns)[0] > 0
 
-    # screened scan
-    torch.cuda.synchronize(dev)
-    t0 = time.perf_counter()
-    p, _ = net.predict(features(s_test))
-    # rays of the scan: seed x momentum offset x angle
-    angles = np.unique(s_test.theta)
-    ray = ((s_test.lattice_index.astype(np.int64) * len(s_test.deltas) + s_test.delta_index)
-           * len(angles) + np.searchsorted(angles, s_test.theta))
-    track, audit = sg.screen_rays(p, s_test.r, ray, args.da_lo, args.da_hi, 0.02, seed=1)
-    st_s, at_s, _ = sc.run_scan(bt_test, s_test, turns, select=track, device=dev)
-    torch.cuda.synchronize(dev)
-    t_screen = time.perf_counter() - t0
-    surv_tracked = sg.targets(st_s, at_s, turns)[0] > 0
-    surv_screen = sg.ray_outcome(p, s_test.r, ray, track, surv_tracked, hi=args.da_hi,
-                                 audit_mask=audit)
-
     n_seeds = len(test_lines)
     da_plain = sc.da_table(s_test, surv_plain, n_seeds)
-    da_screen = sc.da_table(s_test, surv_screen, n_seeds)
-    da_err = float(np.max(np.abs(da_screen - da_plain)))
+    angles = np.unique(s_test.theta)
+    # rays of the scan: seed x momentum offset x angle
+    ray = ((s_test.lattice_index.astype(np.int64) * len(s_test.deltas) + s_test.delta_index)
+           * len(angles) + np.searchsorted(angles, s_test.theta))
+
+    def screened(lo, hi):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        p, _ = net.predict(features(s_test))
+        track, audit = sg.screen_rays(p, s_test.r, ray, lo, hi, 0.02, seed=1)
+        st_s, at_s, _ = sc.run_scan(bt_test, s_test, turns, select=track, device=dev)
+        torch.cuda.synchronize(dev)
+        t = time.perf_counter() - t0
+        surv_tracked = sg.targets(st_s, at_s, turns)[0] > 0
+        surv_screen = sg.ray_outcome(p, s_test.r, ray, track, surv_tracked, hi=hi,
+                                     audit_mask=audit)
+        err = np.abs(sc.da_table(s_test, surv_screen, n_seeds) - da_plain)
+        return p, track, audit, t, err
+
+    sweep = []
+    for lo, hi in args.da_bands:
+        _, tr_, _, t_, err_ = screened(lo, hi)
+        sweep.append({"band": [lo, hi], "speedup": t_plain / t_, "tracked_fraction": float(tr_.mean()),
+                      "da_error_max_sigma": float(err_.max()), "da_error_mean_sigma": float(err_.mean()),
+                      "da_error_median_sigma": float(np.median(err_))})
+    p, track, audit, t_screen, err = screened(args.da_lo, args.da_hi)
+    da_err = float(err.max())
     aud_idx = np.nonzero(audit)[0]
     mis = float(np.mean((p[aud_idx] >= 0.5) != surv_plain[aud_idx])) if aud_idx.size else None
     all_mis = float(np.mean((p >= 0.5) != surv_plain))
@@ -427,6 +440,8 @@ def run_da_screen(args):
            "features": args.da_features, "weight_decay": args.da_weight_decay,
            "plain_s": t_plain, "screened_s": t_screen, "tracked_fraction": float(track.mean()),
            "audit_fraction": float(audit.mean()), "da_error_sigma": da_err,
+           "da_error_mean_sigma": float(err.mean()), "da_error_median_sigma": float(np.median(err)),
+           "band_sweep": sweep,
            "da_plain_mean_sigma": float(da_plain.mean()),
            "audit_misclassification": mis, "misclassification_all": all_mis,
            "train_scan_s": t_train_scan, "fit_s": t_fit, "fit_loss": [hist[0], hist[-1]],
@@ -468,6 +483,8 @@ def main():
     ap.add_argument("--da-train-particles", dest="da_train_particles", type=int, default=16000)
     ap.add_argument("--da-lo", dest="da_lo", type=float, default=0.02)
     ap.add_argument("--da-hi", dest="da_hi", type=float, default=0.98)
+    ap.add_argument("--da-bands", dest="da_bands", default="0.005:0.995,0.001:0.999",
+                    help="extra (lo:hi) screening bands to time, comma separated")
     ap.add_argument("--da-rmax", dest="da_rmax", type=float, default=80.0,
                     help="largest amplitude of the grid (sigma); the synthetic ring at 7 TeV "
                          "keeps everything within 20 sigma, its DA lies near the aperture")
@@ -476,11 +493,13 @@ def main():
     ap.add_argument("--da-train-seeds", dest="da_train_seeds", type=int, default=24)
     ap.add_argument("--da-test-seeds", dest="da_test_seeds", type=int, default=4)
     ap.add_argument("--da-epochs", dest="da_epochs", type=int, default=40)
-    ap.add_argument("--da-features", dest="da_features", default="all", choices=["all", "physics"],
+    ap.add_argument("--da-features", dest="da_features", default="physics",
+                    choices=["all", "physics"],
                     help="all: coordinates, tunes, orbit extremes and the 32 multipole-error "
                          "statistics; physics: without the error statistics")
     ap.add_argument("--da-weight-decay", dest="da_weight_decay", type=float, default=0.0)
     args = ap.parse_args()
+    args.da_bands = [tuple(float(v) for v in b.split(":")) for b in args.da_bands.split(",") if b]
     if args.workload == "da_screen":
         run_da_screen(args)
     elif args.impl == "reference":
