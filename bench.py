@@ -320,15 +320,18 @@ def _tuning_args(args):
 
 
 def run_da_screen(args):
-    """DA-scan time, surrogate-screened vs plain: a scaled-down learned
-    screening study on the thick ring. Seeds of the ring are scanned on a
-    polar grid (11 angles x 2 momentum offsets x amplitudes up to 20 sigma)
-    with all seeds in one persistent launch; a survival MLP is trained on
-    the training seeds' outcomes with the library's kernels, then the test
-    seeds are scanned twice: plainly (every particle tracked) and screened
-    (only 0.05 < P(survive) < 0.95 plus a 2 % audit tracked). value = plain
-    time / screened time; the DA error (sigma) and the audit's
-    misclassification rate judge the screened result against the plain one."""
+    """DA-scan time, screened vs plain, on seeds of the thick ring. The
+    seeds are scanned on a polar grid (11 angles x 2 momentum offsets x
+    amplitudes up to --da-rmax sigma) with all seeds in one persistent
+    launch. A survival MLP is trained with the library's kernels on the
+    training seeds' outcomes (features: coordinates, the seed's tunes,
+    closed-orbit extremes and the ray's linear aperture). The test seeds are
+    then scanned plainly (every particle tracked) and screened three ways:
+    the network's uncertain band alone (one pass); sentinels every
+    --da-stride amplitudes plus that band, then each ray's bracket (two
+    passes); the same two passes without the network. value = plain time /
+    time of the two-pass scan with the network. The DA error per ray (sigma)
+    judges each screened result against the plain one."""
     import torch
     from xtrack_gb300 import scan as sc
     from xtrack_gb300 import surrogate as sg
@@ -347,18 +350,10 @@ def run_da_screen(args):
         return rng.integers(mean // 2, mean * 3 // 2 + 1, size=n)
 
     def features(scan):
-        # coordinates, the seed's multipole-error summary, its linear tunes
-        # and the extremes of its closed orbit around the ring (in mm): the
-        # orbit eats into the aperture, which bounds the DA on this ring,
-        # and the error RMS over hundreds of magnets barely differs
-        # between seeds
-        d = scan.deltas[scan.delta_index]
-        li = scan.lattice_index
-        parts = [sg.coord_features(scan.r, scan.theta, d), scan.tunes[li][:, :2],
-                 1e3 * scan.co_extremes[li]]
+        f = sg.da_features(scan)
         if args.da_features == "all":
-            parts.append(scan.seed_features[li])
-        return np.concatenate(parts, axis=1)
+            f = np.concatenate([f, scan.seed_features[scan.lattice_index]], axis=1)
+        return f
 
     train_lines = [workloads.thick_ring(seed=100 + s) for s in range(args.da_train_seeds)]
     test_lines = [workloads.thick_ring(seed=200 + s) for s in range(args.da_test_seeds)]
@@ -370,16 +365,17 @@ def run_da_screen(args):
     t_setup = time.perf_counter() - t0
     bt_train = BatchTracker(train_lines, device=dev, arith=args.arith)
     bt_test = BatchTracker(test_lines, device=dev, arith=args.arith)
-    # small blocks keep a screened (small) particle set spread over the SMs
+    # one-warp blocks spread a small (screened) particle set over every SM
+    # sub-partition; 12 KB chunks keep eight of them resident per SM
     for bt in (bt_train, bt_test):
-        bt.set_tuning(compact_every=max(1, turns // 10), block_size=64, chunk_bytes=16384)
+        bt.set_tuning(compact_every=max(1, turns // 10), block_size=32, chunk_bytes=12288)
 
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
     st, at, _ = sc.run_scan(bt_train, s_train, turns, device=dev)
     t_train_scan = time.perf_counter() - t0
     surv, lt = sg.targets(st, at, turns)
-    n_in = sg.N_COORD_FEATURES + 6 + (sg.N_SEED_FEATURES if args.da_features == "all" else 0)
+    n_in = sg.N_DA_FEATURES + (sg.N_SEED_FEATURES if args.da_features == "all" else 0)
     net = sg.SurvivalMLP(n_in=n_in, seed=0, device=dev)
     t0 = time.perf_counter()
     hist = net.fit(features(s_train), surv, lt, epochs=args.da_epochs, batch=4096, lr=3e-3,
@@ -393,57 +389,74 @@ def run_da_screen(args):
     st_p, at_p, _ = sc.run_scan(bt_test, s_test, turns, device=dev)
     t_plain = time.perf_counter() - t0
     surv_plain = sg.targets(st_p, at_p, turns)[0] > 0
-
     n_seeds = len(test_lines)
     da_plain = sc.da_table(s_test, surv_plain, n_seeds)
-    angles = np.unique(s_test.theta)
-    # rays of the scan: seed x momentum offset x angle
-    ray = ((s_test.lattice_index.astype(np.int64) * len(s_test.deltas) + s_test.delta_index)
-           * len(angles) + np.searchsorted(angles, s_test.theta))
+    ray = s_test.ray_index()
 
-    def screened(lo, hi):
-        torch.cuda.synchronize(dev)
-        t0 = time.perf_counter()
+    def stats(da, seconds, tracked):
+        err = np.abs(da - da_plain)
+        return {"seconds": seconds, "speedup": t_plain / seconds,
+                "tracked_fraction": float(tracked.mean()),
+                "da_error_max_sigma": float(err.max()), "da_error_mean_sigma": float(err.mean()),
+                "da_error_median_sigma": float(np.median(err)),
+                "rays_exact": float(np.mean(err == 0.0))}
+
+    def predict():
         p, _ = net.predict(features(s_test))
-        track, audit = sg.screen_rays(p, s_test.r, ray, lo, hi, 0.02, seed=1)
-        st_s, at_s, _ = sc.run_scan(bt_test, s_test, turns, select=track, device=dev)
-        torch.cuda.synchronize(dev)
-        t = time.perf_counter() - t0
-        surv_tracked = sg.targets(st_s, at_s, turns)[0] > 0
-        surv_screen = sg.ray_outcome(p, s_test.r, ray, track, surv_tracked, hi=hi,
-                                     audit_mask=audit)
-        err = np.abs(sc.da_table(s_test, surv_screen, n_seeds) - da_plain)
-        return p, track, audit, t, err
+        return p
 
-    sweep = []
-    for lo, hi in args.da_bands:
-        _, tr_, _, t_, err_ = screened(lo, hi)
-        sweep.append({"band": [lo, hi], "speedup": t_plain / t_, "tracked_fraction": float(tr_.mean()),
-                      "da_error_max_sigma": float(err_.max()), "da_error_mean_sigma": float(err_.mean()),
-                      "da_error_median_sigma": float(np.median(err_))})
-    p, track, audit, t_screen, err = screened(args.da_lo, args.da_hi)
-    da_err = float(err.max())
-    aud_idx = np.nonzero(audit)[0]
-    mis = float(np.mean((p[aud_idx] >= 0.5) != surv_plain[aud_idx])) if aud_idx.size else None
-    all_mis = float(np.mean((p >= 0.5) != surv_plain))
+    # (1) the network's band alone, one pass
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    p = predict()
+    track, audit = sg.screen_rays(p, s_test.r, ray, args.da_lo, args.da_hi, 0.0)
+    st_s, at_s, _ = sc.run_scan(bt_test, s_test, turns, select=track, device=dev)
+    t_band = time.perf_counter() - t0
+    surv_band = sg.ray_outcome(p, s_test.r, ray, track, sg.targets(st_s, at_s, turns)[0] > 0,
+                               hi=args.da_hi, audit_mask=audit)
+    band = stats(sc.da_table(s_test, surv_band, n_seeds), t_band, track)
+
+    # (2) sentinels + band, then brackets
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    p = predict()
+    res = sc.screened_da_scan(bt_test, s_test, turns, p_survive=p, stride=args.da_stride,
+                              lo=args.da_lo, hi=args.da_hi, device=dev)
+    t_net = time.perf_counter() - t0
+    two_pass = stats(res.da, t_net, res.tracked)
+    two_pass["pass_seconds"] = res.seconds
+    two_pass["pass_fractions"] = [float(res.pass1.mean()), float(res.pass2.mean())]
+
+    # (3) the same without the network
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    res0 = sc.screened_da_scan(bt_test, s_test, turns, p_survive=None, stride=args.da_stride,
+                               device=dev)
+    t_nonet = time.perf_counter() - t0
+    no_net = stats(res0.da, t_nonet, res0.tracked)
+    no_net["pass_seconds"] = res0.seconds
+    no_net["pass_fractions"] = [float(res0.pass1.mean()), float(res0.pass2.mean())]
+
     grid_step = float(np.max(np.diff(np.unique(s_test.r))))
-    out = {"metric": "DA-scan time, surrogate vs plain", "value": t_plain / t_screen,
+    out = {"metric": "DA-scan time, surrogate vs plain", "value": t_plain / t_net,
            "unit": "x (plain time / screened time)", "higher_is_better": True, "n_gpus": 1,
            "dtype": "f64 tracking, bf16/f32 network", "data": "synthetic",
            "config": {"workload": "thick LHC-like ring seeds (6993 elements), polar grid "
                                   f"0-{args.da_rmax:g} sigma x 11 angles x delta in {{0, 2.7e-4}}",
                       "turns": turns, "screen_band": [args.da_lo, args.da_hi],
-                      "train_seeds": len(train_lines),
-                      "test_seeds": n_seeds, "train_particles": int(s_train.n),
-                      "test_particles": int(s_test.n), "radial_step_sigma": grid_step,
-                      "arith": args.arith},
-           "features": args.da_features, "weight_decay": args.da_weight_decay,
-           "plain_s": t_plain, "screened_s": t_screen, "tracked_fraction": float(track.mean()),
-           "audit_fraction": float(audit.mean()), "da_error_sigma": da_err,
-           "da_error_mean_sigma": float(err.mean()), "da_error_median_sigma": float(np.median(err)),
-           "band_sweep": sweep,
+                      "sentinel_stride": args.da_stride,
+                      "train_seeds": len(train_lines), "test_seeds": n_seeds,
+                      "train_particles": int(s_train.n), "test_particles": int(s_test.n),
+                      "radial_step_sigma": grid_step, "arith": args.arith,
+                      "features": args.da_features},
+           "plain_s": t_plain, "screened_s": t_net,
+           "da_error_sigma": two_pass["da_error_max_sigma"],
+           "da_error_mean_sigma": two_pass["da_error_mean_sigma"],
+           "tracked_fraction": two_pass["tracked_fraction"],
+           "methods": {"learned_band_one_pass": band, "sentinels_band_bracket": two_pass,
+                       "sentinels_bracket_no_network": no_net},
            "da_plain_mean_sigma": float(da_plain.mean()),
-           "audit_misclassification": mis, "misclassification_all": all_mis,
+           "misclassification_all": float(np.mean((p >= 0.5) != surv_plain)),
            "train_scan_s": t_train_scan, "fit_s": t_fit, "fit_loss": [hist[0], hist[-1]],
            "setup_s": t_setup}
     print(json.dumps(out))
@@ -483,23 +496,22 @@ def main():
     ap.add_argument("--da-train-particles", dest="da_train_particles", type=int, default=16000)
     ap.add_argument("--da-lo", dest="da_lo", type=float, default=0.02)
     ap.add_argument("--da-hi", dest="da_hi", type=float, default=0.98)
-    ap.add_argument("--da-bands", dest="da_bands", default="0.005:0.995,0.001:0.999",
-                    help="extra (lo:hi) screening bands to time, comma separated")
+    ap.add_argument("--da-stride", dest="da_stride", type=int, default=34,
+                    help="sentinel spacing of the screened DA scan, in grid amplitudes")
     ap.add_argument("--da-rmax", dest="da_rmax", type=float, default=80.0,
                     help="largest amplitude of the grid (sigma); the synthetic ring at 7 TeV "
                          "keeps everything within 20 sigma, its DA lies near the aperture")
     ap.add_argument("--da-particles", dest="da_particles", type=int, default=100000,
                     help="mean particles per seed (uniform in [n/2, 3n/2])")
     ap.add_argument("--da-train-seeds", dest="da_train_seeds", type=int, default=24)
-    ap.add_argument("--da-test-seeds", dest="da_test_seeds", type=int, default=4)
+    ap.add_argument("--da-test-seeds", dest="da_test_seeds", type=int, default=8)
     ap.add_argument("--da-epochs", dest="da_epochs", type=int, default=40)
     ap.add_argument("--da-features", dest="da_features", default="physics",
                     choices=["all", "physics"],
-                    help="all: coordinates, tunes, orbit extremes and the 32 multipole-error "
-                         "statistics; physics: without the error statistics")
+                    help="physics: coordinates, tunes, orbit extremes and the ray's linear "
+                         "aperture; all: plus the 32 multipole-error statistics")
     ap.add_argument("--da-weight-decay", dest="da_weight_decay", type=float, default=0.0)
     args = ap.parse_args()
-    args.da_bands = [tuple(float(v) for v in b.split(":")) for b in args.da_bands.split(",") if b]
     if args.workload == "da_screen":
         run_da_screen(args)
     elif args.impl == "reference":

@@ -277,7 +277,7 @@ int32_t xtg_track(const xtg_lattice* lattice, const xtg_particles* particles,
  * Allocation-free variant of xtg_track. No reference counterpart: the
  * reference's track_line has no scratch to place. The push's scratch (index
  * list, work queue, counters) lives in one static device array sized for
- * XTG_NOALLOC_MAX_PARTICLES particles (about 4.3 MB per device) instead of
+ * XTG_NOALLOC_MAX_PARTICLES particles (about 4.7 MB per device) instead of
  * the lattice's workspace, so a call makes no cudaMalloc/cudaFree and no
  * framework allocation. Same arguments and results as xtg_track; the
  * element table is read from global memory (the tuning's chunk_bytes and
@@ -322,7 +322,7 @@ int32_t xtg_set_multi_element_monitor(xtg_lattice* lattice,
 
 /* Launch tuning of the push. Results do not depend on it. */
 typedef struct xtg_tuning {
-    int32_t block_size;      /* threads per block: 64, 128 or 256            */
+    int32_t block_size;      /* threads per block: 32, 64, 128 or 256        */
     int32_t compact_every;   /* turns between lost-particle compactions;
                                 0: only at the start of each call            */
     int32_t chunk_bytes;     /* shared-memory chunk of the element table

@@ -39,7 +39,8 @@ def _beam(n, seed, scale):
 
 @pytest.mark.parametrize("arith", ["exact", "fast"])
 @pytest.mark.parametrize("tuning", [{}, {"compact_every": 3, "chunk_bytes": 4096, "use_graph": 1},
-                                    {"chunk_bytes": 0, "block_size": 64}])
+                                    {"chunk_bytes": 0, "block_size": 64},
+                                    {"compact_every": 2, "chunk_bytes": 8192, "block_size": 32}])
 def test_batch_equals_per_seed_trackers(arith, tuning):
     import torch
     lines = _seeds(4)

@@ -172,3 +172,41 @@ def test_scan_module_da_table_matches_plain_tracking():
     p_all = np.full(s.n, 0.5)
     out = sg.screened_outcome(p_all, np.ones(s.n, dtype=bool), surv)
     assert np.array_equal(out, surv)
+
+
+def test_linear_aperture_of_an_uncoupled_ring():
+    """One rectangular aperture at the start of a ring with Courant-Snyder
+    optics (beta_x = 80 m, beta_y = 25 m), no orbit: the linear aperture of
+    a ray at angle t is min(a_x / (cos t sigma_x), a_y / (sin t sigma_y))."""
+    W = np.zeros((6, 6))
+    W[0:2, 0:2] = _cs(80.0, -1.3)
+    W[2:4, 2:4] = _cs(25.0, 0.7)
+    W[4:6, 4:6] = _cs(900.0, 0.0)
+    dx = np.zeros((6, 1))
+    dy = np.zeros((6, 1))
+    dx[0, 0] = 1.0
+    dy[2, 0] = 1.0
+    ax, ay = 0.02, 0.015
+    rect = np.array([[-ax, ax, -ay, ay]])
+    ell = np.full((1, 2), np.inf)
+    angles = np.linspace(0.1, 1.4, 7)
+    beta0, gamma0 = 0.9999, 7000.0
+    eps = 2.5e-6 / (beta0 * gamma0)
+    got = da.linear_aperture(np.zeros(1), np.zeros(1), dx, dy, W, rect, ell, [0.0], angles,
+                             2.5e-6, 2.5e-6, beta0, gamma0)
+    sx, sy = np.sqrt(80.0 * eps), np.sqrt(25.0 * eps)
+    want = np.minimum(ax / (np.cos(angles) * sx), ay / (np.sin(angles) * sy))
+    assert np.allclose(got[0], want, rtol=1e-9)
+    # an orbit offset eats into the aperture on one side
+    got_co = da.linear_aperture(np.array([0.005]), np.zeros(1), dx, dy, W, rect, ell, [0.0],
+                                angles, 2.5e-6, 2.5e-6, beta0, gamma0)
+    want_co = np.minimum((ax - 0.005) / (np.cos(angles) * sx), ay / (np.sin(angles) * sy))
+    assert np.allclose(got_co[0], want_co, rtol=1e-9)
+    # an elliptical aperture of the same half axes, on the diagonal ray
+    got_e = da.linear_aperture(np.zeros(1), np.zeros(1), dx, dy, W,
+                               np.array([[-np.inf, np.inf, -np.inf, np.inf]]),
+                               np.array([[ax, ay]]), [0.0], [np.pi / 4], 2.5e-6, 2.5e-6,
+                               beta0, gamma0)
+    c = np.cos(np.pi / 4)
+    want_e = 1.0 / np.sqrt((c * sx / ax) ** 2 + (c * sy / ay) ** 2)
+    assert np.isclose(got_e[0, 0], want_e, rtol=1e-9)

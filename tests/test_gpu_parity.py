@@ -222,7 +222,7 @@ def test_monitor_repetitions_and_ebe():
 # than the ring), frequent compaction, graph replay of the rounds
 LAUNCH_SHAPES = [
     (1, 256, 0, 0), (7, 128, 49152, 0), (0, 64, 49152, 0), (3, 256, 2048, 0),
-    (5, 256, 1024, 1), (0, 128, 0, 1), (2, 64, 4096, 1),
+    (5, 256, 1024, 1), (0, 128, 0, 1), (2, 64, 4096, 1), (4, 32, 2048, 0), (0, 32, 0, 1),
 ]
 
 

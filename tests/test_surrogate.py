@@ -189,3 +189,78 @@ def test_ray_screening_band_and_outcome():
     t2 = track | aud
     out2 = sg.ray_outcome(p, r, ray, t2, truth[t2], hi=0.98, audit_mask=aud)
     assert np.array_equal(out2, truth)
+
+
+def test_sentinels_bracket_and_ray_survival():
+    """Three rays of 200 amplitudes. Ray 0 is lost from r >= 120, ray 1 from
+    r >= 37 with an isolated loss at r = 15, ray 2 never. Sentinels every
+    10th amplitude (1, 11, 21, ...) find ray 0's bracket (111, 121); tracking it
+    gives ray 0's exact DA; ray 1's isolated loss sits between sentinels and
+    is missed (its DA comes out as 37); ray 2 keeps its largest amplitude."""
+    r = np.tile(np.arange(1.0, 201.0), 3)
+    ray = np.repeat(np.arange(3), 200)
+    truth = np.ones(600, dtype=bool)
+    truth[(ray == 0) & (r >= 120)] = False
+    truth[(ray == 1) & (r >= 37)] = False
+    truth[(ray == 1) & (r == 15)] = False
+    s1 = sg.sentinels(r, ray, 10)
+    assert s1.sum() == 3 * 21
+    assert s1[(ray == 0) & (r == 1)].all() and s1[(ray == 0) & (r == 200)].all()
+    b = sg.bracket(r, ray, s1, truth)
+    assert np.array_equal(np.sort(r[b & (ray == 0)]), np.arange(112.0, 121.0))
+    assert np.array_equal(np.sort(r[b & (ray == 1)]), np.arange(32.0, 41.0))
+    assert not (b & (ray == 2)).any()
+    assert not (b & s1).any()
+    tracked = s1 | b
+    surv = sg.ray_survival(r, ray, tracked, truth)
+    assert np.array_equal(surv[tracked], truth[tracked])
+
+    def da(m):
+        return [r[(ray == k) & ~m].min() if ((ray == k) & ~m).any() else r[ray == k].max()
+                for k in range(3)]
+    assert da(truth) == [120.0, 15.0, 200.0]
+    assert da(surv) == [120.0, 37.0, 200.0]
+
+
+@pytest.mark.gpu
+def test_screened_da_scan_equals_plain_scan_on_most_rays():
+    """End to end on a short ring. The screened DA scan (sentinels every
+    8th amplitude plus the network's band, then each ray's bracket) gives
+    the plain scan's DA on most rays while tracking a fraction of the grid;
+    a ray can only differ through a lost amplitude below its bracket that no
+    pass tracked. The network is trained on four other seeds."""
+    import xtrack_gb300 as xt
+    from xtrack_gb300 import scan as sc
+    from xtrack_gb300 import workloads
+
+    def lines(seeds):
+        return [workloads.thick_ring(seed=s, n_arcs=1, n_cells=3, bend_angle=2 * math.pi / 1104)
+                for s in seeds]
+
+    turns = 40
+    train, test = lines(range(1, 5)), lines([11, 12])
+    s_tr = sc.build_scan(train, [6600] * 4, r_max=400.0, n_angles=5)
+    s_te = sc.build_scan(test, [6600] * 2, r_max=400.0, n_angles=5)
+    assert s_te.r_lin.shape == (2, 2, 5) and np.all(s_te.r_lin > 0)
+    bt = xt.BatchTracker(train, device="cuda", arith="fast")
+    st, at, _ = sc.run_scan(bt, s_tr, turns)
+    surv, lt = sg.targets(st, at, turns)
+    assert 0.1 < surv.mean() < 0.9
+    net = sg.SurvivalMLP(n_in=sg.N_DA_FEATURES, seed=2)
+    net.fit(sg.da_features(s_tr), surv, lt, epochs=30, batch=1024, lr=3e-3)
+    bt_te = xt.BatchTracker(test, device="cuda", arith="fast")
+    st_p, at_p, _ = sc.run_scan(bt_te, s_te, turns)
+    surv_plain = sg.targets(st_p, at_p, turns)[0] > 0
+    da_plain = sc.da_table(s_te, surv_plain, 2)
+    p, _ = net.predict(sg.da_features(s_te))
+    res = sc.screened_da_scan(bt_te, s_te, turns, p_survive=p, stride=8)
+    # tracked outcomes are the plain outcomes (same kernels, same particles)
+    assert np.array_equal(res.survive[res.tracked], surv_plain[res.tracked])
+    assert res.tracked_fraction < 0.5
+    exact = np.isclose(res.da, da_plain, rtol=0, atol=1e-12)
+    assert exact.mean() >= 0.7
+    # a ray that differs has an untracked plain loss below its screened DA
+    ray = s_te.ray_index()
+    for k in np.flatnonzero(~exact.ravel()):
+        m = (ray == k) & ~surv_plain & ~res.tracked
+        assert s_te.r[m].min() < res.da.ravel()[k]

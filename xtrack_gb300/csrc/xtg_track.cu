@@ -10,7 +10,11 @@
 //    each round, a compaction kernel (warp ballot + prefix sum, grouped by
 //    lattice with match_any) lists the particles still alive, and a queue
 //    kernel cuts that list into work items of one block each;
-//  * a persistent kernel pulls work items from the device queue. Each thread
+//  * a persistent kernel pulls work items from the device queue; block b
+//    takes item b first (blocks are dispatched breadth-first over the SMs,
+//    so a round with fewer items than resident blocks spreads evenly and no
+//    FP64 pipe carries two warps while another idles), later items come
+//    from an atomic counter. Each thread
 //    owns one particle, keeps its coordinates in registers for the whole
 //    round and walks the packed element table (xtg_table.h) with
 //    warp-uniform records and a warp-uniform switch on the element type;
@@ -76,9 +80,14 @@ static int32_t set_error(int32_t code, const char* fmt, ...) {
 // push kernel stay within the 227 KB a block may use
 static constexpr int32_t kMaxChunkBytes = 113 * 1024;
 
+// smallest block size of the push; the work-item buffers hold one item per
+// kMinBlock particles plus one per lattice
+static constexpr int32_t kMinBlock = 32;
+
 // device error word values
 #define XTG_DEV_ERR_TIMEOUT 1
 #define XTG_DEV_ERR_LATTICE_INDEX 2
+#define XTG_DEV_ERR_ITEMS 3
 
 // ---------------------------------------------------------------------------
 // kernel arguments
@@ -510,8 +519,10 @@ __global__ void __launch_bounds__(256, kExact ? 1 : XTG_FAST_MIN_BLOCKS) track_k
     rf.preserve_angle = a.preserve_angle != 0;
     bool const ignore_global = flag_on(a.track_flags, XTG_FLAG_IGNORE_GLOBAL_APERTURE) || !a.has_global;
 
+    bool first = true;
     for (;;) {
-        if (tid == 0) s_item = atomicAdd(a.item_counter, 1);
+        if (tid == 0) s_item = first ? (int)blockIdx.x : (int)gridDim.x + atomicAdd(a.item_counter, 1);
+        first = false;
         __syncthreads();
         int const it = s_item;
         int const nit = *((volatile const int32_t*)a.n_items);
@@ -727,15 +738,22 @@ __global__ void compact_kernel(const int64_t* __restrict__ state, const int32_t*
 }
 
 // Cuts each lattice's list into items of at most `block` particles and
-// resets the queue counter.
+// resets the queue counter. A list that needs more than `items_cap` items
+// writes none: the round tracks nothing and the error word says why.
 __global__ void items_kernel(const int32_t* lat_count, const int64_t* lat_pbase, int32_t n_lat,
-                             int32_t block, int4* items, int32_t* n_items, int32_t* item_counter) {
+                             int32_t block, int4* items, int64_t items_cap, int32_t* n_items,
+                             int32_t* item_counter, int32_t* err) {
+    __shared__ int s_fits;
     if (threadIdx.x == 0) {
-        int32_t acc = 0;
+        int64_t acc = 0;
         for (int32_t l = 0; l < n_lat; l++) acc += (lat_count[l] + block - 1) / block;
-        *n_items = acc;
+        s_fits = acc <= items_cap;
+        *n_items = s_fits ? (int32_t)acc : 0;
         *item_counter = 0;
+        if (!s_fits) atomicExch(err, XTG_DEV_ERR_ITEMS);
     }
+    __syncthreads();
+    if (!s_fits) return;
     // one thread per lattice writes that lattice's items
     for (int32_t l = threadIdx.x; l < n_lat; l += blockDim.x) {
         int32_t first = 0;
@@ -932,7 +950,7 @@ static int32_t ensure_ws(Workspace* W, int64_t cap, int32_t n_lat) {
         XTG_CUDA_CHECK(cudaMalloc(&W->idx, (size_t)std::max<int64_t>(cap, 1) * sizeof(int32_t)));
         W->cap = cap;
     }
-    int64_t const items_needed = (cap + 63) / 64 + n_lat + 1;   // blocks of >= 64 threads
+    int64_t const items_needed = (cap + kMinBlock - 1) / kMinBlock + n_lat + 1;
     if (items_needed > W->items_cap) {
         if (W->items) cudaFree(W->items);
         W->items = nullptr;
@@ -996,8 +1014,8 @@ static int32_t launch_round(ExecCtx* C, const TrackArgs& a, const int32_t* lat, 
     XTG_CUDA_CHECK(cudaMemsetAsync(W.lat_count, 0, n_lat * sizeof(int32_t), s));
     int64_t const cgrid = (cap + 255) / 256;
     compact_kernel<<<(unsigned)cgrid, 256, 0, s>>>(a.P.state, lat, cap, n_lat, W.lat_pbase, W.lat_count, W.idx);
-    items_kernel<<<1, 256, 0, s>>>(W.lat_count, W.lat_pbase, n_lat, block, W.items, W.counters + 0,
-                                   W.counters + 1);
+    items_kernel<<<1, 256, 0, s>>>(W.lat_count, W.lat_pbase, n_lat, block, W.items, W.items_cap, W.counters + 0,
+                                   W.counters + 1, W.counters + 2);
     track_kernel<kExact><<<grid, block, smem, s>>>(a);
     g_launch_count.fetch_add(3);
     XTG_CUDA_CHECK(cudaGetLastError());
@@ -1175,7 +1193,7 @@ static int32_t track_impl(ExecCtx* C, const xtg_particles* particles, const int3
 // Layout (bytes from the 256-aligned start): active-particle index list,
 // work items, counters {n_items, item_counter, error word, pad}, lattice
 // count, lattice bases.
-constexpr int64_t kNoAllocItems = XTG_NOALLOC_MAX_PARTICLES / 64 + 2;
+constexpr int64_t kNoAllocItems = XTG_NOALLOC_MAX_PARTICLES / kMinBlock + 2;
 constexpr int64_t kNoAllocIdxOff = 0;
 constexpr int64_t kNoAllocItemsOff = kNoAllocIdxOff + XTG_NOALLOC_MAX_PARTICLES * 4;
 constexpr int64_t kNoAllocCountersOff = kNoAllocItemsOff + kNoAllocItems * 16;
@@ -1231,7 +1249,8 @@ static int32_t run_rounds_noalloc(unsigned char* scratch, TrackArgs a, int64_t c
         XTG_CUDA_CHECK(cudaMemsetAsync(lat_count, 0, sizeof(int32_t), s));
         compact_kernel<<<(unsigned)((cap + 255) / 256), 256, 0, s>>>(a.P.state, nullptr, cap, 1, lat_pbase,
                                                                    lat_count, idx);
-        items_kernel<<<1, 256, 0, s>>>(lat_count, lat_pbase, 1, block, items, counters + 0, counters + 1);
+        items_kernel<<<1, 256, 0, s>>>(lat_count, lat_pbase, 1, block, items, kNoAllocItems, counters + 0,
+                                       counters + 1, counters + 2);
         track_kernel<kExact><<<grid, block, 0, s>>>(a);
         g_launch_count.fetch_add(3);
         XTG_CUDA_CHECK(cudaGetLastError());
@@ -1248,12 +1267,13 @@ static int32_t read_device_status(const ExecCtx* C) {
     if (h[2] == XTG_DEV_ERR_TIMEOUT) return set_error(XTG_E_TIMEOUT, "a bounded device wait timed out");
     if (h[2] == XTG_DEV_ERR_LATTICE_INDEX)
         return set_error(XTG_E_VALUE, "a particle has a lattice index outside the batch");
+    if (h[2] == XTG_DEV_ERR_ITEMS) return set_error(XTG_E_VALUE, "the work-item buffer is too small");
     return XTG_OK;
 }
 
 static int32_t check_tuning(const xtg_tuning* t) {
-    if (!(t->block_size == 64 || t->block_size == 128 || t->block_size == 256))
-        return set_error(XTG_E_VALUE, "block_size must be 64, 128 or 256");
+    if (!(t->block_size == kMinBlock || t->block_size == 64 || t->block_size == 128 || t->block_size == 256))
+        return set_error(XTG_E_VALUE, "block_size must be 32, 64, 128 or 256");
     if (t->compact_every < 0) return set_error(XTG_E_VALUE, "compact_every must be >= 0");
     if (t->chunk_bytes < 0 || t->chunk_bytes % 16 || t->chunk_bytes > kMaxChunkBytes)
         return set_error(XTG_E_VALUE, "chunk_bytes must be a multiple of 16 in [0, %d]", kMaxChunkBytes);

@@ -13,7 +13,10 @@ The pieces a DA study needs around ``Line.track``:
 * ``polar_grid`` and ``normalized_to_physical``: initial conditions on a
   polar grid of normalised amplitudes (in beam sigmas);
 * ``dynamic_aperture``: per angle, the smallest amplitude lost within the
-  turn budget, from the ``state`` / ``at_turn`` map that tracking leaves.
+  turn budget, from the ``state`` / ``at_turn`` map that tracking leaves;
+* ``linear_aperture``: per ray, the amplitude at which the linear motion
+  around the closed orbit first reaches an aperture (a physics prior for
+  the DA of an aperture-limited ring).
 
 ``track_fn(coords) -> coords`` is any one-turn map on an ``(n, 6)`` array of
 (x, px, y, py, zeta, delta); ``line_track_fn`` builds one from a tracker.
@@ -164,3 +167,65 @@ def dynamic_aperture(r, theta, state, at_turn, num_turns):
         rl = r[sel & lost]
         da[k] = rl.min() if rl.size else r[sel].max()
     return angles, da
+
+
+def linear_aperture(co_x, co_y, dx_dz, dy_dz, W, rect, ellipse, deltas, angles, nemitt_x, nemitt_y,
+                    beta0, gamma0, r_hi=1000.0, iters=60):
+    """Linear aperture in sigma for each (delta, angle) ray: the smallest
+    amplitude r at which a particle started at the scan's initial condition
+    (``normalized_to_physical`` with x_norm = r cos(angle), y_norm =
+    r sin(angle), delta offset added) touches an aperture when its
+    transverse normal modes take every phase while its longitudinal mode
+    keeps its initial phase (a short scan sees a fraction of a synchrotron
+    period).
+
+    co_x, co_y: (n_ap,) closed orbit at the apertures; dx_dz, dy_dz:
+    (6, n_ap) derivatives of x and y at the apertures with respect to the
+    start coordinates (one turn of offset particles); rect: (n_ap, 4)
+    min_x, max_x, min_y, max_y (+-inf where unlimited); ellipse: (n_ap, 2)
+    semi-axes a, b (inf where the aperture is not an ellipse). Returns an
+    array (len(deltas), len(angles)); r_hi where nothing is touched."""
+    W = np.asarray(W, dtype=np.float64)
+    Hx = W.T @ np.asarray(dx_dz)          # x at each aperture per normalised coordinate
+    Hy = W.T @ np.asarray(dy_dz)
+    hxx, hxy = np.hypot(Hx[0], Hx[1]), np.hypot(Hx[2], Hx[3])
+    hyx, hyy = np.hypot(Hy[0], Hy[1]), np.hypot(Hy[2], Hy[3])
+    rect = np.asarray(rect, dtype=np.float64)
+    ell = np.asarray(ellipse, dtype=np.float64)
+    gx = np.sqrt(nemitt_x / (beta0 * gamma0))
+    gy = np.sqrt(nemitt_y / (beta0 * gamma0))
+    Winv = np.linalg.inv(W)
+    out = np.empty((len(deltas), len(angles)))
+
+    def touches(r, u, c):
+        zn = r * u + c
+        ax, ay = np.hypot(zn[0], zn[1]), np.hypot(zn[2], zn[3])
+        xc = co_x + Hx[4] * zn[4] + Hx[5] * zn[5]
+        yc = co_y + Hy[4] * zn[4] + Hy[5] * zn[5]
+        ex = ax * hxx + ay * hxy
+        ey = ax * hyx + ay * hyy
+        hit = ((xc + ex > rect[:, 1]) | (xc - ex < rect[:, 0]) |
+               (yc + ey > rect[:, 3]) | (yc - ey < rect[:, 2]))
+        with np.errstate(divide="ignore", invalid="ignore"):
+            e = np.square((np.abs(xc) + ex) / ell[:, 0]) + np.square((np.abs(yc) + ey) / ell[:, 1])
+        return bool(np.any(hit | (e > 1.0)))
+
+    for d, dl in enumerate(deltas):
+        c = Winv @ np.array([0.0, 0.0, 0.0, 0.0, 0.0, float(dl)])
+        for a, th in enumerate(angles):
+            u = np.array([np.cos(th) * gx, 0.0, np.sin(th) * gy, 0.0, 0.0, 0.0])
+            if touches(0.0, u, c):
+                out[d, a] = 0.0
+                continue
+            if not touches(r_hi, u, c):
+                out[d, a] = r_hi
+                continue
+            lo, hi = 0.0, r_hi
+            for _ in range(iters):
+                mid = 0.5 * (lo + hi)
+                if touches(mid, u, c):
+                    hi = mid
+                else:
+                    lo = mid
+            out[d, a] = hi
+    return out

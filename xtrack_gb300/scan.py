@@ -29,10 +29,26 @@ class Scan:
         self.seed_features = None  # (n_seeds, k)
         self.tunes = None
         self.co_extremes = None   # (n_seeds, 4): max x, min x, max y, min y of the orbit
+        self.r_lin = None         # (n_seeds, n_deltas, n_angles): linear aperture in sigma
 
     @property
     def n(self):
         return len(self.r)
+
+    @property
+    def angles(self):
+        return np.unique(self.theta)
+
+    def ray_index(self):
+        """Ray of each particle: (seed, momentum offset, angle) flattened as
+        (seed * n_deltas + delta_index) * n_angles + angle_index."""
+        ang = self.angles
+        return ((self.lattice_index.astype(np.int64) * len(self.deltas) + self.delta_index)
+                * len(ang) + np.searchsorted(ang, self.theta))
+
+    def ray_r_lin(self):
+        """Linear aperture of each particle's ray (sigma)."""
+        return self.r_lin[self.lattice_index, self.delta_index, np.searchsorted(self.angles, self.theta)]
 
 
 def seed_normal_form(tracker, particle_ref_kwargs, device="cuda"):
@@ -56,6 +72,45 @@ def closed_orbit_extremes(tracker, co, particle_ref_kwargs, device="cuda"):
     return np.array([x.max(), x.min(), y.max(), y.min()])
 
 
+def seed_linear_aperture(tracker, co, W, particle_ref_kwargs, deltas, angles, nemitt,
+                         beta0, gamma0, device="cuda", steps=(1e-9, 1e-9, 1e-9, 1e-9, 1e-8, 1e-8)):
+    """Linear aperture (sigma) of one seed per (delta, angle) ray
+    (``da.linear_aperture``): one element-by-element turn of the closed
+    orbit and of six offset particles gives the orbit and the linear
+    optics at every LimitRect and LimitEllipse."""
+    from .elements import LimitEllipse, LimitRect
+    line = tracker.line
+    idx, rect, ell = [], [], []
+    inf = np.inf
+    for e, name in enumerate(line.element_names):
+        el = line.element_dict[name]
+        if isinstance(el, LimitRect):
+            idx.append(e)
+            rect.append((el.min_x, el.max_x, el.min_y, el.max_y))
+            ell.append((inf, inf))
+        elif isinstance(el, LimitEllipse):
+            idx.append(e)
+            rect.append((-inf, inf, -inf, inf))
+            ell.append((el.a, el.b))
+    if not idx:
+        return np.full((len(deltas), len(angles)), 1000.0)
+    h = np.asarray(steps, dtype=np.float64)
+    c = np.tile(np.asarray(co, dtype=np.float64), (7, 1))
+    for k in range(6):
+        c[k + 1, k] += h[k]
+    p = Particles(device=device, x=c[:, 0], px=c[:, 1], y=c[:, 2], py=c[:, 3], zeta=c[:, 4],
+                  delta=c[:, 5], **particle_ref_kwargs)
+    tracker._track(p, num_turns=1, turn_by_turn_monitor="ONE_TURN_EBE")
+    mon = tracker.record_last_track
+    idx = np.asarray(idx)
+    X = np.asarray(mon.x)[:, idx]
+    Y = np.asarray(mon.y)[:, idx]
+    dx = (X[1:] - X[0]) / h[:, None]
+    dy = (Y[1:] - Y[0]) / h[:, None]
+    return da.linear_aperture(X[0], Y[0], dx, dy, W, np.array(rect), np.array(ell), deltas, angles,
+                              nemitt, nemitt, beta0, gamma0)
+
+
 def build_scan(lines, counts, r_max=20.0, n_angles=11, deltas=(0.0, 2.7e-4), nemitt=2.5e-6,
                seed=0, device="cuda", arith="fast", features=None):
     """Initial conditions for ``lines`` (one per seed) with ``counts[s]``
@@ -71,11 +126,14 @@ def build_scan(lines, counts, r_max=20.0, n_angles=11, deltas=(0.0, 2.7e-4), nem
     parts = {k: [] for k in ("coords", "lat", "r", "theta", "di")}
     tunes = []
     co_ext = []
+    r_lin = []
     for s, line in enumerate(lines):
         tr = line.build_tracker(device=device, arith=arith)
         co, W, q = seed_normal_form(tr, ref_kw, device=device)
         tunes.append(q)
         co_ext.append(closed_orbit_extremes(tr, co, ref_kw, device=device))
+        r_lin.append(seed_linear_aperture(tr, co, W, ref_kw, out.deltas, theta_rays, nemitt,
+                                          beta0, gamma0, device=device))
         n_rays = n_angles * len(deltas)
         per_ray = max(1, int(counts[s]) // n_rays)
         r = np.tile(np.linspace(r_max / per_ray, r_max, per_ray), n_rays)
@@ -96,6 +154,7 @@ def build_scan(lines, counts, r_max=20.0, n_angles=11, deltas=(0.0, 2.7e-4), nem
     out.delta_index = np.concatenate(parts["di"])
     out.tunes = np.array(tunes)
     out.co_extremes = np.array(co_ext)
+    out.r_lin = np.array(r_lin)
     out.ref_kw = ref_kw
     if features is not None:
         out.seed_features = np.stack([features(line) for line in lines])
@@ -120,15 +179,77 @@ def run_scan(tracker, scan, num_turns, select=None, device="cuda"):
 
 def da_table(scan, survive, n_seeds):
     """DA (sigma) per seed, momentum offset and angle from a survival map:
-    array (n_seeds, n_deltas, n_angles)."""
-    angles = np.unique(scan.theta)
-    out = np.zeros((n_seeds, len(scan.deltas), len(angles)))
+    array (n_seeds, n_deltas, n_angles); a ray with no loss gets its largest
+    amplitude."""
+    n_d, n_a = len(scan.deltas), len(scan.angles)
+    n_rays = n_seeds * n_d * n_a
+    ray = scan.ray_index()
     lost = ~np.asarray(survive, dtype=bool)
-    for s in range(n_seeds):
-        for d in range(len(scan.deltas)):
-            sel = (scan.lattice_index == s) & (scan.delta_index == d)
-            for k, a in enumerate(angles):
-                m = sel & (scan.theta == a)
-                rl = scan.r[m & lost]
-                out[s, d, k] = rl.min() if rl.size else scan.r[m].max()
-    return out
+    first_loss = np.full(n_rays, np.inf)
+    np.minimum.at(first_loss, ray[lost], scan.r[lost])
+    r_top = np.zeros(n_rays)
+    np.maximum.at(r_top, ray, scan.r)
+    return np.where(np.isfinite(first_loss), first_loss, r_top).reshape(n_seeds, n_d, n_a)
+
+
+class ScreenedDA:
+    """Result of ``screened_da_scan``: per-particle masks of the two passes,
+    the survival map, the DA table (n_seeds, n_deltas, n_angles) and the
+    wall time of each pass (tracking plus the host work that chose it)."""
+
+    def __init__(self):
+        self.pass1 = None
+        self.pass2 = None
+        self.survive = None
+        self.da = None
+        self.seconds = []
+
+    @property
+    def tracked(self):
+        return self.pass1 | self.pass2
+
+    @property
+    def tracked_fraction(self):
+        return float(self.tracked.mean())
+
+
+def screened_da_scan(tracker, scan, num_turns, p_survive=None, stride=34, lo=0.02, hi=0.98,
+                     refine=True, device="cuda"):
+    """DA scan that tracks a subset of the grid. Pass 1 tracks the
+    ``sentinels`` (every ``stride``-th amplitude of each ray) and, when the
+    network's ``p_survive`` is given, the band where it is unsure
+    (``screen_rays`` with lo/hi). Pass 2 (``refine``) tracks each ray's
+    ``bracket``: the untracked amplitudes between the last tracked survivor
+    and the first tracked loss. The ray's DA is its smallest tracked loss;
+    it equals the DA of plain tracking unless a lost amplitude below the
+    bracket was never tracked. Returns a ``ScreenedDA``."""
+    import time
+    from . import surrogate as sg
+
+    res = ScreenedDA()
+    ray = scan.ray_index()
+    n = scan.n
+    survive = np.zeros(n, dtype=bool)
+
+    def track(mask):
+        st, at, _ = run_scan(tracker, scan, num_turns, select=mask, device=device)
+        survive[mask] = sg.targets(st, at, num_turns)[0] > 0
+
+    t0 = time.perf_counter()
+    m1 = sg.sentinels(scan.r, ray, stride)
+    if p_survive is not None:
+        m1 |= sg.screen_rays(p_survive, scan.r, ray, lo, hi, 0.0)[0]
+    track(m1)
+    res.seconds.append(time.perf_counter() - t0)
+    res.pass1 = m1
+    res.pass2 = np.zeros(n, dtype=bool)
+    if refine:
+        t0 = time.perf_counter()
+        m2 = sg.bracket(scan.r, ray, m1, survive)
+        if m2.any():
+            track(m2)
+        res.pass2 = m2
+        res.seconds.append(time.perf_counter() - t0)
+    res.survive = sg.ray_survival(scan.r, ray, res.tracked, survive)
+    res.da = da_table(scan, res.survive, int(scan.lattice_index.max()) + 1 if n else 0)
+    return res

@@ -14,9 +14,12 @@ reduction and an Adam step on FP32 master weights (include/xtrack_gb300.h,
 (P(survive) between two thresholds) plus a random audit fraction and takes
 the network's answer for the rest; ``screen_rays`` does the same per ray
 of a DA scan, tracking the band from the first uncertain amplitude to the
-first confidently lost one. Plain tracking of every particle stays the
-reference the screened result is judged against (DA error in beam sigma,
-misclassification rate on the audit).
+first confidently lost one. A DA scan adds ``sentinels`` (every k-th
+amplitude of each ray) to that band and, in a second pass, tracks the
+``bracket`` between the last surviving and the first lost tracked
+amplitude of each ray (``scan.screened_da_scan``). Plain tracking of every
+particle stays the reference the screened result is judged against (DA
+error in beam sigma, misclassification rate on the audit).
 
 No reference counterpart: xtrack has no learned component.
 """
@@ -30,6 +33,7 @@ from . import _abi
 
 N_SEED_FEATURES = 32
 N_COORD_FEATURES = 6
+N_DA_FEATURES = N_COORD_FEATURES + 8
 
 
 def _ptr(t):
@@ -243,6 +247,18 @@ def coord_features(r, theta, delta, delta_scale=2.7e-4):
                      (r * np.cos(theta)) ** 2 + 0.5 * (r * np.sin(theta)) ** 2], axis=1)
 
 
+def da_features(scan):
+    """Features of each particle of a DA scan (``scan.Scan``): its
+    coordinates (``coord_features``), its seed's linear tunes and
+    closed-orbit extremes (mm), its ray's linear aperture (sigma) and the
+    ratio of its amplitude to it. N_DA_FEATURES columns."""
+    li = scan.lattice_index
+    rl = scan.ray_r_lin()
+    return np.concatenate([coord_features(scan.r, scan.theta, scan.deltas[scan.delta_index]),
+                           scan.tunes[li][:, :2], 1e3 * scan.co_extremes[li], rl[:, None],
+                           (scan.r / np.maximum(rl, 1e-9))[:, None]], axis=1)
+
+
 def targets(state, at_turn, num_turns):
     """(survive, normalised log loss turn) from a tracking result."""
     state = np.asarray(state)
@@ -311,6 +327,67 @@ def ray_outcome(p_survive, r, ray_id, tracked_mask, tracked_survive, hi=0.95, au
             out[untracked] = r[untracked] < r_band_lo
         else:
             out[untracked] = p[untracked] >= hi
+    return out
+
+
+def _rays(r, ray_id):
+    """Particle indices sorted by (ray, amplitude) and the [start, end) of
+    each ray in that order."""
+    order = np.lexsort((np.asarray(r), np.asarray(ray_id)))
+    rid = np.asarray(ray_id)[order]
+    starts = np.flatnonzero(np.r_[True, rid[1:] != rid[:-1]]) if len(rid) else np.zeros(0, np.int64)
+    ends = np.r_[starts[1:], len(order)]
+    return order, starts, ends
+
+
+def sentinels(r, ray_id, stride):
+    """Mask of every ``stride``-th amplitude of each ray, counted from the
+    smallest, plus the largest."""
+    mask = np.zeros(len(r), dtype=bool)
+    order, starts, ends = _rays(r, ray_id)
+    for a, b in zip(starts, ends):
+        idx = order[a:b]
+        mask[idx[::stride]] = True
+        mask[idx[-1]] = True
+    return mask
+
+
+def bracket(r, ray_id, tracked_mask, survive):
+    """Mask of the untracked particles of each ray between the largest
+    tracked survivor below the ray's smallest tracked loss and that loss:
+    the amplitudes where the ray's DA can still lie. ``survive`` is read
+    where ``tracked_mask`` is set."""
+    tracked_mask = np.asarray(tracked_mask, dtype=bool)
+    survive = np.asarray(survive, dtype=bool)
+    mask = np.zeros(len(r), dtype=bool)
+    order, starts, ends = _rays(r, ray_id)
+    for a, b in zip(starts, ends):
+        idx = order[a:b]
+        t = np.flatnonzero(tracked_mask[idx])
+        lost = t[~survive[idx[t]]]
+        if lost.size == 0:
+            continue
+        first = lost[0]
+        below = t[t < first]
+        lo = below[-1] + 1 if below.size else 0
+        mask[idx[lo:first]] = True
+    return mask
+
+
+def ray_survival(r, ray_id, tracked_mask, survive):
+    """Survival map of a sentinel/bracket scan: tracked particles keep their
+    outcome; an untracked particle survives if it lies below its ray's
+    smallest tracked loss (so the map's DA per ray is that loss)."""
+    tracked_mask = np.asarray(tracked_mask, dtype=bool)
+    out = np.where(tracked_mask, np.asarray(survive, dtype=bool), False)
+    order, starts, ends = _rays(r, ray_id)
+    r = np.asarray(r)
+    for a, b in zip(starts, ends):
+        idx = order[a:b]
+        lost = idx[tracked_mask[idx] & ~out[idx]]
+        r_loss = r[lost].min() if lost.size else np.inf
+        un = idx[~tracked_mask[idx]]
+        out[un] = r[un] < r_loss
     return out
 
 

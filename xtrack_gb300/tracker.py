@@ -109,7 +109,7 @@ class Tracker:
         return {f: getattr(t, f) for f, _ in _abi.XtgTuning._fields_}
 
     def set_tuning(self, **kw):
-        """block_size (64/128/256), compact_every (turns), chunk_bytes (0: no
+        """block_size (32/64/128/256), compact_every (turns), chunk_bytes (0: no
         shared-memory staging), use_graph. Results do not depend on them."""
         cur = self.get_tuning()
         unknown = set(kw) - set(cur)
