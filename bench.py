@@ -421,7 +421,8 @@ def run_da_screen(args):
     t0 = time.perf_counter()
     p = predict()
     res = sc.screened_da_scan(bt_test, s_test, turns, p_survive=p, stride=args.da_stride,
-                              lo=args.da_lo, hi=args.da_hi, device=dev)
+                              lo=args.da_lo, hi=args.da_hi, band_stride=args.da_band_stride,
+                              device=dev)
     t_net = time.perf_counter() - t0
     two_pass = stats(res.da, t_net, res.tracked)
     two_pass["pass_seconds"] = res.seconds
@@ -444,7 +445,7 @@ def run_da_screen(args):
            "config": {"workload": "thick LHC-like ring seeds (6993 elements), polar grid "
                                   f"0-{args.da_rmax:g} sigma x 11 angles x delta in {{0, 2.7e-4}}",
                       "turns": turns, "screen_band": [args.da_lo, args.da_hi],
-                      "sentinel_stride": args.da_stride,
+                      "sentinel_stride": args.da_stride, "band_stride": args.da_band_stride,
                       "train_seeds": len(train_lines), "test_seeds": n_seeds,
                       "train_particles": int(s_train.n), "test_particles": int(s_test.n),
                       "radial_step_sigma": grid_step, "arith": args.arith,
@@ -460,6 +461,44 @@ def run_da_screen(args):
            "train_scan_s": t_train_scan, "fit_s": t_fit, "fit_loss": [hist[0], hist[-1]],
            "setup_s": t_setup}
     print(json.dumps(out))
+
+
+def run_turn_latency(args):
+    """Milliseconds per turn of the thick ring for particle counts from a
+    fraction of one resident wave (8 warps per SM) to four waves, for
+    several block sizes: where a small tracked set (a screened scan) stops
+    being latency-bound. One JSON line per (count, block, chunk)."""
+    import torch
+    import xtrack_gb300 as xt
+    from xtrack_gb300 import workloads
+
+    rank, world, local = _dist()
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    line = workloads.thick_ring(seed=1)
+    tr = line.build_tracker(device=dev, arith=args.arith)
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    rng = np.random.default_rng(0)
+    for per_sm in (64, 128, 256, 512, 1024):
+        n = per_sm * sms
+        for block, chunk in ((32, 12288), (64, 16384), (256, 49152)):
+            tr.set_tuning(block_size=block, compact_every=10, chunk_bytes=chunk, use_graph=0)
+            best = None
+            for _ in range(2):
+                p = xt.Particles(device=dev, p0c=7e12, mass0=workloads.PROTON_MASS_EV,
+                                 x=rng.normal(0, 1e-4, n), y=rng.normal(0, 1e-4, n))
+                torch.cuda.synchronize(dev)
+                t0 = time.perf_counter()
+                tr._track(p, num_turns=10)
+                torch.cuda.synchronize(dev)
+                t = (time.perf_counter() - t0) / 10
+                best = t if best is None else min(best, t)
+            alive = int((p.state > 0).sum())
+            print(json.dumps({"workload": "turn_latency", "particles": n, "per_sm": per_sm,
+                              "block": block, "chunk_bytes": chunk, "ms_per_turn": 1e3 * best,
+                              "alive": alive, "arith": args.arith}), flush=True)
 
 
 def _traffic():
@@ -491,13 +530,16 @@ def main():
     ap.add_argument("--use-graph", dest="use_graph", type=int, default=None)
     ap.add_argument("--monitor-first", dest="monitor_first", type=int, default=0,
                     help="record 6 coordinates per turn of the first N particles")
-    ap.add_argument("--workload", default="thick_ring", choices=["thick_ring", "da_screen"])
+    ap.add_argument("--workload", default="thick_ring",
+                    choices=["thick_ring", "da_screen", "turn_latency"])
     ap.add_argument("--da-turns", dest="da_turns", type=int, default=100)
     ap.add_argument("--da-train-particles", dest="da_train_particles", type=int, default=16000)
     ap.add_argument("--da-lo", dest="da_lo", type=float, default=0.02)
     ap.add_argument("--da-hi", dest="da_hi", type=float, default=0.98)
     ap.add_argument("--da-stride", dest="da_stride", type=int, default=34,
                     help="sentinel spacing of the screened DA scan, in grid amplitudes")
+    ap.add_argument("--da-band-stride", dest="da_band_stride", type=int, default=4,
+                    help="spacing of the tracked amplitudes inside the network's uncertain band")
     ap.add_argument("--da-rmax", dest="da_rmax", type=float, default=80.0,
                     help="largest amplitude of the grid (sigma); the synthetic ring at 7 TeV "
                          "keeps everything within 20 sigma, its DA lies near the aperture")
@@ -514,6 +556,8 @@ def main():
     args = ap.parse_args()
     if args.workload == "da_screen":
         run_da_screen(args)
+    elif args.workload == "turn_latency":
+        run_turn_latency(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

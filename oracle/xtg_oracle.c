@@ -1963,8 +1963,12 @@ int32_t xto_track(const xtg_element* els, int64_t n_elements, const xtg_config* 
     int64_t const capacity = P->capacity;
 
     if (mode == XTO_MODE_PER_PARTICLE) {
+        /* chunks of 64 particles, or single particles when that would leave
+           threads idle */
+        int const dyn = capacity >= (int64_t)64 * 4 * nth ? 64 : 1;
+        (void)dyn;
 #ifdef _OPENMP
-#pragma omp parallel for schedule(dynamic, 64) num_threads(nth)
+#pragma omp parallel for schedule(dynamic, dyn) num_threads(nth)
 #endif
         for (int64_t i = 0; i < capacity; i++) xto_track_one(&a, i);
         return XTG_OK;

@@ -211,6 +211,10 @@ def test_sentinels_bracket_and_ray_survival():
     assert np.array_equal(np.sort(r[b & (ray == 1)]), np.arange(32.0, 41.0))
     assert not (b & (ray == 2)).any()
     assert not (b & s1).any()
+    band = (r >= 50) & (r <= 62)
+    th = sg.thin(band, r, ray, 4)
+    assert np.array_equal(r[th & (ray == 2)], [50.0, 54.0, 58.0, 62.0])
+    assert not (th & ~band).any()
     tracked = s1 | b
     surv = sg.ray_survival(r, ray, tracked, truth)
     assert np.array_equal(surv[tracked], truth[tracked])

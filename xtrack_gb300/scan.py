@@ -214,11 +214,12 @@ class ScreenedDA:
 
 
 def screened_da_scan(tracker, scan, num_turns, p_survive=None, stride=34, lo=0.02, hi=0.98,
-                     refine=True, device="cuda"):
+                     band_stride=1, refine=True, device="cuda"):
     """DA scan that tracks a subset of the grid. Pass 1 tracks the
     ``sentinels`` (every ``stride``-th amplitude of each ray) and, when the
-    network's ``p_survive`` is given, the band where it is unsure
-    (``screen_rays`` with lo/hi). Pass 2 (``refine``) tracks each ray's
+    network's ``p_survive`` is given, every ``band_stride``-th amplitude of
+    the band where it is unsure (``screen_rays`` with lo/hi). Pass 2
+    (``refine``) tracks each ray's
     ``bracket``: the untracked amplitudes between the last tracked survivor
     and the first tracked loss. The ray's DA is its smallest tracked loss;
     it equals the DA of plain tracking unless a lost amplitude below the
@@ -238,7 +239,10 @@ def screened_da_scan(tracker, scan, num_turns, p_survive=None, stride=34, lo=0.0
     t0 = time.perf_counter()
     m1 = sg.sentinels(scan.r, ray, stride)
     if p_survive is not None:
-        m1 |= sg.screen_rays(p_survive, scan.r, ray, lo, hi, 0.0)[0]
+        band = sg.screen_rays(p_survive, scan.r, ray, lo, hi, 0.0)[0]
+        if band_stride > 1:
+            band = sg.thin(band, scan.r, ray, band_stride)
+        m1 |= band
     track(m1)
     res.seconds.append(time.perf_counter() - t0)
     res.pass1 = m1

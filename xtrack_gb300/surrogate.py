@@ -352,6 +352,16 @@ def sentinels(r, ray_id, stride):
     return mask
 
 
+def thin(mask, r, ray_id, stride):
+    """Every ``stride``-th particle of ``mask`` on each ray, counted by
+    amplitude from the smallest, plus the ray's largest masked one."""
+    mask = np.asarray(mask, dtype=bool)
+    sel = np.flatnonzero(mask)
+    out = np.zeros(len(mask), dtype=bool)
+    out[sel[sentinels(np.asarray(r)[sel], np.asarray(ray_id)[sel], stride)]] = True
+    return out
+
+
 def bracket(r, ray_id, tracked_mask, survive):
     """Mask of the untracked particles of each ray between the largest
     tracked survivor below the ray's smallest tracked loss and that loss:
