@@ -463,6 +463,80 @@ def run_da_screen(args):
     print(json.dumps(out))
 
 
+def run_batch_scan(args):
+    """Batched DA scan of many error seeds with uneven particle counts
+    (uniform in [--batch-min, --batch-max] per seed) on the thick ring:
+    all seeds in one persistent launch (BatchTracker, per-particle lattice
+    index, autotuned launch shape) against the reference's way, one
+    tracker and one tracking call per seed, run one after the other with
+    the same launch shape. Both give bit-identical state / at_turn /
+    at_element (checked). value = particle-turns/s of the batched scan."""
+    import torch
+    import xtrack_gb300 as xt
+    from xtrack_gb300 import scan as sc
+    from xtrack_gb300 import tuning as tu
+    from xtrack_gb300 import workloads
+
+    rank, world, local = _dist()
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    turns = args.batch_turns
+    rng = np.random.default_rng(11)
+    n_seeds = args.batch_seeds
+    counts = rng.integers(args.batch_min, args.batch_max + 1, size=n_seeds)
+    lines = [workloads.thick_ring(seed=300 + s) for s in range(n_seeds)]
+    t0 = time.perf_counter()
+    scan = sc.build_scan(lines, counts, r_max=args.da_rmax, device=dev)
+    t_setup = time.perf_counter() - t0
+    bt = xt.BatchTracker(lines, device=dev, arith=args.arith)
+    probe = sc.make_particles(scan, device=dev)
+    t0 = time.perf_counter()
+    tuning, rep = tu.autotune(bt, probe, turns, probe_turns=2, repeats=1,
+                              lattice_index=scan.lattice_index)
+    t_tune = time.perf_counter() - t0
+    del probe
+
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    st_b, at_b, ae_b = sc.run_scan(bt, scan, turns, device=dev)
+    t_batch = time.perf_counter() - t0
+
+    trackers = [ln.build_tracker(device=dev, arith=args.arith) for ln in lines]
+    for tr in trackers:
+        tr.set_tuning(**tuning)
+    parts = [sc.make_particles(scan, select=scan.lattice_index == s, device=dev)
+             for s in range(n_seeds)]
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for tr, p in zip(trackers, parts):
+        tr._track(p, num_turns=turns)
+    torch.cuda.synchronize(dev)
+    t_seq = time.perf_counter() - t0
+    same = True
+    for s, p in enumerate(parts):
+        sel = scan.lattice_index == s
+        same &= bool(np.array_equal(p.state.cpu().numpy(), st_b[sel]) and
+                     np.array_equal(p.at_turn.cpu().numpy(), at_b[sel]) and
+                     np.array_equal(p.at_element.cpu().numpy(), ae_b[sel]))
+    pt = float(np.sum(at_b))
+    out = {"metric": "batched DA-scan particle-turns/s (60 seeds, one launch)",
+           "value": pt / t_batch, "unit": "particle-turns/s", "higher_is_better": True,
+           "n_gpus": 1, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": f"{n_seeds} seeds of the thick ring (6993 elements), "
+                                  f"{args.batch_min}-{args.batch_max} particles per seed on a "
+                                  f"polar grid 0-{args.da_rmax:g} sigma x 11 angles x 2 deltas",
+                      "turns": turns, "particles": int(scan.n), "arith": args.arith},
+           "batched_s": t_batch, "per_seed_s": t_seq, "speedup_vs_per_seed": t_seq / t_batch,
+           "per_seed_particle_turns_per_s": pt / t_seq, "particle_turns": pt,
+           "results_identical": same, "tuning": tuning, "autotune_s": t_tune,
+           "autotune_candidates": len(rep.get("timings", [])), "setup_s": t_setup}
+    print(json.dumps(out))
+    if not same:
+        raise SystemExit("batched and per-seed results differ")
+
+
 def run_turn_latency(args):
     """Milliseconds per turn of the thick ring for particle counts from a
     fraction of one resident wave (8 warps per SM) to four waves, for
@@ -531,7 +605,11 @@ def main():
     ap.add_argument("--monitor-first", dest="monitor_first", type=int, default=0,
                     help="record 6 coordinates per turn of the first N particles")
     ap.add_argument("--workload", default="thick_ring",
-                    choices=["thick_ring", "da_screen", "turn_latency"])
+                    choices=["thick_ring", "da_screen", "turn_latency", "batch_scan"])
+    ap.add_argument("--batch-seeds", dest="batch_seeds", type=int, default=60)
+    ap.add_argument("--batch-min", dest="batch_min", type=int, default=1000)
+    ap.add_argument("--batch-max", dest="batch_max", type=int, default=20000)
+    ap.add_argument("--batch-turns", dest="batch_turns", type=int, default=20)
     ap.add_argument("--da-turns", dest="da_turns", type=int, default=100)
     ap.add_argument("--da-train-particles", dest="da_train_particles", type=int, default=16000)
     ap.add_argument("--da-lo", dest="da_lo", type=float, default=0.02)
@@ -558,6 +636,8 @@ def main():
         run_da_screen(args)
     elif args.workload == "turn_latency":
         run_turn_latency(args)
+    elif args.workload == "batch_scan":
+        run_batch_scan(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

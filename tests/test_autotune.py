@@ -109,3 +109,32 @@ def test_autotuned_tracker_matches_default(tmp_path):
     tr2 = line.build_tracker(device="cuda", arith="fast")
     best2, rep2 = at.autotune(tr2, beam, 30, cache_path=path)
     assert rep2["source"] == "cache" and best2 == best
+
+
+@pytest.mark.gpu
+def test_autotuned_batch_matches_default(tmp_path):
+    """The tuner drives a BatchTracker through its lattice index; the tuned
+    batch tracks every particle as the default one does."""
+    import math
+
+    import torch
+    import xtrack_gb300 as xt
+    from xtrack_gb300 import workloads
+    lines = [workloads.thick_ring(seed=s, n_arcs=1, n_cells=3, bend_angle=2 * math.pi / 1104)
+             for s in range(3)]
+    n = 2000
+    lat = np.random.default_rng(4).integers(0, 3, size=n).astype(np.int32)
+    beam = workloads.gaussian_beam(n, 7e12, seed=5, device="cuda", sigma_x=2e-3, sigma_px=2e-5)
+    ref = beam.copy()
+    xt.BatchTracker(lines, device="cuda", arith="fast").track(ref, lattice_index=lat, num_turns=12)
+    bt = xt.BatchTracker(lines, device="cuda", arith="fast")
+    best, rep = at.autotune(bt, beam, 12, cache_path=str(tmp_path / "t.json"), probe_turns=2,
+                            repeats=1, lattice_index=lat,
+                            space={"block_size": (32, 256), "chunk_bytes": (0, 12288)})
+    assert rep["source"] == "search" and bt.get_tuning() == best
+    assert len(rep["timings"]) >= 3
+    got = beam.copy()
+    bt.track(got, lattice_index=lat, num_turns=12)
+    bt.device_status()
+    for f in ("x", "px", "y", "py", "zeta", "delta", "state", "at_turn", "at_element"):
+        assert torch.equal(getattr(got, f), getattr(ref, f)), f

@@ -268,3 +268,13 @@ def test_screened_da_scan_equals_plain_scan_on_most_rays():
     for k in np.flatnonzero(~exact.ravel()):
         m = (ray == k) & ~surv_plain & ~res.tracked
         assert s_te.r[m].min() < res.da.ravel()[k]
+    # the same scan without the network: what the network adds is its band
+    # (tracked on top of the sentinels); both results are judged the same way
+    res0 = sc.screened_da_scan(bt_te, s_te, turns, p_survive=None, stride=8)
+    assert np.array_equal(res0.survive[res0.tracked], surv_plain[res0.tracked])
+    exact0 = np.isclose(res0.da, da_plain, rtol=0, atol=1e-12)
+    assert exact0.mean() >= 0.7
+    assert not (res0.pass1 & ~res.pass1).any()
+    print(f"rays exact: {exact.mean():.3f} with the network "
+          f"({res.tracked_fraction:.3f} tracked), {exact0.mean():.3f} without "
+          f"({res0.tracked_fraction:.3f} tracked)")

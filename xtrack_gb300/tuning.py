@@ -21,8 +21,8 @@ import os
 import numpy as np
 
 SPACE = {
-    "block_size": (64, 128, 256),
-    "chunk_bytes": (0, 16384, 49152, 98304),
+    "block_size": (32, 64, 128, 256),
+    "chunk_bytes": (0, 12288, 16384, 49152, 98304),
     "compact_every": (0, 1, 8, 64),
     "use_graph": (0, 1),
 }
@@ -66,7 +66,7 @@ def save_cache(path, cache):
     os.replace(tmp, path)
 
 
-def _cuda_timer(tracker, particles, num_turns, repeats):
+def _cuda_timer(tracker, particles, num_turns, repeats, lattice_index=None):
     import torch
 
     def run(tuning):
@@ -78,7 +78,10 @@ def _cuda_timer(tracker, particles, num_turns, repeats):
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            tracker._track(p, num_turns=num_turns)
+            if lattice_index is None:
+                tracker._track(p, num_turns=num_turns)
+            else:
+                tracker.track(p, lattice_index=lattice_index, num_turns=num_turns)
             e1.record(stream)
             e1.synchronize()
             best = min(best, e0.elapsed_time(e1))
@@ -88,14 +91,15 @@ def _cuda_timer(tracker, particles, num_turns, repeats):
 
 
 def autotune(tracker, particles, num_turns, cache_path=None, refresh=False, probe_turns=None,
-             repeats=2, space=None, timer=None, device_name=None):
+             repeats=2, space=None, timer=None, device_name=None, lattice_index=None):
     """Finds and applies the fastest tuning of ``tracker`` for tracking
     ``particles`` over ``num_turns`` turns. Returns ``(tuning, report)``;
     ``report['source']`` is 'cache' or 'search'.
 
     ``probe_turns`` (default ``min(num_turns, 16)``) turns are timed per
     candidate on copies of ``particles``; ``particles`` itself is not
-    tracked. ``timer(tuning) -> ms`` replaces the CUDA-event timer."""
+    tracked. A ``BatchTracker`` takes the particles' ``lattice_index``.
+    ``timer(tuning) -> ms`` replaces the CUDA-event timer."""
     space = dict(SPACE if space is None else space)
     key = tuning_key(tracker, particles._capacity, num_turns, device_name=device_name)
     cache = load_cache(cache_path)
@@ -106,7 +110,7 @@ def autotune(tracker, particles, num_turns, cache_path=None, refresh=False, prob
     if probe_turns is None:
         probe_turns = min(int(num_turns), 16)
     if timer is None:
-        timer = _cuda_timer(tracker, particles, probe_turns, repeats)
+        timer = _cuda_timer(tracker, particles, probe_turns, repeats, lattice_index)
     best = dict(tracker.get_tuning())
     timings = []
     seen = {}
