@@ -381,6 +381,18 @@ int64_t xtg_launch_count(void);
 int32_t xtg_measure_fp64_peak(double* flops_per_s);
 
 /*
+ * Diagnostic of the push's failure path (no reference counterpart: the
+ * reference's kernel has no waits). Runs one shared-memory barrier wait of
+ * the kind the push uses to stage its element table, on a barrier that
+ * nothing completes, bounded at `limit_cycles` SM clock cycles (1 to
+ * 4e9). The wait gives up, records the time-out in a device error word and
+ * the kernel returns; the call reads the word as xtg_device_status does and
+ * returns XTG_E_TIMEOUT. The context stays usable. Returns XTG_OK only if
+ * the wait did not time out.
+ */
+int32_t xtg_check_bounded_wait(int64_t limit_cycles);
+
+/*
  * Survival surrogate kernels (no reference counterpart: the reference has
  * no learned component). A multilayer perceptron with BF16 weights and
  * activations and FP32 accumulation screens dynamic-aperture scans. All

@@ -33,7 +33,7 @@ import pytest
 
 import pyoracle
 import xtrack_gb300 as xt
-from xtrack_gb300 import workloads
+from xtrack_gb300 import _abi, workloads
 from lattice_cases import element_zoo, sliced_line, small_beam
 from xtg_testutil import compare, compare_within_spread, fma_spread, gpu_track, make_monitor
 
@@ -311,6 +311,19 @@ def test_batch_matches_per_seed_oracle():
         ref = {k: v[sel].copy() for k, v in arrs.items()}
         pyoracle.track(sets[s], ref, line_length=L, num_turns=12)
         compare({k: v[sel] for k, v in got.items()}, ref, 5e-14)
+
+
+def test_bounded_wait_times_out_and_the_context_survives():
+    """The push's staging wait, on a barrier nothing completes and bounded
+    at about 1 ms, gives up and reports XTG_E_TIMEOUT through the device
+    error word; tracking on the same context afterwards still equals the
+    oracle."""
+    lib = _abi.load_library()
+    assert lib.xtg_check_bounded_wait(2_000_000) == _abi.XTG_E_TIMEOUT
+    assert "timed out" in _abi.last_error(lib)
+    recs, arrs, L = _setup(workloads.toy_ring(), small_beam(500, p0c=450e9, seed=31))
+    got, ref = _run_both(recs, arrs, L, num_turns=3)
+    compare(got, ref, 1e-14)
 
 
 def test_edge_cases():

@@ -105,6 +105,9 @@ def test_null_arguments_return_errors():
     assert lib.xtg_lattice_create(None, 0, None, None) == _abi.XTG_E_NULL
     assert lib.xtg_track(None, None, 1, 0, 0, 0, 0, 0, 0, 0.0, None, 0, None) == _abi.XTG_E_NULL
     assert lib.xtg_lattice_destroy(None) == _abi.XTG_OK
+    # the wait check validates its bound before touching the device
+    assert lib.xtg_check_bounded_wait(0) == _abi.XTG_E_VALUE
+    assert lib.xtg_check_bounded_wait(5_000_000_000) == _abi.XTG_E_VALUE
 
 
 def test_particles_initialisation_formulas():

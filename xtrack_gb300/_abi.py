@@ -222,6 +222,7 @@ EXPORTED_SYMBOLS = (
     "xtg_get_tuning", "xtg_set_tuning", "xtg_device_status",
     "xtg_batch_create", "xtg_batch_destroy", "xtg_batch_get_tuning", "xtg_batch_set_tuning", "xtg_batch_device_status",
     "xtg_track_batch", "xtg_sync", "xtg_launch_count", "xtg_measure_fp64_peak",
+    "xtg_check_bounded_wait",
     "xtg_mlp_gemm", "xtg_mlp_act_backward", "xtg_mlp_colsum", "xtg_mlp_loss", "xtg_mlp_adam",
     "xtg_mlp_to_bf16", "xtg_mlp_get_last_error",
 )
@@ -304,6 +305,8 @@ def load_library(path=None):
     lib.xtg_launch_count.restype = c.c_int64
     lib.xtg_measure_fp64_peak.argtypes = [c.POINTER(c.c_double)]
     lib.xtg_measure_fp64_peak.restype = c.c_int32
+    lib.xtg_check_bounded_wait.argtypes = [c.c_int64]
+    lib.xtg_check_bounded_wait.restype = c.c_int32
     if lib.xtg_abi_version() != 2:
         raise RuntimeError("xtrack_gb300: ABI version mismatch")
     if path == LIB_PATH:

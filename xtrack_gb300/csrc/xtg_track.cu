@@ -170,11 +170,15 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 
 // Bounded wait (about 2 s of SM clock): on time-out records the error word
 // and returns false.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int32_t* err) {
+// about 2 s at the GB300's 2.07 GHz SM clock
+static constexpr long long kWaitLimitCycles = 4000000000LL;
+
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int32_t* err,
+                                                  long long limit = kWaitLimitCycles) {
     if (mbar_try_wait(bar, parity)) return true;
     long long const t0 = clock64();
     while (!mbar_try_wait(bar, parity)) {
-        if (clock64() - t0 > 4000000000LL) {
+        if (clock64() - t0 > limit) {
             atomicExch(err, XTG_DEV_ERR_TIMEOUT);
             return false;
         }
@@ -765,6 +769,19 @@ __global__ void items_kernel(const int32_t* lat_count, const int64_t* lat_pbase,
             items[first + j] = make_int4(l, (int32_t)(lat_pbase[l] + (int64_t)j * block), cnt, 0);
         }
     }
+}
+
+// One wait of the push's kind on a barrier that nothing completes: thread
+// 0 gives up after `limit` cycles and records the time-out in `err`.
+__global__ void wait_check_kernel(int32_t* err, long long limit) {
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) (void)mbar_wait_bounded(&bar, 0u, err, limit);
+    __syncthreads();
 }
 
 // ---------------------------------------------------------------------------
@@ -1541,6 +1558,27 @@ int32_t xtg_track_batch(xtg_batch* batch, const xtg_particles* particles, const 
     return track_impl(&batch->ctx, particles, lattice_index, num_turns, ele_start, num_ele_track,
                       flag_end_turn_actions, flag_reset_s_at_end_turn, flag_monitor, num_ele_line, line_length,
                       monitor, track_flags, stream);
+}
+
+int32_t xtg_check_bounded_wait(int64_t limit_cycles) {
+    if (limit_cycles < 1 || limit_cycles > kWaitLimitCycles)
+        return set_error(XTG_E_VALUE, "xtg_check_bounded_wait: limit must be in [1, %lld] cycles",
+                         (long long)kWaitLimitCycles);
+    int32_t* d_err = nullptr;
+    XTG_CUDA_CHECK(cudaMalloc(&d_err, sizeof(int32_t)));
+    int32_t h = 0;
+    cudaError_t ce = cudaMemset(d_err, 0, sizeof(int32_t));
+    if (ce == cudaSuccess) {
+        wait_check_kernel<<<1, 32>>>(d_err, (long long)limit_cycles);
+        g_launch_count.fetch_add(1);
+        ce = cudaGetLastError();
+    }
+    if (ce == cudaSuccess) ce = cudaDeviceSynchronize();
+    if (ce == cudaSuccess) ce = cudaMemcpy(&h, d_err, sizeof(int32_t), cudaMemcpyDeviceToHost);
+    cudaFree(d_err);
+    if (ce != cudaSuccess) return set_error(XTG_E_CUDA, "xtg_check_bounded_wait: %s", cudaGetErrorString(ce));
+    if (h == XTG_DEV_ERR_TIMEOUT) return set_error(XTG_E_TIMEOUT, "a bounded device wait timed out");
+    return XTG_OK;
 }
 
 int32_t xtg_measure_fp64_peak(double* flops_per_s) {
