@@ -22,7 +22,7 @@ import numpy as np
 
 SPACE = {
     "block_size": (32, 64, 128, 256),
-    "chunk_bytes": (0, 12288, 16384, 49152, 98304),
+    "chunk_bytes": (0, 12288, 16384, 32768, 49152, 98304),
     "compact_every": (0, 1, 8, 64),
     "use_graph": (0, 1),
 }
