@@ -97,7 +97,6 @@ def test_normalized_to_physical_round_trip():
 
 @pytest.mark.gpu
 def test_batched_da_scan_equals_per_seed_scans():
-    import torch
     import xtrack_gb300 as xt
     from xtrack_gb300 import workloads
     # 3 cells: horizontal tune near 0.75 (4 cells would sit on the integer)

@@ -9,7 +9,6 @@ launch, per-particle lattice index). The outcome per particle is its
 momentum offset is the smallest lost amplitude (``da.dynamic_aperture``).
 """
 import numpy as np
-import torch
 
 from . import da
 from .batch import BatchTracker

@@ -14,7 +14,6 @@ value raises, naming the element and the field.
 dict with a ``line`` entry.
 """
 import json
-import math
 
 import numpy as np
 
