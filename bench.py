@@ -537,6 +537,58 @@ def run_batch_scan(args):
         raise SystemExit("batched and per-seed results differ")
 
 
+def run_toy_ring(args):
+    """The toy thin ring (100 cells of drift, thin multipole, drift, thin
+    multipole, LimitEllipse; one cavity; protons at 450 GeV): 10,000
+    particles x 1000 turns through Line.track on the GPU (exact and fast
+    arithmetic, CUDA-synchronised wall time of the whole call), and the
+    oracle's port of the reference OpenMP path on all host cores over the
+    same particles for --toy-cpu-turns turns. One JSON line."""
+    import torch
+    from xtrack_gb300 import workloads
+    import pyoracle
+
+    rank, world, local = _dist()
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    n, turns = args.toy_particles, args.toy_turns
+    line = workloads.toy_ring()
+    p0c = float(line.particle_ref.p0c[0])
+    out = {"metric": "toy ring particle-turns/s", "unit": "particle-turns/s",
+           "higher_is_better": True, "n_gpus": 1, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": f"toy thin ring ({len(line.element_names)} elements), "
+                                  f"{n} protons 450 GeV x {turns} turns", "particles": n,
+                      "turns": turns}}
+    for arith in ("exact", "fast"):
+        tr = line.build_tracker(device=dev, arith=arith)
+        warm = workloads.gaussian_beam(n, p0c, seed=1, device=dev)
+        tr._track(warm, num_turns=10)
+        p = workloads.gaussian_beam(n, p0c, seed=2, device=dev)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        tr._track(p, num_turns=turns)
+        torch.cuda.synchronize(dev)
+        dt = time.perf_counter() - t0
+        pt = float(p.at_turn.sum().item())
+        out[arith] = {"particle_turns_per_s": pt / dt, "seconds": dt,
+                      "alive": int((p.state > 0).sum().item())}
+    out["value"] = out["fast"]["particle_turns_per_s"]
+    pyoracle.ensure_built(with_ref=False)
+    recs = line._element_records()
+    cpu_turns = min(turns, args.toy_cpu_turns)
+    beam = pyoracle.host_arrays(workloads.gaussian_beam(n, p0c, seed=2, device="cpu").to_numpy())
+    t0 = time.perf_counter()
+    pyoracle.track(recs, beam, num_turns=cpu_turns, line_length=line.get_length(),
+                   mode=pyoracle.MODE_OPENMP)
+    dt = time.perf_counter() - t0
+    out["cpu_baseline"] = {"value": float(np.sum(beam["at_turn"])) / dt, "unit": "particle-turns/s",
+                           "cores": pyoracle.max_threads(), "kind": "port",
+                           "sample": f"{n} particles x {cpu_turns} turns ({dt:.1f} s, OpenMP)"}
+    print(json.dumps(out))
+
+
 def run_turn_latency(args):
     """Milliseconds per turn of the thick ring for particle counts from a
     fraction of one resident wave (8 warps per SM) to four waves, for
@@ -605,7 +657,10 @@ def main():
     ap.add_argument("--monitor-first", dest="monitor_first", type=int, default=0,
                     help="record 6 coordinates per turn of the first N particles")
     ap.add_argument("--workload", default="thick_ring",
-                    choices=["thick_ring", "da_screen", "turn_latency", "batch_scan"])
+                    choices=["thick_ring", "da_screen", "turn_latency", "batch_scan", "toy_ring"])
+    ap.add_argument("--toy-particles", dest="toy_particles", type=int, default=10000)
+    ap.add_argument("--toy-turns", dest="toy_turns", type=int, default=1000)
+    ap.add_argument("--toy-cpu-turns", dest="toy_cpu_turns", type=int, default=1000)
     ap.add_argument("--batch-seeds", dest="batch_seeds", type=int, default=60)
     ap.add_argument("--batch-min", dest="batch_min", type=int, default=1000)
     ap.add_argument("--batch-max", dest="batch_max", type=int, default=20000)
@@ -638,6 +693,8 @@ def main():
         run_turn_latency(args)
     elif args.workload == "batch_scan":
         run_batch_scan(args)
+    elif args.workload == "toy_ring":
+        run_toy_ring(args)
     elif args.impl == "reference":
         run_reference(args)
     else:
