@@ -136,6 +136,28 @@ def test_thick_ring_1000_turns():
             compare(got, ref, 1e-8, mask=m)
 
 
+@pytest.mark.parametrize("arith", ["exact", "fast"])
+def test_full_size_beam_sampled_against_oracle(arith):
+    """The bench's full size: 1e6 protons through the thick ring, 2 turns
+    with a compaction between them, default launch shape. Each particle's
+    result depends on nothing but its own coordinates, so a random sample
+    of 256 tracked by the oracle checks the whole launch: integer fields
+    bit-exact, coordinates within 1e-13 (exact mode: the first turn's
+    last-ulp cavity difference carried through the second) or 1e-12
+    (fast mode)."""
+    line = workloads.thick_ring()
+    recs, L = line._element_records(), line.get_length()
+    beam = workloads.gaussian_beam(1_000_000, 7e12, seed=41, device="cpu")
+    arrs = pyoracle.host_arrays(beam.to_numpy())
+    got, _ = gpu_track(recs, arrs, arith=arith, line_length=L, num_turns=2, compact_every=1)
+    idx = np.sort(np.random.default_rng(42).choice(len(arrs["x"]), 256, replace=False))
+    ref = {k: np.ascontiguousarray(v[idx]) for k, v in arrs.items()}
+    pyoracle.track(recs, ref, line_length=L, num_turns=2)
+    sub = {k: v[idx] for k, v in got.items()}
+    assert np.all(sub["at_turn"] == 2)
+    compare(sub, ref, 1e-13 if arith == "exact" else 1e-12)
+
+
 def test_thick_ring_100_turns_fast():
     recs, arrs, L = _setup(workloads.thick_ring(), small_beam(64, seed=26))
     got, ref = _run_both(recs, arrs, L, arith="fast", num_turns=100)
