@@ -49,20 +49,22 @@ def _stale(target, deps):
 
 
 def _defines():
-    """Build-time options of the fast push's register budget (see
-    xtg_track.cu): XTG_FAST_MIN_BLOCKS (1 or 2) resident blocks of at most
-    XTG_FAST_LB_THREADS (384, the default, or 256) threads each."""
+    """Build-time options of the push's register budget (see xtg_track.cu):
+    XTG_FAST_MIN_BLOCKS (1 or 2) resident blocks of at most
+    XTG_FAST_LB_THREADS (384, the default, or 256) threads each for the fast
+    push; XTG_EXACT_LB_THREADS (256, the default, or 384) for the exact one."""
     out = []
     v = os.environ.get("XTG_FAST_MIN_BLOCKS")
     if v:
         if v not in ("1", "2"):
             raise ValueError("XTG_FAST_MIN_BLOCKS must be 1 or 2")
         out.append(f"-DXTG_FAST_MIN_BLOCKS={v}")
-    v = os.environ.get("XTG_FAST_LB_THREADS")
-    if v:
-        if v not in ("256", "384"):
-            raise ValueError("XTG_FAST_LB_THREADS must be 256 or 384")
-        out.append(f"-DXTG_FAST_LB_THREADS={v}")
+    for name in ("XTG_FAST_LB_THREADS", "XTG_EXACT_LB_THREADS"):
+        v = os.environ.get(name)
+        if v:
+            if v not in ("256", "384"):
+                raise ValueError(f"{name} must be 256 or 384")
+            out.append(f"-D{name}={v}")
     return out
 
 

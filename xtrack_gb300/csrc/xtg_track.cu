@@ -81,6 +81,10 @@ static int32_t set_error(int32_t code, const char* fmt, ...) {
 #ifndef XTG_FAST_LB_THREADS
 #define XTG_FAST_LB_THREADS 384
 #endif
+// the same for the exact push: 256 (228 registers) or 384 (168)
+#ifndef XTG_EXACT_LB_THREADS
+#define XTG_EXACT_LB_THREADS 256
+#endif
 
 // largest staging chunk: two chunks plus the static shared memory of the
 // push kernel stay within the 227 KB a block may use
@@ -500,7 +504,7 @@ __device__ __forceinline__ void end_turn(const TrackArgs& a, PState& p, bool act
 // the persistent push kernel
 // ---------------------------------------------------------------------------
 template <bool kExact>
-__global__ void __launch_bounds__(kExact ? 256 : XTG_FAST_LB_THREADS, kExact ? 1 : XTG_FAST_MIN_BLOCKS)
+__global__ void __launch_bounds__(kExact ? XTG_EXACT_LB_THREADS : XTG_FAST_LB_THREADS, kExact ? 1 : XTG_FAST_MIN_BLOCKS)
     track_kernel(const TrackArgs a) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ uint64_t full_bar[2];
