@@ -74,6 +74,11 @@ extern "C" {
 #define XTG_FLAG_KILL_CAVITY_KICK        2
 #define XTG_FLAG_IGNORE_GLOBAL_APERTURE  3
 #define XTG_FLAG_IGNORE_LOCAL_APERTURE   4
+/* Freeze the longitudinal coordinates (zeta, ptau, delta, rpp, rvv) for the
+   call: the reference's Line.track(freeze_longitudinal=True), which compiles
+   its setters of those variables into no-ops (FREEZE_VAR_<name>,
+   particles.py:185-225; line.py:4446-4469). Outside the reference's bits. */
+#define XTG_FLAG_FREEZE_LONGITUDINAL     32
 
 /*
  * One lattice element as the reference stores it (the `_xofields` of each

@@ -25,7 +25,9 @@ REF_LIBS = {
     "default": os.path.join(HERE, "_ref", "libxtref.so"),
     "exact_drifts": os.path.join(HERE, "_ref", "libxtref_exact.so"),
     "preserve_angle": os.path.join(HERE, "_ref", "libxtref_preserve.so"),
+    "frozen": os.path.join(HERE, "_ref", "libxtref_frozen.so"),
 }
+FLAG_FREEZE_LONGITUDINAL = 32
 
 MODE_PER_PARTICLE = 0
 MODE_OPENMP = 1
@@ -137,7 +139,7 @@ def track(records, arrs, q0=1.0, mass0=938272088.16, t_sim=0.0, num_turns=1, ele
           num_ele_track=None, flag_end_turn_actions=1, flag_reset_s=1, line_length=0.0,
           track_flags=0, use_exact_drifts=False, cavity_preserve_angle=False,
           global_xy_limit=1.0, monitor=None, flag_monitor=0, mode=MODE_PER_PARTICLE,
-          num_threads=0, num_ele_line=None, which="oracle"):
+          num_threads=0, num_ele_line=None, which="oracle", freeze_longitudinal=False):
     """Runs one track_line call in place on host arrays ``arrs``.
 
     which='oracle'     -> C restatement (no contraction: the reference's CPU
@@ -145,7 +147,10 @@ def track(records, arrs, q0=1.0, mass0=938272088.16, t_sim=0.0, num_turns=1, ele
     which='oracle_fma' -> the same source compiled with fused multiply-adds
                           (the reference's arithmetic as its CUDA build
                           rounds it);
-    which='ref'        -> reference-compiled code (no monitor, no OpenMP mode)."""
+    which='ref'        -> reference-compiled code (no monitor, no OpenMP mode).
+
+    freeze_longitudinal: the oracle sets its freeze flag; the reference
+    build with the FREEZE_VAR_<name> set of freeze_longitudinal is used."""
     records = np.ascontiguousarray(records)
     n = len(records)
     if num_ele_track is None:
@@ -154,6 +159,8 @@ def track(records, arrs, q0=1.0, mass0=938272088.16, t_sim=0.0, num_turns=1, ele
         num_ele_line = n
     cfg = _config(use_exact_drifts, cavity_preserve_angle, global_xy_limit)
     ps = _pstruct(arrs, q0, mass0, t_sim)
+    if freeze_longitudinal and which in ("oracle", "oracle_fma"):
+        track_flags = int(track_flags) | (1 << FLAG_FREEZE_LONGITUDINAL)
     if which in ("oracle", "oracle_fma"):
         ensure_built(with_ref=False)
         lib = _load(ORACLE_LIB if which == "oracle" else ORACLE_FMA_LIB, "oracle")
@@ -170,7 +177,11 @@ def track(records, arrs, q0=1.0, mass0=938272088.16, t_sim=0.0, num_turns=1, ele
                            ctypes.byref(mst) if mst is not None else None,
                            int(track_flags), mode, num_threads)
     else:
-        if use_exact_drifts:
+        if freeze_longitudinal:
+            if use_exact_drifts or cavity_preserve_angle:
+                raise ValueError("no reference build freezes with another config switch")
+            path = REF_LIBS["frozen"]
+        elif use_exact_drifts:
             path = REF_LIBS["exact_drifts"]
         elif cavity_preserve_angle:
             path = REF_LIBS["preserve_angle"]

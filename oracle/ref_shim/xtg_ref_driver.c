@@ -12,8 +12,9 @@
  *     from one xtg_element record (slice parents resolved into the record),
  *   - a per-particle restatement of the track_line driver
  *     (tracker.py:594-736, GPU semantics).
- * Build flags choose the TrackerConfig: XTRACK_USE_EXACT_DRIFTS and
- * XTRACK_CAVITY_PRESERVE_ANGLE produce separate libraries.
+ * Build flags choose the TrackerConfig: XTRACK_USE_EXACT_DRIFTS,
+ * XTRACK_CAVITY_PRESERVE_ANGLE and the FREEZE_VAR_<name> set of
+ * freeze_longitudinal produce separate libraries.
  */
 #define XO_CONTEXT_CPU
 #define XO_CONTEXT_CPU_OPENMP
@@ -70,7 +71,44 @@ typedef struct {
     static inline void LocalParticle_scale_##f(LocalParticle* p, T v) { p->f[p->ipart] *= v; }
 #define XTR_ACC_D(f) XTR_ACC(double, f)
 #define XTR_ACC_I(f) XTR_ACC(int64_t, f)
-XTR_DBL_FIELDS(XTR_ACC_D)
+/* FREEZE_VAR_<name>: the generator wraps the setter, adder and scaler of
+ * <name> in #ifndef FREEZE_VAR_<name> (particles.py:185-225), so a frozen
+ * variable keeps its value; freeze_longitudinal freezes zeta and the four
+ * energy variables (line.py:4446-4469). */
+#define XTR_ACC_FROZEN(T, f) \
+    static inline T LocalParticle_get_##f(LocalParticle* p) { return p->f[p->ipart]; } \
+    static inline void LocalParticle_set_##f(LocalParticle* p, T v) { (void)p; (void)v; } \
+    static inline void LocalParticle_add_to_##f(LocalParticle* p, T v) { (void)p; (void)v; } \
+    static inline void LocalParticle_scale_##f(LocalParticle* p, T v) { (void)p; (void)v; }
+#define XTR_FREE_DBL_FIELDS(X) X(p0c) X(gamma0) X(beta0) X(s) X(x) X(y) \
+    X(px) X(py) X(chi) X(charge_ratio) X(weight) \
+    X(ax) X(ay) X(spin_x) X(spin_y) X(spin_z) X(anomalous_magnetic_moment)
+XTR_FREE_DBL_FIELDS(XTR_ACC_D)
+#ifdef FREEZE_VAR_zeta
+XTR_ACC_FROZEN(double, zeta)
+#else
+XTR_ACC_D(zeta)
+#endif
+#ifdef FREEZE_VAR_ptau
+XTR_ACC_FROZEN(double, ptau)
+#else
+XTR_ACC_D(ptau)
+#endif
+#ifdef FREEZE_VAR_delta
+XTR_ACC_FROZEN(double, delta)
+#else
+XTR_ACC_D(delta)
+#endif
+#ifdef FREEZE_VAR_rpp
+XTR_ACC_FROZEN(double, rpp)
+#else
+XTR_ACC_D(rpp)
+#endif
+#ifdef FREEZE_VAR_rvv
+XTR_ACC_FROZEN(double, rvv)
+#else
+XTR_ACC_D(rvv)
+#endif
 XTR_I64_FIELDS(XTR_ACC_I)
 
 static inline double LocalParticle_get_q0(LocalParticle* p) { return p->q0; }

@@ -49,6 +49,20 @@ static int flag_set(const xto_part* p, int bit) {
     return (int)((p->track_flags >> bit) & 1u);
 }
 
+/* Frozen longitudinal coordinates: the generated setters, adders and
+ * scalers of zeta, ptau, delta, rpp and rvv are no-ops
+ * (particles.py:185-225, FREEZE_VAR_<name>; line.py:4446-4469). */
+static int xto_frozen(const xto_part* p) { return flag_set(p, XTG_FLAG_FREEZE_LONGITUDINAL); }
+static void xto_set_zeta(xto_part* p, double v) { if (!xto_frozen(p)) p->zeta = v; }
+static void xto_add_to_zeta(xto_part* p, double v) { if (!xto_frozen(p)) p->zeta += v; }
+static void xto_set_energy(xto_part* p, double delta, double rvv, double rpp, double ptau) {
+    if (xto_frozen(p)) return;
+    p->delta = delta;
+    p->rvv = rvv;
+    p->ptau = ptau;
+    p->rpp = rpp;
+}
+
 /* ---------------------------------------------------------------------- */
 /* Energy variables: particles/local_particle_custom_api.h                */
 /* ---------------------------------------------------------------------- */
@@ -60,10 +74,7 @@ static void xto_update_ptau(xto_part* p, double new_ptau) {
     double const irpp = sqrt(ptau * ptau + 2 * ptau / beta0 + 1);
     double const new_rpp = 1. / irpp;
     double const new_rvv = irpp / (1 + beta0 * ptau);
-    p->delta = irpp - 1;
-    p->rvv = new_rvv;
-    p->ptau = ptau;
-    p->rpp = new_rpp;
+    xto_set_energy(p, irpp - 1, new_rvv, new_rpp, ptau);
 }
 
 /* local_particle_custom_api.h:195-217 */
@@ -94,7 +105,7 @@ static void xto_drift_expanded(xto_part* p, double length) {
     p->x += xp * length;
     p->y += yp * length;
     p->s += length;
-    p->zeta += length * dzeta;
+    xto_add_to_zeta(p, length * dzeta);
 }
 
 /* track_drift.h:26-42 */
@@ -107,7 +118,7 @@ static void xto_drift_exact(xto_part* p, double length) {
     double const dzeta = 1 - rv0v * opd * one_over_pz;
     p->x += px * one_over_pz * length;
     p->y += py * one_over_pz * length;
-    p->zeta += dzeta * length;
+    xto_add_to_zeta(p, dzeta * length);
     p->s += length;
 }
 
@@ -139,7 +150,7 @@ static void xto_drift_polar(xto_part* p, double length, double h) {
     p->x = new_x;
     p->px = new_px;
     p->y = new_y;
-    p->zeta += length - delta_ell / rvv;
+    xto_add_to_zeta(p, length - delta_ell / rvv);
     p->s += s;
 }
 
@@ -228,7 +239,7 @@ static void xto_drift_cf_expanded(xto_part* p, double length, double k0_,
     p->px = px_;
     p->y = y_;
     p->py = py_;
-    p->zeta += dzeta;
+    xto_add_to_zeta(p, dzeta);
     p->s += length;
 }
 
@@ -265,7 +276,7 @@ static void xto_drift_curved_exact_bend(xto_part* p, double length, double k0,
     p->x += delta_x;
     p->px = pxs;
     p->y = new_y;
-    p->zeta += length - delta_ell / rvv;
+    xto_add_to_zeta(p, length - delta_ell / rvv);
     p->s += s;
 }
 
@@ -290,7 +301,7 @@ static void xto_drift_straight_exact_bend(xto_part* p, double length, double k0)
     p->x = new_x;
     p->px = new_px;
     p->y = new_y;
-    p->zeta += length - delta_ell / rvv;
+    xto_add_to_zeta(p, length - delta_ell / rvv);
     p->s += s;
 }
 
@@ -455,7 +466,7 @@ static void xto_magnet_kick(xto_part* p, const xto_body* b, double kick_weight) 
     dpy += htot * chi * (b->k1_h_correction * length + k1l_mult) * kick_weight * x * y;
     p->px += dpx;
     p->py += dpy;
-    p->zeta += dzeta;
+    xto_add_to_zeta(p, dzeta);
 }
 
 /* track_magnet_kick.h:149-179 */
@@ -638,10 +649,8 @@ static void xto_update_delta(xto_part* p, double new_delta_value) {
     double const delta_beta0 = new_delta_value * beta0;
     double const ptau_beta0 = sqrt(delta_beta0 * delta_beta0 + 2 * delta_beta0 * beta0 + 1) - 1;
     double const one_plus_delta = 1 + new_delta_value;
-    p->delta = new_delta_value;
-    p->rvv = one_plus_delta / (1 + ptau_beta0);
-    p->rpp = 1 / one_plus_delta;
-    p->ptau = ptau_beta0 / beta0;
+    xto_set_energy(p, new_delta_value, one_plus_delta / (1 + ptau_beta0), 1 / one_plus_delta,
+                   ptau_beta0 / beta0);
 }
 
 /* local_particle_custom_api.h:248-256 */
@@ -650,7 +659,7 @@ static void xto_kill(xto_part* p, int64_t kill_state) {
     p->px = 1e30;
     p->y = 1e30;
     p->py = 1e30;
-    p->zeta = 1e30;
+    xto_set_zeta(p, 1e30);
     xto_update_delta(p, -1);
     p->state = kill_state;
 }
@@ -670,7 +679,7 @@ static void xto_yrotation(xto_part* p, double sin_angle, double cos_angle, doubl
     p->x = x_hat;
     p->px = px_hat;
     p->y = y_hat;
-    p->zeta = t_hat * beta0;
+    xto_set_zeta(p, t_hat * beta0);
 }
 
 /* track_dipole_fringe.h:16-82 (the MAD-NG form, the default build) */
@@ -719,7 +728,7 @@ static void xto_dipole_fringe(xto_part* p, double fint, double hgap, double k0) 
     p->x = new_x;
     p->y = new_y;
     p->py = new_py;
-    p->zeta = new_t * beta0;
+    xto_set_zeta(p, new_t * beta0);
 }
 
 /* track_mult_fringe.h:12-128 */
@@ -799,7 +808,7 @@ static void xto_mult_fringe(xto_part* p, const double* kn, const double* ks, int
     p->y += -fy * rpp;
     p->px = new_px;
     p->py = new_py;
-    p->zeta = (t + delta_t) * beta0;
+    xto_set_zeta(p, (t + delta_t) * beta0);
 }
 
 /* track_wedge.h:14-58 (no spin) */
@@ -829,7 +838,7 @@ static void xto_wedge(xto_part* p, double theta, double k0) {
     p->x = new_x;
     p->y += delta_y;
     p->px = new_px;
-    p->zeta += -delta_ell / rvv;
+    xto_add_to_zeta(p, -delta_ell / rvv);
 }
 
 /* track_wedge.h:60-82 */

@@ -396,6 +396,53 @@ def test_api_line_track_matches_oracle():
     compare(p2.to_numpy(), h2, 1e-14)
 
 
+@pytest.mark.parametrize("arith", ["exact", "fast"])
+@pytest.mark.parametrize("case", ["zoo", "fringe", "thick"])
+def test_freeze_longitudinal_matches_oracle(arith, case):
+    """XTG_FLAG_FREEZE_LONGITUDINAL against the oracle's freeze (itself
+    pinned to the reference's FREEZE_VAR build): zeta and the energy
+    variables keep their initial values bit for bit, the transverse motion
+    agrees as in the unfrozen tests."""
+    from lattice_cases import fringe_zoo
+    line, beam, turns = {"zoo": (element_zoo(), small_beam(256, seed=15, scale=0.3), 2),
+                         "fringe": (fringe_zoo(), small_beam(256, seed=19, scale=0.5), 2),
+                         "thick": (workloads.thick_ring(), small_beam(64, seed=43), 3)}[case]
+    recs, arrs, L = _setup(line, beam)
+    flags = 1 << _abi.FLAG_FREEZE_LONGITUDINAL
+    got, ref = _run_both(recs, arrs, L, arith=arith, num_turns=turns, track_flags=flags)
+    for f in ("zeta", "ptau", "delta", "rpp", "rvv"):
+        assert np.array_equal(got[f], arrs[f]), f
+    compare(got, ref, 5e-14 if arith == "exact" else 1e-10)
+
+
+def test_freeze_longitudinal_api():
+    """Line.track(freeze_longitudinal=True), Line.freeze_longitudinal and
+    the freeze_longitudinal context manager give the frozen oracle result;
+    unfreezing restores the normal push."""
+    line = workloads.toy_ring()
+    beam_kw = small_beam(500, p0c=450e9, seed=44)
+    host = pyoracle.host_arrays(xt.Particles(device="cpu", **beam_kw).to_numpy())
+    ref = {k: v.copy() for k, v in host.items()}
+    pyoracle.track(line._element_records(), ref, num_turns=4, line_length=line.get_length(),
+                   freeze_longitudinal=True)
+    line.build_tracker(device="cuda")
+    p1 = xt.Particles(device="cuda", **beam_kw)
+    line.track(p1, num_turns=4, freeze_longitudinal=True)
+    compare(p1.to_numpy(), ref, 1e-14)
+    p2 = xt.Particles(device="cuda", **beam_kw)
+    with xt.freeze_longitudinal(line):
+        line.track(p2, num_turns=4)
+    compare(p2.to_numpy(), ref, 1e-14)
+    line.freeze_longitudinal(True)
+    p3 = xt.Particles(device="cuda", **beam_kw)
+    line.track(p3, num_turns=4)
+    compare(p3.to_numpy(), ref, 1e-14)
+    line.freeze_longitudinal(False)
+    p4 = xt.Particles(device="cuda", **beam_kw)
+    line.track(p4, num_turns=4)
+    assert not np.array_equal(p4.to_numpy()["zeta"], host["zeta"])
+
+
 def test_backtrack_returns_to_start():
     """tests/test_magnet.py:62-110 of the reference: tracking forward then
     backward through a line gives back the initial coordinates."""

@@ -185,6 +185,7 @@ def test_turn_split(monkeypatch):
             self.line = line
             self.num_elements = len(line.element_names)
             self.track_flags = xt.TrackFlags()
+            self.frozen_longitudinal = False
             self.line_length = line.get_length()
             self.record_last_track = None
             self.time_last_track = None

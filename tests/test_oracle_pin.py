@@ -70,6 +70,29 @@ def test_fringe_zoo(flags):
         assert (a["state"] > 0).sum() > 50
 
 
+@pytest.mark.parametrize("flags", [0, 1 << 0, 1 << 2])
+@pytest.mark.parametrize("case", ["zoo", "fringe", "toy"])
+def test_freeze_longitudinal(case, flags):
+    """freeze_longitudinal: the restatement with its freeze flag equals the
+    reference's code compiled with the FREEZE_VAR set of freeze_longitudinal
+    bit for bit (cavities, curved and exact drifts, edges, kills), and
+    zeta, ptau, delta, rpp and rvv keep their initial values."""
+    line, beam = {"zoo": (element_zoo, small_beam(64, seed=3, scale=0.3)),
+                  "fringe": (fringe_zoo, small_beam(64, seed=9, scale=0.5)),
+                  "toy": (workloads.toy_ring, small_beam(300, p0c=450e9, seed=1))}[case]
+    line = line()
+    a, b = _both(line, beam, num_turns=3, track_flags=flags, freeze_longitudinal=True)
+    _assert_identical(a, b)
+    p0 = pyoracle.host_arrays(xt.Particles(device="cpu", **beam).to_numpy())
+    for f in ("zeta", "ptau", "delta", "rpp", "rvv"):
+        assert np.array_equal(a[f], p0[f]), f
+    moved = np.any(a["x"] != p0["x"])
+    assert moved
+    # without the freeze the same call changes the longitudinal coordinates
+    c, _ = _both(line, beam, num_turns=3, track_flags=flags)
+    assert np.any(c["zeta"] != p0["zeta"])
+
+
 @pytest.mark.parametrize("thin", [True, False])
 @pytest.mark.parametrize("flags", [0, 1])
 def test_sliced_lines(thin, flags):

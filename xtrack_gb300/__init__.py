@@ -12,7 +12,7 @@ from .elements import *  # noqa: F401,F403  (slice classes)
 from .monitors import (ParticlesMonitor, LastTurnsMonitor, BeamPositionMonitor, BeamSizeMonitor,
                        BeamProfileMonitor, MultiElementMonitor)
 from .slicing import Strategy, Teapot, Uniform
-from .line import Line, TrackerConfig
+from .line import Line, TrackerConfig, freeze_longitudinal
 from .tracker import Tracker, TrackFlags
 from .batch import BatchTracker
 from .tuning import autotune

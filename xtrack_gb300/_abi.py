@@ -51,6 +51,7 @@ FLAG_BACKTRACK = 0
 FLAG_KILL_CAVITY_KICK = 2
 FLAG_IGNORE_GLOBAL_APERTURE = 3
 FLAG_IGNORE_LOCAL_APERTURE = 4
+FLAG_FREEZE_LONGITUDINAL = 32
 
 ARITH_EXACT = 0
 ARITH_FAST = 1

@@ -42,6 +42,7 @@ class BatchTracker(Tracker):
         self.device = first.device
         self._lib = first._lib
         self.track_flags = first.track_flags
+        self.frozen_longitudinal = False
         self.num_elements = n0
         self._records = None
         self._cfg = first._cfg

@@ -36,11 +36,29 @@ struct PState {
     double ax, ay;
     int64_t state, at_element, at_turn;
     bool chi_one;     // chi == 1: per-element products precomputed at chi = 1 apply
+    bool frozen;      // longitudinal coordinates frozen (zeta, ptau, delta, rpp, rvv)
 };
 
 XTG_DEV void refresh_energy_cache(PState& p) {
     p.rv0v = 1. / p.rvv;
     p.opd = 1. + p.delta;
+}
+
+// The reference's generated setters, adders and scalers of a frozen
+// variable are no-ops (particles.py:185-225, FREEZE_VAR_<name>); with the
+// longitudinal coordinates frozen, every write to zeta and to the energy
+// variables leaves the old value, and later reads in the same element see
+// it.
+XTG_DEV void set_zeta(PState& p, double v) {
+    if (!p.frozen) p.zeta = v;
+}
+XTG_DEV void set_energy(PState& p, double delta, double rvv, double rpp, double ptau) {
+    if (!p.frozen) {
+        p.delta = delta;
+        p.rvv = rvv;
+        p.rpp = rpp;
+        p.ptau = ptau;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -57,7 +75,7 @@ XTG_DEV void drift_expanded(PState& p, double length) {
         p.x = p.x + xp * length;
         p.y = p.y + yp * length;
         p.s = p.s + length;
-        p.zeta = p.zeta + length * dzeta;
+        set_zeta(p, p.zeta + length * dzeta);
     } else {
         // the reference's grouping, contracted as its FMA build contracts
         // it: 1 + (xp^2 + yp^2)/2 is rounded before the product with 1/rvv
@@ -69,7 +87,7 @@ XTG_DEV void drift_expanded(PState& p, double length) {
         double const dzeta = fma(-p.rv0v, fma(t, 0.5, 1.0), 1.0);
         p.x = fma(xp, length, p.x);
         p.y = fma(yp, length, p.y);
-        p.zeta = fma(length, dzeta, p.zeta);
+        set_zeta(p, fma(length, dzeta, p.zeta));
         p.s = p.s + length;
     }
 }
@@ -84,7 +102,7 @@ XTG_DEV void drift_exact(PState& p, double length) {
         double const dzeta = 1 - p.rv0v * opd * one_over_pz;
         p.x = p.x + px * one_over_pz * length;
         p.y = p.y + py * one_over_pz * length;
-        p.zeta = p.zeta + dzeta * length;
+        set_zeta(p, p.zeta + dzeta * length);
         p.s = p.s + length;
     } else {
         double const pz2 = fma(-py, py, fma(-px, px, opd * opd));
@@ -93,7 +111,7 @@ XTG_DEV void drift_exact(PState& p, double length) {
         double const fl = one_over_pz * length;
         p.x = fma(px, fl, p.x);
         p.y = fma(py, fl, p.y);
-        p.zeta = fma(dzeta, length, p.zeta);
+        set_zeta(p, fma(dzeta, length, p.zeta));
         p.s = p.s + length;
     }
 }
@@ -119,7 +137,7 @@ XTG_DEV void drift_polar(PState& p, double length, double h) {
     p.x = new_x;
     p.px = new_px;
     p.y = new_y;
-    p.zeta = p.zeta + (length - delta_ell / p.rvv);
+    set_zeta(p, p.zeta + (length - delta_ell / p.rvv));
     p.s = p.s + s;
 }
 
@@ -191,7 +209,7 @@ XTG_DEV void drift_cf_expanded(PState& p, double length, double k0_, double k1_,
     p.px = px_;
     p.y = y_;
     p.py = py_;
-    p.zeta = p.zeta + dzeta;
+    set_zeta(p, p.zeta + dzeta);
     p.s = p.s + length;
 }
 
@@ -215,7 +233,7 @@ XTG_DEV void drift_straight_exact_bend(PState& p, double length, double k0) {
     p.x = new_x;
     p.px = new_px;
     p.y = new_y;
-    p.zeta = p.zeta + (length - delta_ell / p.rvv);
+    set_zeta(p, p.zeta + (length - delta_ell / p.rvv));
     p.s = p.s + s;
 }
 
@@ -250,7 +268,7 @@ XTG_DEV void drift_curved_exact_bend(PState& p, double length, double k0, double
     p.x = p.x + delta_x;
     p.px = pxs;
     p.y = new_y;
-    p.zeta = p.zeta + (length - delta_ell / p.rvv);
+    set_zeta(p, p.zeta + (length - delta_ell / p.rvv));
     p.s = p.s + s;
 }
 
@@ -436,7 +454,7 @@ XTG_DEV void apply_kick(PState& p, const KickArgs& a, const double* __restrict__
             }
             p.px = p.px + dpx;
             p.py = p.py + dpy;
-            p.zeta = p.zeta + dzeta;
+            set_zeta(p, p.zeta + dzeta);
         }
     } else {
         // merged polynomial sum_i (cn_i + i cs_i) z^i, z = x + i y; the
@@ -467,7 +485,7 @@ XTG_DEV void apply_kick(PState& p, const KickArgs& a, const double* __restrict__
             if (curv & 1) {
                 double const hl = a.hl;
                 p.px = fma(hl, p.opd, p.px);
-                p.zeta = fma(-p.rv0v * hl, x, p.zeta);
+                set_zeta(p, fma(-p.rv0v * hl, x, p.zeta));
             }
             if (curv & 2) p.px = fma(p.chi_one ? a.C0 : chi * a.C0, x, p.px);
             if (curv & 4) {
@@ -498,10 +516,8 @@ XTG_DEV void set_delta_and_energy(PState& p, double new_delta) {
     double const beta0 = p.beta0;
     double const delta_beta0 = new_delta * beta0;
     double const ptau_beta0 = sqrt(delta_beta0 * delta_beta0 + 2. * delta_beta0 * beta0 + 1.) - 1.;
-    p.delta = new_delta;
-    p.rvv = (1. + new_delta) / (1. + ptau_beta0);
-    p.rpp = 1. / (1. + new_delta);
-    p.ptau = ptau_beta0 / beta0;
+    set_energy(p, new_delta, (1. + new_delta) / (1. + ptau_beta0), 1. / (1. + new_delta),
+               ptau_beta0 / beta0);
 }
 
 // local_particle_custom_api.h:248-256
@@ -510,7 +526,7 @@ XTG_DEV void kill_particle(PState& p, int64_t kill_state) {
     p.px = 1e30;
     p.y = 1e30;
     p.py = 1e30;
-    p.zeta = 1e30;
+    set_zeta(p, 1e30);
     set_delta_and_energy(p, -1.);
     refresh_energy_cache(p);
     p.state = kill_state;
@@ -531,7 +547,7 @@ XTG_DEV void y_rotation(PState& p, double sin_a, double cos_a, double tan_a) {
     p.x = x_hat;
     p.px = px_hat;
     p.y = y_hat;
-    p.zeta = t_hat * beta0;
+    set_zeta(p, t_hat * beta0);
 }
 
 // track_dipole_fringe.h:16-82 (MAD-NG form)
@@ -580,7 +596,7 @@ XTG_DEV void dipole_fringe(PState& p, double fint, double hgap, double k0) {
     p.x = new_x;
     p.y = new_y;
     p.py = new_py;
-    p.zeta = new_t * beta0;
+    set_zeta(p, new_t * beta0);
 }
 
 // track_mult_fringe.h:12-128 with k_order = 3, min_order = 1
@@ -659,7 +675,7 @@ XTG_DEV void mult_fringe(PState& p, const double* kn, const double* ks, const do
     p.y = p.y + -fy * rpp;
     p.px = new_px;
     p.py = new_py;
-    p.zeta = (t + delta_t) * beta0;
+    set_zeta(p, (t + delta_t) * beta0);
 }
 
 // track_wedge.h:14-58 (spin off); the trigonometric values of theta come
@@ -687,7 +703,7 @@ XTG_DEV void wedge(PState& p, double theta, double sin_t, double cos_t, double t
     p.x = new_x;
     p.y = p.y + delta_y;
     p.px = new_px;
-    p.zeta = p.zeta + -delta_ell / rvv;
+    set_zeta(p, p.zeta + -delta_ell / rvv);
 }
 
 // track_wedge.h:60-82
@@ -835,12 +851,10 @@ XTG_DEV void add_to_energy(PState& p, double delta_energy, bool pz_only) {
     double const irpp = sqrt(ptau * ptau + 2 * ptau / beta0 + 1);
     double const new_rpp = 1. / irpp;
     double const new_rvv = irpp / (1 + beta0 * ptau);
-    p.delta = irpp - 1;
-    p.rvv = new_rvv;
-    p.ptau = ptau;
-    p.rpp = new_rpp;
+    set_energy(p, irpp - 1, new_rvv, new_rpp, ptau);
     if (!pz_only) {
-        double const f = old_rpp / new_rpp;
+        // the reference reads rpp back (frozen: unchanged, f = 1)
+        double const f = old_rpp / p.rpp;
         p.px = p.px * f;
         p.py = p.py * f;
     }

@@ -567,6 +567,7 @@ __global__ void __launch_bounds__(kExact ? XTG_EXACT_LB_THREADS : XTG_FAST_LB_TH
             p.at_element = P.at_element[i];
             p.at_turn = P.at_turn[i];
             p.chi_one = (p.chi == 1.0);
+            p.frozen = flag_on(a.track_flags, XTG_FLAG_FREEZE_LONGITUDINAL);
             refresh_energy_cache(p);
             if (a.load_pid) pid = P.particle_id[i];
         }

@@ -8,6 +8,8 @@ Covers ``Line(elements=..., element_names=...)`` (line.py:144-351),
 (line.py:6817-6851), plus ``to_dict`` / ``from_dict`` for the elements built
 here.
 """
+import contextlib
+
 import numpy as np
 
 from . import _abi
@@ -133,6 +135,17 @@ class Line:
     def discard_tracker(self):
         self.tracker = None
 
+    def freeze_longitudinal(self, state=True):
+        """Freezes (True) or unfreezes (False) the longitudinal coordinates
+        zeta, ptau, delta, rpp and rvv in every following track call
+        (line.py:4446-4469: the tracker's FREEZE_VAR_<name> config, whose
+        setters become no-ops)."""
+        if state not in (True, False):
+            raise ValueError("state must be True or False")
+        if not self._has_valid_tracker():
+            self.build_tracker()
+        self.tracker.frozen_longitudinal = state
+
     def _has_valid_tracker(self):
         return self.tracker is not None and self.tracker.num_elements == len(self.element_names)
 
@@ -221,3 +234,20 @@ def _element_length(e):
     if getattr(e, "isthick", False):
         return float(getattr(e, "length", 0.0))
     return 0.0
+
+
+@contextlib.contextmanager
+def freeze_longitudinal(line_or_tracker):
+    """Context manager that freezes the longitudinal coordinates of a line
+    (or tracker) and restores the previous state on exit (line.py:7673-7684)."""
+    tr = line_or_tracker
+    if isinstance(line_or_tracker, Line):
+        if not line_or_tracker._has_valid_tracker():
+            line_or_tracker.build_tracker()
+        tr = line_or_tracker.tracker
+    previous = tr.frozen_longitudinal
+    tr.frozen_longitudinal = True
+    try:
+        yield None
+    finally:
+        tr.frozen_longitudinal = previous

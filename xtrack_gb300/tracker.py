@@ -62,6 +62,9 @@ class Tracker:
                                f"(got device {self.device})")
         self._lib = _abi.load_library()
         self.track_flags = TrackFlags()
+        # Line.freeze_longitudinal(True): every call freezes zeta, ptau,
+        # delta, rpp and rvv (the reference's FREEZE_VAR_<name> config)
+        self.frozen_longitudinal = False
         self.num_elements = len(line.element_names)
         self._records = line._element_records()
         cfg = line.config
@@ -184,14 +187,12 @@ class Tracker:
                turn_by_turn_monitor=None, freeze_longitudinal=False, time=False,
                with_progress=False, backtrack=False, _force_no_end_turn_actions=False,
                multi_element_monitor_at=None):
-        if freeze_longitudinal:
-            raise NotImplementedError("freeze_longitudinal is not supported")
         if particles.device.type != "cuda":
             raise RuntimeError("particles must live on a CUDA device")
         if with_progress:
             return self._track_with_progress(particles, ele_start, ele_stop, num_elements,
                                              num_turns, turn_by_turn_monitor, time,
-                                             with_progress, backtrack)
+                                             with_progress, backtrack, freeze_longitudinal)
         t0 = None
         if time:
             torch.cuda.synchronize(particles.device)
@@ -263,6 +264,8 @@ class Tracker:
         flags = self.track_flags.get_flags_register()
         if backtrack:
             flags = np.uint64(int(flags) | (1 << _abi.FLAG_BACKTRACK))
+        if freeze_longitudinal or self.frozen_longitudinal:
+            flags = np.uint64(int(flags) | (1 << _abi.FLAG_FREEZE_LONGITUDINAL))
 
         mem = self._get_multi_element_monitor(multi_element_monitor_at, particles, monitor_turns)
         pstruct = particles._xtg_struct()
@@ -291,7 +294,8 @@ class Tracker:
         return None
 
     def _track_with_progress(self, particles, ele_start, ele_stop, num_elements, num_turns,
-                             turn_by_turn_monitor, time, with_progress, backtrack):
+                             turn_by_turn_monitor, time, with_progress, backtrack,
+                             freeze_longitudinal=False):
         """tracker.py:313-381: batches of turns, same result as one call."""
         if turn_by_turn_monitor not in (None, False):
             raise NotImplementedError("with_progress together with a monitor is not supported")
@@ -305,7 +309,7 @@ class Tracker:
         while done < num_turns:
             n = min(batch, num_turns - done)
             self._track(particles, ele_start=ele_start if first else 0, num_turns=n,
-                        backtrack=backtrack)
+                        backtrack=backtrack, freeze_longitudinal=freeze_longitudinal)
             first = False
             done += n
         if time:
