@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define XTG_ABI_VERSION 2
+#define XTG_ABI_VERSION 3
 
 /* Maximum number of multipole coefficients per array (order <= 20). */
 #define XTG_MAX_KNL 21
@@ -58,7 +58,8 @@ extern "C" {
 #define XTG_CLS_LIMIT_RECT      9   /* limit_rect.py, limitrect.h            */
 #define XTG_CLS_MONITOR        10   /* monitors/*.py placed in the line      */
 #define XTG_CLS_LIMIT_POLYGON  11   /* limit_polygon.py, limitpolygon.h      */
-#define XTG_NUM_CLS            12
+#define XTG_CLS_DIPOLE_EDGE    12   /* dipole_edge.py, dipoleedge.h          */
+#define XTG_NUM_CLS            13
 
 /* Slice kind of a record (slice classes of slice_elements_*.py). A slice
  * record carries its parent's parameters plus its own `weight`. */
@@ -130,6 +131,12 @@ typedef struct xtg_element {
      *                          lattice's lifetime);
      *   XTG_CLS_LIMIT_POLYGON  an xtg_polygon (vertices copied). */
     uint64_t aux;
+    /* DipoleEdge: k, e1, hgap, fint and the linear coefficients r21, r43 as
+     * the class computes them (_update_r21_r43 from k, e1, e1_fd, hgap,
+     * fint); side 0 entry, 1 exit; `model` 0 linear, 1 full, -1 suppressed. */
+    double k, e1, hgap, fint, r21, r43;
+    int32_t side;
+    int32_t reserved_dipole_edge;
 } xtg_element;
 
 /* Vertices of a LimitPolygon aperture (limit_polygon.py), host arrays. */

@@ -207,6 +207,15 @@ XTR_CLASS(ThinSliceOctupoleEntry) XTR_CLASS(ThinSliceOctupoleExit)
 XTR_CLASS(ThickSliceMultipole) XTR_CLASS(ThinSliceMultipole) XTR_CLASS(DriftSliceMultipole)
 XTR_CLASS(ThickSliceCavity) XTR_CLASS(ThinSliceCavity) XTR_CLASS(DriftSliceCavity)
 
+/* DipoleEdge (dipole_edge.py _xofields): r21, r43 as the class computes
+ * them, the full model's k, e1, fint, hgap, side; model 0/1/-1. */
+typedef const xtg_element* DipoleEdgeData;
+XTR_GET_D(DipoleEdge, r21, el->r21) XTR_GET_D(DipoleEdge, r43, el->r43)
+XTR_GET_D(DipoleEdge, k, el->k) XTR_GET_D(DipoleEdge, e1, el->e1)
+XTR_GET_D(DipoleEdge, fint, el->fint) XTR_GET_D(DipoleEdge, hgap, el->hgap)
+XTR_GET_D(DipoleEdge, delta_taper, 0.)
+XTR_GET_I(DipoleEdge, model, el->model) XTR_GET_I(DipoleEdge, side, el->side)
+
 /* ---- the reference's element code, compiled as-is --------------------- */
 #include "xtrack/headers/constants.h"
 #include "xtrack/headers/particle_states.h"
@@ -220,6 +229,7 @@ XTR_CLASS(ThickSliceCavity) XTR_CLASS(ThinSliceCavity) XTR_CLASS(DriftSliceCavit
 #include "xtrack/beam_elements/elements_src/cavity.h"
 #include "xtrack/beam_elements/elements_src/limitellipse.h"
 #include "xtrack/beam_elements/elements_src/limitrect.h"
+#include "xtrack/beam_elements/elements_src/dipoleedge.h"
 #include "xtrack/beam_elements/elements_src/thick_slice_bend.h"
 #include "xtrack/beam_elements/elements_src/thin_slice_bend.h"
 #include "xtrack/beam_elements/elements_src/drift_slice_bend.h"
@@ -265,6 +275,7 @@ static int xtr_apply(const xtg_element* e, LocalParticle* lp) {
     case XTG_CLS_DRIFT: Drift_track_local_particle(e, lp); return 1;
     case XTG_CLS_LIMIT_ELLIPSE: LimitEllipse_track_local_particle(e, lp); return 0;
     case XTG_CLS_LIMIT_RECT: LimitRect_track_local_particle(e, lp); return 0;
+    case XTG_CLS_DIPOLE_EDGE: DipoleEdge_track_local_particle(e, lp); return 0;
     case XTG_CLS_MULTIPOLE: XTR_SLICES(Multipole, 0) return 0;
     case XTG_CLS_BEND: XTR_EDGES(Bend) XTR_SLICES(Bend, 1) return 0;
     case XTG_CLS_QUADRUPOLE: XTR_EDGES(Quadrupole) XTR_SLICES(Quadrupole, 1) return 0;

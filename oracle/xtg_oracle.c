@@ -1446,6 +1446,42 @@ static int xto_apply(const xtg_element* e, const xtg_config* cfg, xto_part* p,
         }
         return 0;
     }
+    case XTG_CLS_DIPOLE_EDGE: {
+        /* dipoleedge.h:14-71 (no synchrotron-radiation taper) */
+        if (e->model == 0) {
+            double r21 = e->r21, r43 = e->r43;
+            if (backtrack) {
+                r21 = -r21;
+                r43 = -r43;
+            }
+            /* track_dipole_edge_linear.h:29-37 */
+            double const x = p->x, y = p->y, chi = p->chi;
+            p->px += chi * r21 * x;
+            p->py += chi * r43 * y;
+        } else if (e->model == 1) {
+            if (backtrack) {
+                xto_kill(p, -32);
+                return 0;
+            }
+            /* track_dipole_edge_nonlinear.h:9-44 */
+            double sin_, cos_, tan_;
+            if (fabs(e->e1) < 10e-10) {
+                sin_ = -999.0; cos_ = -999.0; tan_ = -999.0;
+            } else {
+                sin_ = sin(e->e1); cos_ = cos(e->e1); tan_ = tan(e->e1);
+            }
+            if (e->side == 0) {
+                if (sin_ > -99.) xto_yrotation(p, -sin_, cos_, -tan_);
+                xto_dipole_fringe(p, e->fint, e->hgap, e->k);
+                if (sin_ > -99.) xto_wedge(p, -e->e1, e->k);
+            } else {
+                if (sin_ > -99.) xto_wedge(p, -e->e1, e->k);
+                xto_dipole_fringe(p, e->fint, e->hgap, -e->k);
+                if (sin_ > -99.) xto_yrotation(p, -sin_, cos_, -tan_);
+            }
+        }
+        return 0;
+    }
     case XTG_CLS_LIMIT_RECT: {
         /* limitrect.h:9-36 */
         if (flag_set(p, XTG_FLAG_IGNORE_LOCAL_APERTURE)) return 0;
@@ -1611,6 +1647,9 @@ int32_t xto_validate(const xtg_element* els, int64_t n, char* msg, int64_t msg_l
             int64_t model = e->model == 0 ? 6 : e->model;
             if (!(model == -1 || model == 4 || model == 5 || model == 6))
                 why = "unsupported cavity model";
+        } else if (e->cls == XTG_CLS_DIPOLE_EDGE) {
+            if (e->model < -1 || e->model > 1) why = "unknown DipoleEdge model (linear, full, suppressed)";
+            else if (e->side != 0 && e->side != 1) why = "DipoleEdge side must be 0 (entry) or 1 (exit)";
         }
         if (why) {
             if (msg && msg_len > 0) snprintf(msg, (size_t)msg_len, "element %lld: %s", (long long)i, why);
@@ -1932,6 +1971,8 @@ int32_t xto_abi_sizes(int64_t* out) {
     out[7] = (int64_t)sizeof(xtg_element_monitor);
     out[8] = (int64_t)offsetof(xtg_element_monitor, particles);
     out[9] = (int64_t)offsetof(xtg_element, aux);
+    out[10] = (int64_t)offsetof(xtg_element, r21);
+    out[11] = (int64_t)offsetof(xtg_element, side);
     return 4;
 }
 

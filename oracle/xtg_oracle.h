@@ -43,9 +43,9 @@ int32_t xto_track(const xtg_element* elements, int64_t n_elements,
                   int32_t mode, int32_t num_threads);
 
 /* sizeof / offsetof of the C-ABI structs (layout check of foreign mirrors):
- * out[0..9] = element, particles, monitor, config sizes; offsets of
+ * out[0..11] = element, particles, monitor, config sizes; offsets of
  * element.knl, element.shift_x, monitor.data; element-monitor size, its
- * offset of particles, element.monitor offset. */
+ * offset of particles; offsets of element.aux, element.r21, element.side. */
 int32_t xto_abi_sizes(int64_t* out);
 
 /* Multi-element monitor applied by the following xto_track calls (NULL

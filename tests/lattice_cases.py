@@ -66,6 +66,11 @@ def element_zoo(seed=3):
     add("cav_thick", xt.Cavity(voltage=2e6, frequency=400e6, lag=170.0, length=0.5,
                                num_kicks=3))
     add("cav_abs", xt.Cavity(voltage=1e6, frequency=100e6, lag=180.0, absolute_time=1))
+    add("de_in", xt.DipoleEdge(k=2e-3, e1=0.01, hgap=0.03, fint=0.5))
+    add("de_out", xt.DipoleEdge(k=2e-3, e1=-0.004, e1_fd=1e-3, hgap=0.03, fint=0.4,
+                                side="exit"))
+    add("de_zero", xt.DipoleEdge(k=1e-3))
+    add("de_off", xt.DipoleEdge(k=5e-3, e1=0.02, model="suppressed"))
     add("ell", xt.LimitEllipse(a=0.03, b=0.02))
     add("rect", xt.LimitRect(min_x=-0.03, max_x=0.028, min_y=-0.02, max_y=0.021))
     return xt.Line(elements=els, element_names=names)
@@ -111,6 +116,11 @@ def fringe_zoo(seed=5):
                                 edge_exit_active=True, num_multipole_kicks=3))
     add("o_edges", xt.Octupole(length=0.3, k3=2.0, k3s=0.5, edge_exit_active=True,
                                num_multipole_kicks=2, integrator="teapot"))
+    # DipoleEdge full model: entry, a face angle below 1e-9 (no rotation), exit
+    add("de_full_in", xt.DipoleEdge(k=3e-3, e1=0.015, hgap=0.03, fint=0.5, model="full"))
+    add("de_full_flat", xt.DipoleEdge(k=3e-3, e1=5e-10, hgap=0.03, fint=0.5, model="full"))
+    add("de_full_out", xt.DipoleEdge(k=3e-3, e1=0.015, hgap=0.03, fint=0.5, model="full",
+                                     side="exit"))
     add("d_end", xt.Drift(length=0.4))
     return xt.Line(elements=els, element_names=names)
 

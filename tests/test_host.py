@@ -34,14 +34,14 @@ def test_library_exports_every_declared_entry_point():
     assert len(names) >= 10
     for n in names:
         assert hasattr(lib, n), f"{n} declared in the header but not exported"
-    assert lib.xtg_abi_version() == 2
+    assert lib.xtg_abi_version() == 3
     assert set(names) == set(_abi.EXPORTED_SYMBOLS)
 
 
 def test_ctypes_layout_matches_c():
     pyoracle.ensure_built(with_ref=False)
     lib = pyoracle._load(pyoracle.ORACLE_LIB, "oracle")
-    out = (ctypes.c_int64 * 10)()
+    out = (ctypes.c_int64 * 12)()
     lib.xto_abi_sizes(out)
     assert out[0] == ctypes.sizeof(_abi.XtgElement) == _abi.ELEMENT_DTYPE.itemsize
     assert out[1] == ctypes.sizeof(_abi.XtgParticles)
@@ -53,6 +53,8 @@ def test_ctypes_layout_matches_c():
     assert out[7] == ctypes.sizeof(_abi.XtgElementMonitor)
     assert out[8] == _abi.XtgElementMonitor.particles.offset
     assert out[9] == _abi.XtgElement.aux.offset
+    assert out[10] == _abi.XtgElement.r21.offset
+    assert out[11] == _abi.XtgElement.side.offset
 
 
 @pytest.mark.parametrize("element,msg", [

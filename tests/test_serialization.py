@@ -13,10 +13,11 @@ import pyoracle
 import xtrack_gb300 as xt
 from xtrack_gb300 import serialization as ser
 from xtrack_gb300 import workloads
-from lattice_cases import element_zoo, sliced_line
+from lattice_cases import element_zoo, fringe_zoo, sliced_line
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LHC = os.path.join(HERE, "golden", "lhc", "hllhc14_thin_64p_10t.npz")
+SPS = os.path.join(HERE, "golden", "sps", "sps_thin_128p_20t.npz")
 
 
 def _same_records(a, b):
@@ -38,7 +39,7 @@ def _with_polygon():
 
 
 @pytest.mark.parametrize("factory", [workloads.toy_ring, element_zoo, lambda: sliced_line(True),
-                                     _with_polygon,
+                                     _with_polygon, fringe_zoo,
                                      lambda: sliced_line(False),
                                      lambda: workloads.thick_ring(n_arcs=1, n_cells=2)])
 def test_dict_and_json_round_trip(factory, tmp_path):
@@ -91,8 +92,31 @@ def test_out_of_scope_fields_are_rejected(bad):
         ser.element_from_dict(bad, "e")
 
 
-def _lhc():
-    d = np.load(LHC)
+def test_dipole_edge_dicts():
+    """DipoleEdge as the reference writes it (nonzero scalars, model and
+    side by name) and in its older form (h for k, stored r21/r43, which are
+    recomputed): the same element and record."""
+    new = ser.element_from_dict({"__class__": "DipoleEdge", "k": 0.0013490601351007177,
+                                 "e1": 0.004222570771, "hgap": 0.02, "fint": 0.5,
+                                 "model": "full", "side": "exit"})
+    old = ser.element_from_dict({"__class__": "DipoleEdge", "h": 0.0013490601351007177,
+                                 "e1": 0.004222570771, "hgap": 0.02, "fint": 0.5,
+                                 "r21": 1.0, "r43": 2.0, "model": "full", "side": "exit"})
+    assert new.model == old.model == "full" and new.side == old.side == "exit"
+    assert new.r21 == old.r21 and new.r43 == old.r43 and new.r21 != 1.0
+    rec = new.to_record()
+    assert rec["model"] == 1 and rec["side"] == 1 and rec["r21"] == new.r21
+    assert ser.element_to_dict(new) == {"__class__": "DipoleEdge", "k": new.k, "e1": new.e1,
+                                        "hgap": 0.02, "fint": 0.5, "model": "full",
+                                        "side": "exit"}
+    # changing a parameter recomputes the linear coefficients
+    r43 = new.r43
+    new.fint = 0.7
+    assert new.r43 != r43
+
+
+def _fixture(path):
+    d = np.load(path)
     meta = json.loads(str(d["meta"]))
     recs = d["records"]
     arrs = pyoracle.host_arrays({k[3:]: d[k].copy() for k in d.files if k.startswith("in_")})
@@ -101,7 +125,7 @@ def _lhc():
 
 
 def test_lhc_fixture_oracle_reproduces_reference():
-    recs, arrs, out, meta = _lhc()
+    recs, arrs, out, meta = _fixture(LHC)
     assert meta["n_elements"] == len(recs) == 11603
     pyoracle.track(recs, arrs, line_length=meta["line_length"], num_turns=meta["num_turns"],
                    q0=meta["q0"], mass0=meta["mass0"])
@@ -116,7 +140,7 @@ def test_lhc_fixture_gpu(arith):
     reference-compiled result after 10 turns: exact within 1e-14, fast
     within 3x the reference's own FMA spread."""
     from xtg_testutil import compare, compare_within_spread, fma_spread, gpu_track
-    recs, arrs, out, meta = _lhc()
+    recs, arrs, out, meta = _fixture(LHC)
     kw = dict(line_length=meta["line_length"], num_turns=meta["num_turns"], q0=meta["q0"],
               mass0=meta["mass0"])
     got, _ = gpu_track(recs, {k: v.copy() for k, v in arrs.items()}, arith=arith, **kw)
@@ -125,5 +149,39 @@ def test_lhc_fixture_gpu(arith):
     else:
         for f in ("state", "at_turn", "at_element"):
             assert np.array_equal(got[f], out[f]), f
+        spread, ok = fma_spread(recs, arrs, **kw)
+        compare_within_spread(got, out, spread, ok)
+
+
+def test_sps_fixture_oracle_reproduces_reference():
+    """The thin SPS line (8199 elements: drifts, thin multipoles, 1488
+    DipoleEdges, 1698 LimitRect/LimitEllipse apertures, cavities) after 20
+    turns of the reference-compiled code, with real aperture losses."""
+    recs, arrs, out, meta = _fixture(SPS)
+    assert meta["n_elements"] == len(recs) == 8199
+    assert np.sum(out["state"] <= 0) > 5
+    pyoracle.track(recs, arrs, line_length=meta["line_length"], num_turns=meta["num_turns"],
+                   q0=meta["q0"], mass0=meta["mass0"])
+    for k, v in out.items():
+        assert np.array_equal(arrs[k], v), k
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("arith", ["exact", "fast"])
+def test_sps_fixture_gpu(arith):
+    """The real SPS line on the GPU against the reference-compiled result:
+    state, at_turn and at_element of every aperture loss bit-exact;
+    coordinates within 1e-14 (exact) or 3x the reference's FMA spread
+    (fast)."""
+    from xtg_testutil import compare, compare_within_spread, fma_spread, gpu_track
+    recs, arrs, out, meta = _fixture(SPS)
+    kw = dict(line_length=meta["line_length"], num_turns=meta["num_turns"], q0=meta["q0"],
+              mass0=meta["mass0"])
+    got, _ = gpu_track(recs, {k: v.copy() for k, v in arrs.items()}, arith=arith, **kw)
+    for f in ("state", "at_turn", "at_element"):
+        assert np.array_equal(got[f], out[f]), f
+    if arith == "exact":
+        compare(got, out, 1e-14)
+    else:
         spread, ok = fma_spread(recs, arrs, **kw)
         compare_within_spread(got, out, spread, ok)

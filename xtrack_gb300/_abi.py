@@ -39,6 +39,7 @@ CLS_LIMIT_ELLIPSE = 8
 CLS_LIMIT_RECT = 9
 CLS_MONITOR = 10
 CLS_LIMIT_POLYGON = 11
+CLS_DIPOLE_EDGE = 12
 
 SLICE_NONE = 0
 SLICE_THICK = 1
@@ -99,6 +100,9 @@ class XtgElement(ctypes.Structure):
         ("rot_x_rad", ctypes.c_double), ("rot_y_rad", ctypes.c_double),
         ("rot_s_rad", ctypes.c_double), ("rot_s_rad_no_frame", ctypes.c_double),
         ("aux", ctypes.c_uint64),
+        ("k", ctypes.c_double), ("e1", ctypes.c_double), ("hgap", ctypes.c_double),
+        ("fint", ctypes.c_double), ("r21", ctypes.c_double), ("r43", ctypes.c_double),
+        ("side", ctypes.c_int32), ("reserved_dipole_edge", ctypes.c_int32),
     ]
 
 
@@ -308,7 +312,7 @@ def load_library(path=None):
     lib.xtg_measure_fp64_peak.restype = c.c_int32
     lib.xtg_check_bounded_wait.argtypes = [c.c_int64]
     lib.xtg_check_bounded_wait.restype = c.c_int32
-    if lib.xtg_abi_version() != 2:
+    if lib.xtg_abi_version() != 3:
         raise RuntimeError("xtrack_gb300: ABI version mismatch")
     if path == LIB_PATH:
         _lib = lib

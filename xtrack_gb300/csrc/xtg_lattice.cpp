@@ -289,6 +289,42 @@ void edge_linear(const MagnetIn& m, bool exit, double factor_knl_ksl_edge,
     *r43 = r43_out * factor_for_backtrack;
 }
 
+// DipoleEdge full model (track_dipole_edge_nonlinear.h:9-44) in the
+// dipole-only layout that fringe_edge runs: y-rotation by the face angle
+// (skipped below 1e-9 rad, as the reference's sentinel test does), dipole
+// fringe with k (-k at the exit), wedge by -e1 with k. The trigonometric
+// values are evaluated here with the libm calls the reference makes.
+std::vector<double> dipole_edge_fringe_block(const xtg_element& e) {
+    std::vector<double> fr(FR_KNL, 0.0);
+    bool const exit = e.side == 1;
+    fr[FR_MODEL] = 2;
+    fr[FR_IS_EXIT] = exit ? 1.0 : 0.0;
+    fr[FR_K0] = exit ? -e.k : e.k;
+    fr[FR_FINT] = e.fint;
+    fr[FR_HGAP] = e.hgap;
+    fr[FR_FACE_ANGLE] = e.e1;
+    if (!(std::fabs(e.e1) < 10e-10)) {
+        fr[FR_ROTATE] = 1.0;
+        fr[FR_SIN] = std::sin(e.e1);
+        fr[FR_COS] = std::cos(e.e1);
+        fr[FR_TAN] = std::tan(e.e1);
+    } else {
+        fr[FR_ROTATE] = 0.0;
+        fr[FR_SIN] = 0.0;
+        fr[FR_COS] = 1.0;
+        fr[FR_TAN] = 0.0;
+    }
+    double const theta = -e.e1;
+    fr[FR_WSIN] = std::sin(theta);
+    fr[FR_WCOS] = std::cos(theta);
+    fr[FR_WTAN] = std::tan(theta);
+    fr[FR_WSIN2] = std::sin(2 * theta);
+    fr[FR_LENGTH] = 0.0;
+    fr[FR_KL_ORDER] = -1.0;
+    fr[FR_KNORM] = e.k;
+    return fr;
+}
+
 // Parameter block of one nonlinear edge (track_magnet_edge.h:40-50 for the
 // fringe's k0, 83-158 for the rest); layout FR_* of xtg_table.h. The
 // trigonometric values of the face angle are evaluated here once, with the
@@ -410,6 +446,10 @@ int32_t validate_element(const xtg_element& e, int64_t idx, std::string* why) {
             return fail("Cavity has no entry/exit slices");
     } else if (e.slice != XTG_SLICE_NONE) {
         return fail("slice kind not valid for this class");
+    }
+    if (e.cls == XTG_CLS_DIPOLE_EDGE) {
+        if (e.model < -1 || e.model > 1) return fail("unknown DipoleEdge model (linear, full, suppressed)");
+        if (e.side != 0 && e.side != 1) return fail("DipoleEdge side must be 0 (entry) or 1 (exit)");
     }
     if (e.cls == XTG_CLS_LIMIT_POLYGON) {
         const xtg_polygon* pg = reinterpret_cast<const xtg_polygon*>(e.aux);
@@ -965,6 +1005,29 @@ int32_t pack_lattice(const xtg_element* els, int64_t n, const xtg_config& cfg,
             rb.pad16();
             break;
         }
+        case XTG_CLS_DIPOLE_EDGE: {
+            // dipoleedge.h:14-71: model -1 does nothing
+            if (e.model == -1) {
+                rb.init(sizeof(RecHeader));
+                rb.head<RecHeader>()->op = OP_NOP;
+                break;
+            }
+            rb.init(sizeof(DipoleEdgeRec));
+            rb.head<DipoleEdgeRec>()->h.op = OP_DIPOLE_EDGE;
+            rb.head<DipoleEdgeRec>()->model = e.model;
+            rb.head<DipoleEdgeRec>()->backtrack = backtrack ? 1 : 0;
+            if (e.model == 0) {
+                // the linear coefficients change sign when backtracking
+                rb.head<DipoleEdgeRec>()->r21 = backtrack ? -e.r21 : e.r21;
+                rb.head<DipoleEdgeRec>()->r43 = backtrack ? -e.r43 : e.r43;
+            } else {
+                std::vector<double> fr = dipole_edge_fringe_block(e);
+                rb.pad16();
+                int32_t const off = rb.append(fr.data(), fr.size(), sizeof(DipoleEdgeRec));
+                rb.head<DipoleEdgeRec>()->fringe = off;
+            }
+            break;
+        }
         case XTG_CLS_LIMIT_RECT: {
             rb.init(sizeof(LimitRectRec));
             LimitRectRec* r = rb.head<LimitRectRec>();
@@ -1027,6 +1090,12 @@ double canonical_flops(const unsigned char* rec) {
         return 5.0;                    // 2 mul, 1 fma-free mul-add pair
     case OP_LIMIT_RECT:
         return 0.0;
+    case OP_DIPOLE_EDGE: {
+        // linear: two products and two fused adds; full: as a magnet's
+        // dipole-only fringe
+        const DipoleEdgeRec* r = reinterpret_cast<const DipoleEdgeRec*>(rec);
+        return r->model == 0 ? 4.0 : 60.0;
+    }
     case OP_CAVITY:
         return 25.0;
     case OP_KICK: {

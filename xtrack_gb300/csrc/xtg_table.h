@@ -32,6 +32,7 @@ enum Op : int32_t {
     OP_MON_BPM = 9,       // beam position and beam size monitors
     OP_MON_PROFILE = 10,
     OP_LIMIT_POLYGON = 11,
+    OP_DIPOLE_EDGE = 12,  // DipoleEdge (dipoleedge.h): linear or full model
 };
 
 // RecHeader.flags
@@ -161,6 +162,19 @@ struct alignas(16) KickRec {
     int32_t reserved;
     ExactPass pass[3];
     double kw, hl, C0, C1, htot, Q0, Q1, reserved2;
+    // coefficient area follows (doubles)
+};
+
+// DipoleEdge (dipoleedge.h:14-71). model 0: the linear kick with r21, r43
+// (negated in backtracking tables); model 1: a FringeRec block (dipole-only
+// layout) at `fringe` doubles into the coefficient area that follows.
+struct alignas(16) DipoleEdgeRec {
+    RecHeader h;
+    int32_t model;
+    int32_t fringe;
+    int32_t backtrack;
+    int32_t reserved;
+    double r21, r43;
     // coefficient area follows (doubles)
 };
 

@@ -383,6 +383,21 @@ __device__ __forceinline__ bool apply_record(PState& p, const unsigned char* __r
                     r.backtrack != 0);
         break;
     }
+    case OP_DIPOLE_EDGE: {
+        // dipoleedge.h:14-71: the linear kick (track_dipole_edge_linear.h:
+        // 29-37) or the full model, which kills when backtracking; neither
+        // touches ax, ay
+        const DipoleEdgeRec& r = *reinterpret_cast<const DipoleEdgeRec*>(rec);
+        if (r.model == 0) {
+            double const x = p.x, y = p.y, chi = p.chi;
+            p.px = p.px + chi * r.r21 * x;
+            p.py = p.py + chi * r.r43 * y;
+        } else {
+            p = fringe_edge(p, reinterpret_cast<const double*>(rec + sizeof(DipoleEdgeRec)) + r.fringe,
+                            r.backtrack != 0);
+        }
+        break;
+    }
     case OP_CAVITY: {
         const CavityRec& r = *reinterpret_cast<const CavityRec*>(rec);
         p = cavity_cold<kExact>(p, r, rf);

@@ -508,6 +508,102 @@ class LimitRect(BeamElement):
                 ("min_y", self.min_y), ("max_y", self.max_y)]
 
 
+class DipoleEdge(BeamElement):
+    """Thin dipole edge (dipole_edge.py; dipoleedge.h:14-71). ``model``:
+    'linear' (px += chi r21 x, py += chi r43 y), 'full' (y-rotation by the
+    face angle, dipole fringe, wedge; backtracking kills) or 'suppressed';
+    ``side``: 'entry' or 'exit'. r21 and r43 follow the class's own
+    _update_r21_r43 (numpy, from k, e1, e1_fd, hgap, fint) and are
+    recomputed whenever one of those changes."""
+    _cls = _abi.CLS_DIPOLE_EDGE
+    _MODELS = {"linear": 0, "full": 1, "suppressed": -1}
+    _SIDES = {"entry": 0, "exit": 1}
+
+    def __init__(self, k=None, e1=None, e1_fd=None, hgap=None, fint=None, model=None,
+                 side=None, h=None):
+        if h is not None:
+            if k is not None:
+                raise ValueError("give k or its older name h, not both")
+            k = h
+        self._k = float(k) if k is not None else 0.0
+        self._e1 = float(e1) if e1 is not None else 0.0
+        self._e1_fd = float(e1_fd) if e1_fd is not None else 0.0
+        self._hgap = float(hgap) if hgap is not None else 0.0
+        self._fint = float(fint) if fint is not None else 0.0
+        self._model = 0
+        self._side = 0
+        if model is not None:
+            self.model = model
+        if side is not None:
+            self.side = side
+        self._update_r21_r43()
+
+    def _update_r21_r43(self):
+        k, e1 = np.float64(self._k), np.float64(self._e1)
+        corr = np.float64(2.0) * k * np.float64(self._hgap) * np.float64(self._fint)
+        r21 = k * np.tan(e1)
+        e1_v = e1 + np.float64(self._e1_fd)
+        temp = corr / np.cos(e1_v) * (np.float64(1) + np.sin(e1_v) * np.sin(e1_v))
+        r43 = -k * np.tan(e1_v - temp)
+        self.r21 = float(r21)
+        self.r43 = float(r43)
+
+    def _param(name):
+        def get(self):
+            return getattr(self, "_" + name)
+
+        def set_(self, value):
+            setattr(self, "_" + name, float(value))
+            self._update_r21_r43()
+        return property(get, set_)
+
+    k = _param("k")
+    e1 = _param("e1")
+    e1_fd = _param("e1_fd")
+    hgap = _param("hgap")
+    fint = _param("fint")
+    del _param
+
+    @property
+    def model(self):
+        return {v: k for k, v in self._MODELS.items()}[self._model]
+
+    @model.setter
+    def model(self, value):
+        if isinstance(value, str):
+            if value not in self._MODELS:
+                raise ValueError(f"model must be one of {list(self._MODELS)}")
+            value = self._MODELS[value]
+        if int(value) not in self._MODELS.values():
+            raise ValueError(f"model must be one of {list(self._MODELS)}")
+        self._model = int(value)
+
+    @property
+    def side(self):
+        return {v: k for k, v in self._SIDES.items()}[self._side]
+
+    @side.setter
+    def side(self, value):
+        if isinstance(value, str):
+            if value not in self._SIDES:
+                raise ValueError("side must be 'entry' or 'exit'")
+            value = self._SIDES[value]
+        if int(value) not in (0, 1):
+            raise ValueError("side must be 'entry' or 'exit'")
+        self._side = int(value)
+
+    def _fill(self, rec):
+        rec["cls"] = self._cls
+        rec["model"] = self._model
+        rec["side"] = self._side
+        for f in ("k", "e1", "hgap", "fint", "r21", "r43"):
+            rec[f] = getattr(self, f)
+
+    def _repr_items(self):
+        return [("k", self.k), ("e1", self.e1), ("e1_fd", self.e1_fd), ("hgap", self.hgap),
+                ("fint", self.fint), ("model", self.model), ("side", self.side)]
+
+
 class LimitPolygon(BeamElement):
     """Polygonal aperture (limit_polygon.py): a particle survives when the
     crossing-number test puts (x, y) inside the closed polygon of the
@@ -654,4 +750,5 @@ def slice_class(parent, prefix, suffix=""):
 
 
 __all__ = ["Marker", "Drift", "Multipole", "Bend", "Quadrupole", "Sextupole", "Octupole",
-           "Cavity", "LimitEllipse", "LimitRect", "BeamElement", "slice_class"] + sorted(_SLICE_CLASSES)
+           "Cavity", "LimitEllipse", "LimitRect", "LimitPolygon", "DipoleEdge", "BeamElement",
+           "slice_class"] + sorted(_SLICE_CLASSES)

@@ -27,7 +27,7 @@ _NEUTRAL = {
 }
 # derived fields that are recomputed, not read
 _DERIVED = {"inv_factorial_order", "h", "k0_from_h", "_isthick", "prototype", "x_normal",
-            "y_normal", "svg"}
+            "y_normal", "svg", "name_associated_aperture", "r21", "r43", "extra"}
 
 _MAGNET_KEYS = ("knl", "ksl", "order", "knl_rel", "ksl_rel", "model", "integrator",
                 "num_multipole_kicks")
@@ -52,6 +52,7 @@ _ACCEPT = {
     "LimitEllipse": ("a_squ", "b_squ", "a_b_squ", "a", "b"),
     "LimitRect": ("min_x", "max_x", "min_y", "max_y"),
     "LimitPolygon": ("x_vertices", "y_vertices"),
+    "DipoleEdge": ("k", "e1", "e1_fd", "hgap", "fint", "model", "side"),
 }
 
 
@@ -87,6 +88,9 @@ def element_from_dict(dct, name="?"):
             kw["angle"] = float(d["h"]) * float(kw.get("length", 0.0))
         if d.get("k0_from_h"):
             kw["k0"] = "from_h"
+    if cname == "DipoleEdge" and "k" not in kw and "h" in d:
+        # dipole_edge.py backward compatibility: h -> k
+        kw["k"] = d["h"]
     if cname == "Multipole" and "isthick" in kw:
         kw["isthick"] = bool(kw["isthick"])
     if cname == "LimitEllipse" and ("a" in kw or "b" in kw) and "a_squ" in kw:
@@ -121,6 +125,17 @@ def element_to_dict(e):
     if isinstance(e, el.LimitPolygon):
         out.update(x_vertices=e.x_vertices.tolist(), y_vertices=e.y_vertices.tolist())
         return out
+    if isinstance(e, el.DipoleEdge):
+        # dipole_edge.py to_dict: nonzero scalars, model and side when not default
+        for f in ("k", "e1", "e1_fd", "hgap", "fint"):
+            v = getattr(e, f)
+            if not np.isclose(v, 0, atol=1e-16):
+                out[f] = v
+        if e._model != 0:
+            out["model"] = e.model
+        if e._side != 0:
+            out["side"] = e.side
+        return out
     # magnets
     out.update(knl=e.knl.tolist(), ksl=e.ksl.tolist(), order=e.order,
                knl_rel=e.knl_rel.tolist(), ksl_rel=e.ksl_rel.tolist(), model=e._model,
@@ -148,11 +163,27 @@ def element_to_dict(e):
 
 
 def line_from_dict(dct):
-    """A Line from an xtrack line dict ({'elements': {name: dict}, 'element_names': [...]})."""
+    """A Line from an xtrack line dict ({'elements': {name: dict}, 'element_names': [...]}).
+    Only the elements the sequence uses, and the parents of its slices, are
+    built: a dict written by an environment also holds prototypes that no
+    line references."""
     from .line import Line
+    all_elements = dct["elements"]
+    used = set(dct["element_names"])
+    missing = used - set(all_elements)
+    if missing:
+        raise ValueError(f"element_names refer to unknown elements {sorted(missing)[:5]}")
+    for n in list(used):
+        d = all_elements[n]
+        if d["__class__"] in el._SLICE_CLASSES:
+            pname = d.get("parent_name", d.get("_parent_name"))
+            if pname in all_elements:
+                used.add(pname)
     elements = {}
     slices = {}
-    for n, d in dct["elements"].items():
+    for n, d in all_elements.items():
+        if n not in used:
+            continue
         if d["__class__"] in el._SLICE_CLASSES:
             slices[n] = d
         else:
