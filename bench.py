@@ -589,6 +589,103 @@ def run_toy_ring(args):
     print(json.dumps(out))
 
 
+def run_real_lattice(args):
+    """A real machine: the thin SPS line of the reference's test data
+    (8199 elements: drifts, thin multipoles, 1488 DipoleEdges, 1698
+    apertures, cavities; packed records of the committed parity fixture
+    tests/golden/sps), --particles protons around the fixture's particle
+    with its spread (some are lost on the apertures), one turn per step,
+    through the C-ABI (xtg_lattice_create / xtg_track) with CUDA events;
+    the oracle's port of the reference OpenMP path on the host cores as
+    the CPU baseline."""
+    import ctypes
+
+    import torch
+    import xtrack_gb300 as xt
+    from xtrack_gb300 import _abi
+    import pyoracle
+
+    rank, world, local = _dist()
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    d = np.load(os.path.join(ROOT, "tests", "golden", "sps", "sps_thin_128p_20t.npz"))
+    meta = json.loads(str(d["meta"]))
+    recs = np.ascontiguousarray(d["records"])
+    n_el, L = len(recs), float(meta["line_length"])
+    p0 = {k[3:]: d[k] for k in d.files if k.startswith("in_")}
+    rng = np.random.default_rng(16)
+    sig = {"x": 6e-3, "px": 1.5e-4, "y": 5e-3, "py": 1.5e-4, "zeta": 0.05, "delta": 5e-4}
+    base = {k: float(np.mean(p0[k])) for k in sig}
+
+    def beam(n, device):
+        kw = {k: base[k] + rng.normal(0.0, s, n) for k, s in sig.items()}
+        return xt.Particles(device=device, p0c=float(p0["p0c"][0]), mass0=meta["mass0"],
+                            q0=meta["q0"], **kw)
+
+    lib = _abi.load_library()
+    cfg = _abi.XtgConfig()
+    cfg.has_global_xy_limit = 1
+    cfg.global_xy_limit = 1.0
+    cfg.arith = _abi.ARITH_FAST if args.arith == "fast" else _abi.ARITH_EXACT
+    h = ctypes.c_void_p()
+    _abi.check(lib.xtg_lattice_create(recs.ctypes.data_as(ctypes.c_void_p), n_el,
+                                      ctypes.byref(cfg), ctypes.byref(h)), lib)
+    nn, fl = ctypes.c_int64(), ctypes.c_double()
+    _abi.check(lib.xtg_lattice_info(h, ctypes.byref(nn), 0, n_el, ctypes.byref(fl)), lib)
+    flops_pt = fl.value
+    p = beam(args.particles, dev)
+    ps = p._xtg_struct()
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        _abi.check(lib.xtg_track(h, ctypes.byref(ps), 1, 0, n_el, 1, 1, 0, n_el, L, None, 0,
+                                 ctypes.c_void_p(stream.cuda_stream)), lib)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize(dev)
+    alive0 = int((p.state > 0).sum())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    e1.synchronize()
+    _abi.check(lib.xtg_device_status(h), lib)
+    ms = e0.elapsed_time(e1)
+    alive1 = int((p.state > 0).sum())
+    value = alive1 * args.steps / (ms * 1e-3)
+    peak = ctypes.c_double()
+    _abi.check(lib.xtg_measure_fp64_peak(ctypes.byref(peak)), lib)
+    lib.xtg_lattice_destroy(h)
+    # CPU: the oracle port on all host cores, one turn of a sample
+    pyoracle.ensure_built(with_ref=False)
+    n_cpu = 20000
+    arrs = pyoracle.host_arrays(beam(n_cpu, "cpu").to_numpy())
+    t0 = time.perf_counter()
+    pyoracle.track(recs, arrs, line_length=L, num_turns=1, q0=meta["q0"], mass0=meta["mass0"],
+                   mode=pyoracle.MODE_OPENMP)
+    dt = time.perf_counter() - t0
+    cpu = float(np.sum(arrs["state"] > 0)) / dt
+    achieved = value * flops_pt / 1e12
+    out = {"metric": "real-lattice particle-turns/s (thin SPS line)", "value": value,
+           "unit": "particle-turns/s", "higher_is_better": True, "n_gpus": 1, "dtype": "f64",
+           "data": "synthetic beam on a real lattice", "arith": args.arith,
+           "config": {"workload": f"thin SPS line of the reference's test data ({n_el} elements)",
+                      "particles": args.particles, "turns_per_step": 1},
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+           "alive_before": alive0, "alive_after": alive1,
+           "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak.value / 1e12,
+                        "unit": "TFLOP/s", "frac": achieved / (peak.value / 1e12),
+                        "flops_per_particle_turn": flops_pt},
+           "cpu_baseline": {"value": cpu, "unit": "particle-turns/s",
+                            "cores": pyoracle.max_threads(), "kind": "port",
+                            "sample": f"{n_cpu} particles x 1 turn ({dt:.2f} s, OpenMP)"}}
+    print(json.dumps(out))
+
+
 def run_turn_latency(args):
     """Milliseconds per turn of the thick ring for particle counts from a
     fraction of one resident wave (8 warps per SM) to four waves, for
@@ -657,7 +754,8 @@ def main():
     ap.add_argument("--monitor-first", dest="monitor_first", type=int, default=0,
                     help="record 6 coordinates per turn of the first N particles")
     ap.add_argument("--workload", default="thick_ring",
-                    choices=["thick_ring", "da_screen", "turn_latency", "batch_scan", "toy_ring"])
+                    choices=["thick_ring", "da_screen", "turn_latency", "batch_scan", "toy_ring",
+                             "real_lattice"])
     ap.add_argument("--toy-particles", dest="toy_particles", type=int, default=10000)
     ap.add_argument("--toy-turns", dest="toy_turns", type=int, default=1000)
     ap.add_argument("--toy-cpu-turns", dest="toy_cpu_turns", type=int, default=1000)
@@ -695,6 +793,8 @@ def main():
         run_batch_scan(args)
     elif args.workload == "toy_ring":
         run_toy_ring(args)
+    elif args.workload == "real_lattice":
+        run_real_lattice(args)
     elif args.impl == "reference":
         run_reference(args)
     else:
