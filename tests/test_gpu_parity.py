@@ -316,6 +316,43 @@ def test_nan_coordinates_lost_at_global_aperture(arith):
         assert np.sum(got["state"] == -1) > 100
 
 
+@pytest.mark.parametrize("arith", ["exact", "fast"])
+def test_aperture_compare_edge_values(arith):
+    """LimitRect and the global aperture compare integer keys of the IEEE
+    bit patterns on the GPU; the oracle compares doubles as the reference
+    does. Coordinates on and one ulp beyond each bound, signed zeros at
+    zero bounds, NaN of both signs, infinities and subnormals all end in
+    the same state and at_element."""
+    lim = 0.004
+    specials = [0.0, -0.0, 0.01, np.nextafter(0.01, 1.0), 0.02, -0.02,
+                np.nextafter(-0.02, -1.0), lim, -lim, np.nextafter(lim, 1.0),
+                np.nextafter(-lim, -1.0), np.nan, -np.nan, np.inf, -np.inf, 5e-324, -5e-324,
+                1e-3, -1e-3]
+    xs, ys = np.meshgrid(np.array(specials), np.array(specials), indexing="ij")
+    n = xs.size
+    line = xt.Line(elements=[
+        xt.LimitRect(min_x=0.0, max_x=0.01, min_y=-0.02, max_y=-0.0),
+        xt.Drift(length=0.0),
+        xt.LimitRect(min_x=-0.0, max_x=0.02, min_y=-0.02, max_y=0.0),
+        xt.Drift(length=0.0),
+    ])
+    recs = line._element_records()
+    beam = xt.Particles(device="cpu", p0c=7e12, x=xs.ravel(), y=ys.ravel(), px=np.zeros(n),
+                        py=np.zeros(n))
+    arrs = pyoracle.host_arrays(beam.to_numpy())
+    for glim in (lim, 1.0):
+        for flags in (0, 1 << _abi.FLAG_IGNORE_LOCAL_APERTURE):
+            ref = {k: v.copy() for k, v in arrs.items()}
+            pyoracle.track(recs, ref, line_length=0.0, num_turns=1, global_xy_limit=glim,
+                           track_flags=flags)
+            got, _ = gpu_track(recs, {k: v.copy() for k, v in arrs.items()}, arith=arith,
+                               line_length=0.0, num_turns=1, global_xy_limit=glim,
+                               track_flags=flags)
+            for f in ("state", "at_element", "at_turn"):
+                assert np.array_equal(got[f], ref[f]), (glim, flags, f)
+            assert len(set(ref["state"].tolist())) > 1
+
+
 def test_batch_matches_per_seed_oracle():
     """Three error seeds of one ring in one persistent launch, particles of
     the seeds interleaved: each particle equals the oracle run of its seed."""

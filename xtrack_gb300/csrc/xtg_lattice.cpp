@@ -1032,10 +1032,10 @@ int32_t pack_lattice(const xtg_element* els, int64_t n, const xtg_config& cfg,
             rb.init(sizeof(LimitRectRec));
             LimitRectRec* r = rb.head<LimitRectRec>();
             r->h.op = OP_LIMIT_RECT;
-            r->min_x = e.min_x;
-            r->max_x = e.max_x;
-            r->min_y = e.min_y;
-            r->max_y = e.max_y;
+            r->key_min_x = lower_key(e.min_x);
+            r->key_max_x = upper_key(e.max_x);
+            r->key_min_y = lower_key(e.min_y);
+            r->key_max_y = upper_key(e.max_y);
             break;
         }
         case XTG_CLS_CAVITY:

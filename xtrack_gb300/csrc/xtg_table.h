@@ -12,8 +12,15 @@
 // Shared by the host packer (xtg_lattice.cpp) and the kernels (xtg_track.cu).
 #pragma once
 #include <stdint.h>
+#include <string.h>
 
 #include "../../include/xtrack_gb300.h"
+
+#ifdef __CUDACC__
+#define XTG_HD_INLINE __host__ __device__ __forceinline__
+#else
+#define XTG_HD_INLINE static inline
+#endif
 
 namespace xtg {
 
@@ -59,10 +66,37 @@ struct alignas(16) LimitEllipseRec {
     double a_squ, b_squ, a_b_squ, reserved;
 };
 
+// LimitRect (limitrect.h:9-36): the bounds as ordered integer keys of their
+// IEEE bit patterns (ord_key in xtg_table.h), so that the four compares
+// run on the integer pipe instead of the narrow FP64 pipe.
 struct alignas(16) LimitRectRec {
     RecHeader h;
-    double min_x, max_x, min_y, max_y;
+    int64_t key_min_x, key_max_x, key_min_y, key_max_y;
 };
+
+// Ordered integer key of an IEEE double: for non-NaN a, b other than the
+// pair (-0, +0), a <= b exactly when key(a) <= key(b); a NaN of either sign
+// lies above key(+inf) or below key(-inf), outside every interval between
+// non-NaN bounds. The bounds are normalised so that both zeros pass as they
+// do in the FP64 compare: a lower bound of 0 is key(-0), an upper bound of
+// 0 is key(+0); a NaN bound loses every particle, as the FP64 compare does.
+XTG_HD_INLINE int64_t ord_key(double v) {
+#ifdef __CUDA_ARCH__
+    int64_t const b = __double_as_longlong(v);
+#else
+    int64_t b;
+    memcpy(&b, &v, sizeof(b));
+#endif
+    return b ^ ((b >> 63) & (int64_t)0x7FFFFFFFFFFFFFFFLL);
+}
+XTG_HD_INLINE int64_t lower_key(double lo) {
+    if (lo != lo) return (int64_t)0x7FFFFFFFFFFFFFFFLL;
+    return ord_key(lo == 0.0 ? -0.0 : lo);
+}
+XTG_HD_INLINE int64_t upper_key(double hi) {
+    if (hi != hi) return (int64_t)(-0x7FFFFFFFFFFFFFFFLL - 1);
+    return ord_key(hi == 0.0 ? 0.0 : hi);
+}
 
 // LimitPolygon (limitpolygon.h:13-90): x vertices then y vertices follow.
 struct alignas(16) LimitPolygonRec {

@@ -121,6 +121,7 @@ struct TrackArgs {
     int32_t has_global;
     int32_t preserve_angle;
     double global_lim;
+    int64_t global_key_lo, global_key_hi;   // lower_key(-global_lim), upper_key(global_lim)
     int64_t num_ele_line;
     double line_length;
     uint64_t track_flags;
@@ -415,8 +416,12 @@ __device__ __forceinline__ bool apply_record(PState& p, const unsigned char* __r
     case OP_LIMIT_RECT: {
         // limitrect.h:9-36
         if (!flag_on(a.track_flags, XTG_FLAG_IGNORE_LOCAL_APERTURE)) {
+            // the FP64 compares of the reference as integer compares of
+            // ordered keys (ord_key, xtg_table.h): same outcome, NaN lost
             const LimitRectRec& r = *reinterpret_cast<const LimitRectRec*>(rec);
-            bool const alive = (p.x >= r.min_x) && (p.x <= r.max_x) && (p.y >= r.min_y) && (p.y <= r.max_y);
+            int64_t const kx = ord_key(p.x), ky = ord_key(p.y);
+            bool const alive = (kx >= r.key_min_x) && (kx <= r.key_max_x) && (ky >= r.key_min_y) &&
+                               (ky <= r.key_max_y);
             if (!alive) p.state = 0;
         }
         break;
@@ -476,8 +481,10 @@ __device__ __forceinline__ void walk(PState& p, bool& active, const unsigned cha
         bool const thick = apply_record<kExact>(p, rec, a, rf, i, pid);
         if (thick && !ignore_global) {
             // local_particle_custom_api.h:259-287
-            double const lim = a.global_lim;
-            bool const within = (p.x >= -lim) && (p.x <= lim) && (p.y >= -lim) && (p.y <= lim);
+            // |x|, |y| <= limit as ordered-key compares (ord_key)
+            int64_t const kx = ord_key(p.x), ky = ord_key(p.y);
+            bool const within = (kx >= a.global_key_lo) && (kx <= a.global_key_hi) &&
+                                (ky >= a.global_key_lo) && (ky <= a.global_key_hi);
             if (p.state > 0 && !within) p.state = -1;
         }
         if (p.state <= 0) {
@@ -1216,6 +1223,8 @@ static int32_t track_impl(ExecCtx* C, const xtg_particles* particles, const int3
     a.has_global = C->config.has_global_xy_limit;
     a.preserve_angle = C->config.cavity_preserve_angle;
     a.global_lim = C->config.global_xy_limit;
+    a.global_key_lo = lower_key(-a.global_lim);
+    a.global_key_hi = upper_key(a.global_lim);
     a.num_ele_line = num_ele_line;
     a.line_length = line_length;
     a.track_flags = track_flags;
@@ -1512,6 +1521,8 @@ int32_t xtg_track_noalloc(const xtg_lattice* lattice, const xtg_particles* parti
     a.has_global = C->config.has_global_xy_limit;
     a.preserve_angle = C->config.cavity_preserve_angle;
     a.global_lim = C->config.global_xy_limit;
+    a.global_key_lo = lower_key(-a.global_lim);
+    a.global_key_hi = upper_key(a.global_lim);
     a.num_ele_line = num_ele_line;
     a.line_length = line_length;
     a.track_flags = track_flags;
