@@ -318,9 +318,9 @@ def test_nan_coordinates_lost_at_global_aperture(arith):
 
 @pytest.mark.parametrize("arith", ["exact", "fast"])
 def test_aperture_compare_edge_values(arith):
-    """LimitRect and the global aperture compare integer keys of the IEEE
-    bit patterns on the GPU; the oracle compares doubles as the reference
-    does. Coordinates on and one ulp beyond each bound, signed zeros at
+    """LimitRect, LimitEllipse and the global aperture compare integer keys
+    of the IEEE bit patterns on the GPU; the oracle compares doubles as the
+    reference does. Coordinates on and one ulp beyond each bound, signed zeros at
     zero bounds, NaN of both signs, infinities and subnormals all end in
     the same state and at_element."""
     lim = 0.004
@@ -330,17 +330,15 @@ def test_aperture_compare_edge_values(arith):
                 1e-3, -1e-3]
     xs, ys = np.meshgrid(np.array(specials), np.array(specials), indexing="ij")
     n = xs.size
-    line = xt.Line(elements=[
-        xt.LimitRect(min_x=0.0, max_x=0.01, min_y=-0.02, max_y=-0.0),
-        xt.Drift(length=0.0),
-        xt.LimitRect(min_x=-0.0, max_x=0.02, min_y=-0.02, max_y=0.0),
-        xt.Drift(length=0.0),
-    ])
-    recs = line._element_records()
+    rects = [xt.LimitRect(min_x=0.0, max_x=0.01, min_y=-0.02, max_y=-0.0), xt.Drift(length=0.0),
+             xt.LimitRect(min_x=-0.0, max_x=0.02, min_y=-0.02, max_y=0.0), xt.Drift(length=0.0)]
+    ellipses = [xt.LimitEllipse(a=0.01, b=0.02), xt.Drift(length=0.0),
+                xt.LimitEllipse(a=0.02, b=0.004), xt.Drift(length=0.0)]
     beam = xt.Particles(device="cpu", p0c=7e12, x=xs.ravel(), y=ys.ravel(), px=np.zeros(n),
                         py=np.zeros(n))
     arrs = pyoracle.host_arrays(beam.to_numpy())
-    for glim in (lim, 1.0):
+    for glim, els in ((lim, rects), (1.0, rects), (lim, ellipses), (1.0, ellipses)):
+        recs = xt.Line(elements=els)._element_records()
         for flags in (0, 1 << _abi.FLAG_IGNORE_LOCAL_APERTURE):
             ref = {k: v.copy() for k, v in arrs.items()}
             pyoracle.track(recs, ref, line_length=0.0, num_turns=1, global_xy_limit=glim,

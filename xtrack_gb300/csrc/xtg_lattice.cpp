@@ -899,7 +899,7 @@ int32_t pack_lattice(const xtg_element* els, int64_t n, const xtg_config& cfg,
             r->h.op = OP_LIMIT_ELLIPSE;
             r->a_squ = e.a_squ;
             r->b_squ = e.b_squ;
-            r->a_b_squ = e.a_b_squ;
+            r->key_a_b_squ = upper_key(e.a_b_squ);
             break;
         }
         case XTG_CLS_MONITOR: {

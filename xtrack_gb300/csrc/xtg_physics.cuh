@@ -751,8 +751,26 @@ XTG_COLD PState fringe_edge(PState p, const double* __restrict__ fr, bool backtr
     return p;
 }
 
+// track_dipole_edge_linear.h:29-37: px += chi*r21*x, py += chi*r43*y. The
+// reference rounds chi*r21 first; at chi == 1 that product is r21 exactly
+// and is skipped. The fast mode fuses the remaining product and sum.
+template <bool kExact>
+XTG_DEV void edge_linear_kick(PState& p, double r21, double r43) {
+    double const x = p.x, y = p.y;
+    double const c21 = p.chi_one ? r21 : p.chi * r21;
+    double const c43 = p.chi_one ? r43 : p.chi * r43;
+    if (kExact) {
+        p.px = p.px + c21 * x;
+        p.py = p.py + c43 * y;
+    } else {
+        p.px = fma(c21, x, p.px);
+        p.py = fma(c43, y, p.py);
+    }
+}
+
 // track_magnet_edge.h:16-80 with the linear model (track_dipole_edge_linear.h);
 // the nonlinear models go to fringe_edge
+template <bool kExact>
 XTG_DEV void magnet_edge(PState& p, int kind, bool is_exit, double r21, double r43,
                          const double* __restrict__ fringe, bool backtrack) {
     if (kind == EDGE_NONE) return;
@@ -774,11 +792,7 @@ XTG_DEV void magnet_edge(PState& p, int kind, bool is_exit, double r21, double r
         p.ax = (-0.5 * 0.0) * (p.y - 0.);
         p.ay = (0.5 * 0.0) * (p.x - 0.);
     }
-    if (kind == EDGE_LINEAR) {
-        double const x = p.x, y = p.y, chi = p.chi;
-        p.px = p.px + chi * r21 * x;
-        p.py = p.py + chi * r43 * y;
-    }
+    if (kind == EDGE_LINEAR) edge_linear_kick<kExact>(p, r21, r43);
 }
 
 // track_magnet.h:25-285 (body) after the host-side resolution.

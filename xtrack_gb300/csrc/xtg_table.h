@@ -61,9 +61,15 @@ struct alignas(16) DriftRec {
     int32_t reserved;
 };
 
+// LimitEllipse (limitellipse.h:12-38): the final compare of x^2 b^2 +
+// y^2 a^2 against a_b_squ on ordered keys (upper_key(a_b_squ)); the sum is
+// +0 or more, or NaN, so [key(-0), key_a_b_squ] decides it as the FP64
+// compare does.
 struct alignas(16) LimitEllipseRec {
     RecHeader h;
-    double a_squ, b_squ, a_b_squ, reserved;
+    double a_squ, b_squ;
+    int64_t key_a_b_squ;
+    int64_t reserved;
 };
 
 // LimitRect (limitrect.h:9-36): the bounds as ordered integer keys of their

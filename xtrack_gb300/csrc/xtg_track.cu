@@ -376,11 +376,11 @@ __device__ __forceinline__ bool apply_record(PState& p, const unsigned char* __r
     case OP_MAGNET: {
         const MagnetRec& r = *reinterpret_cast<const MagnetRec*>(rec);
         const double* coefs = reinterpret_cast<const double*>(rec + sizeof(MagnetRec));
-        magnet_edge(p, r.edge_entry, false, r.entry_r21, r.entry_r43, coefs + r.entry_fringe,
+        magnet_edge<kExact>(p, r.edge_entry, false, r.entry_r21, r.entry_r43, coefs + r.entry_fringe,
                     r.backtrack != 0);
         if (p.state <= 0) break;   // killed by a nonlinear edge while backtracking
         if (r.body_active) magnet_body<kExact>(p, r, coefs);
-        magnet_edge(p, r.edge_exit, true, r.exit_r21, r.exit_r43, coefs + r.exit_fringe,
+        magnet_edge<kExact>(p, r.edge_exit, true, r.exit_r21, r.exit_r43, coefs + r.exit_fringe,
                     r.backtrack != 0);
         break;
     }
@@ -390,9 +390,7 @@ __device__ __forceinline__ bool apply_record(PState& p, const unsigned char* __r
         // touches ax, ay
         const DipoleEdgeRec& r = *reinterpret_cast<const DipoleEdgeRec*>(rec);
         if (r.model == 0) {
-            double const x = p.x, y = p.y, chi = p.chi;
-            p.px = p.px + chi * r.r21 * x;
-            p.py = p.py + chi * r.r43 * y;
+            edge_linear_kick<kExact>(p, r.r21, r.r43);
         } else {
             p = fringe_edge(p, reinterpret_cast<const double*>(rec + sizeof(DipoleEdgeRec)) + r.fringe,
                             r.backtrack != 0);
@@ -409,7 +407,8 @@ __device__ __forceinline__ bool apply_record(PState& p, const unsigned char* __r
         if (!flag_on(a.track_flags, XTG_FLAG_IGNORE_LOCAL_APERTURE)) {
             const LimitEllipseRec& r = *reinterpret_cast<const LimitEllipseRec*>(rec);
             double const temp = p.x * p.x * r.b_squ + p.y * p.y * r.a_squ;
-            if (!(temp <= r.a_b_squ)) p.state = 0;
+            int64_t const kt = ord_key(temp);
+            if (!(kt >= lower_key(0.0) && kt <= r.key_a_b_squ)) p.state = 0;
         }
         break;
     }
