@@ -591,7 +591,7 @@ def run_toy_ring(args):
 
 def run_real_lattice(args):
     """A real machine: the thin SPS line of the reference's test data
-    (8199 elements: drifts, thin multipoles, 1488 DipoleEdges, 1698
+    (8200 elements: drifts, thin multipoles, 1488 DipoleEdges, 1698
     apertures, cavities; packed records of the committed parity fixture
     tests/golden/sps), --particles protons around the fixture's particle
     with its spread (some are lost on the apertures), one turn per step,

@@ -172,6 +172,10 @@ typedef void* SynchrotronRadiationRecordData;
     XTR_GET_D(C, min_x, el->min_x) XTR_GET_D(C, max_x, el->max_x) \
     XTR_GET_D(C, min_y, el->min_y) XTR_GET_D(C, max_y, el->max_y) \
     XTR_GET_D(C, weight, el->weight) XTR_GET_D(C, delta_taper, 0.) \
+    XTR_GET_D(C, shift_x, el->shift_x) XTR_GET_D(C, shift_y, el->shift_y) \
+    XTR_GET_D(C, shift_s, el->shift_s) XTR_GET_D(C, rot_x_rad, el->rot_x_rad) \
+    XTR_GET_D(C, rot_y_rad, el->rot_y_rad) XTR_GET_D(C, rot_s_rad, el->rot_s_rad) \
+    XTR_GET_D(C, rot_s_rad_no_frame, el->rot_s_rad_no_frame) XTR_GET_D(C, rot_shift_anchor, 0.) \
     XTR_GET_D(C, lag_taper, 0.) XTR_GET_D(C, phase_taper, 0.) \
     XTR_GET_I(C, order, el->order) XTR_GET_I(C, num_multipole_kicks, el->num_multipole_kicks) \
     XTR_GET_I(C, num_kicks, el->num_multipole_kicks) XTR_GET_I(C, model, el->model) \
@@ -230,6 +234,20 @@ XTR_GET_I(DipoleEdge, model, el->model) XTR_GET_I(DipoleEdge, side, el->side)
 #include "xtrack/beam_elements/elements_src/limitellipse.h"
 #include "xtrack/beam_elements/elements_src/limitrect.h"
 #include "xtrack/beam_elements/elements_src/dipoleedge.h"
+
+/* The apertures through the reference's transformation wrapper, as its
+ * kernel calls every element (base_element.py:83-126): the entry and exit
+ * shifts of a shifted aperture come from the reference's own code. */
+#define ELEMENT_NAME LimitRect
+#define ALLOW_ROT_AND_SHIFT 1
+#include "xtrack/headers/track_local_particle_with_transformations.h"
+#undef ALLOW_ROT_AND_SHIFT
+#undef ELEMENT_NAME
+#define ELEMENT_NAME LimitEllipse
+#define ALLOW_ROT_AND_SHIFT 1
+#include "xtrack/headers/track_local_particle_with_transformations.h"
+#undef ALLOW_ROT_AND_SHIFT
+#undef ELEMENT_NAME
 #include "xtrack/beam_elements/elements_src/thick_slice_bend.h"
 #include "xtrack/beam_elements/elements_src/thin_slice_bend.h"
 #include "xtrack/beam_elements/elements_src/drift_slice_bend.h"
@@ -273,8 +291,8 @@ static int xtr_apply(const xtg_element* e, LocalParticle* lp) {
     switch (e->cls) {
     case XTG_CLS_MARKER: return 0;
     case XTG_CLS_DRIFT: Drift_track_local_particle(e, lp); return 1;
-    case XTG_CLS_LIMIT_ELLIPSE: LimitEllipse_track_local_particle(e, lp); return 0;
-    case XTG_CLS_LIMIT_RECT: LimitRect_track_local_particle(e, lp); return 0;
+    case XTG_CLS_LIMIT_ELLIPSE: LimitEllipse_track_local_particle_with_transformations(e, lp); return 0;
+    case XTG_CLS_LIMIT_RECT: LimitRect_track_local_particle_with_transformations(e, lp); return 0;
     case XTG_CLS_DIPOLE_EDGE: DipoleEdge_track_local_particle(e, lp); return 0;
     case XTG_CLS_MULTIPOLE: XTR_SLICES(Multipole, 0) return 0;
     case XTG_CLS_BEND: XTR_EDGES(Bend) XTR_SLICES(Bend, 1) return 0;

@@ -1360,52 +1360,22 @@ static void xto_profile(const xtg_element_monitor* m, const xto_part* p) {
     }
 }
 
-/* Applies one element to one particle. Returns whether the class is
- * statically thick (global aperture check follows, tracker.py:681-689).
- * `src`/`isrc` locate the particle in its arrays (monitors copy the fields
- * the push does not carry). */
-static int xto_apply(const xtg_element* e, const xtg_config* cfg, xto_part* p,
-                     const xtg_particles* src, int64_t isrc) {
-    int const backtrack = flag_set(p, XTG_FLAG_BACKTRACK);
+/* The aperture check of one LimitEllipse / LimitPolygon / LimitRect on the
+ * particle's current x, y (limitellipse.h, limitpolygon.h, limitrect.h). */
+static void xto_aperture(const xtg_element* e, xto_part* p) {
     switch (e->cls) {
-    case XTG_CLS_MARKER:
-        return 0;
-    case XTG_CLS_MONITOR: {
-        /* monitors/*.py: get_backtrack_element is a Marker */
-        const xtg_element_monitor* m = (const xtg_element_monitor*)(uintptr_t)e->aux;
-        if (backtrack) return 0;
-        if (m->kind == XTG_MON_PARTICLES) xto_monitor(&m->particles, p, src, isrc);
-        else if (m->kind == XTG_MON_LAST_TURNS) xto_last_turns(m, p);
-        else if (m->kind == XTG_MON_BEAM_POSITION || m->kind == XTG_MON_BEAM_SIZE) xto_bpm(m, p);
-        else if (m->kind == XTG_MON_BEAM_PROFILE) xto_profile(m, p);
-        return 0;
-    }
-    case XTG_CLS_DRIFT: {
-        /* drift.h:13-37 */
-        double length = e->length;
-        if (backtrack) length = -length;
-        int model;
-        if (cfg->use_exact_drifts) model = 2;
-        else {
-            model = e->model;
-            if (model == 0) model = 1;
-        }
-        if (model == 1) xto_drift_expanded(p, length);
-        else if (model == 2) xto_drift_exact(p, length);
-        return 1;
-    }
     case XTG_CLS_LIMIT_ELLIPSE: {
         /* limitellipse.h:12-38 */
-        if (flag_set(p, XTG_FLAG_IGNORE_LOCAL_APERTURE)) return 0;
+        if (flag_set(p, XTG_FLAG_IGNORE_LOCAL_APERTURE)) return;
         double const x = p->x, y = p->y;
         double const temp = x * x * e->b_squ + y * y * e->a_squ;
         int64_t const is_alive = (int64_t)(temp <= e->a_b_squ);
         if (!is_alive) p->state = 0;
-        return 0;
+        return;
     }
     case XTG_CLS_LIMIT_POLYGON: {
         /* limitpolygon.h:13-90 (CPU build: inscribed-circle shortcut) */
-        if (flag_set(p, XTG_FLAG_IGNORE_LOCAL_APERTURE)) return 0;
+        if (flag_set(p, XTG_FLAG_IGNORE_LOCAL_APERTURE)) return;
         const xtg_polygon* pg = (const xtg_polygon*)(uintptr_t)e->aux;
         int64_t const N_edg = pg->n_vertices;
         double inner_radius_sq = 0.0;
@@ -1444,6 +1414,80 @@ static int xto_apply(const xtg_element* e, const xtg_config* cfg, xto_part* p,
             }
             if (!is_alive) p->state = 0;
         }
+        return;
+    }
+    case XTG_CLS_LIMIT_RECT: {
+        /* limitrect.h:9-36 */
+        if (flag_set(p, XTG_FLAG_IGNORE_LOCAL_APERTURE)) return;
+        double const x = p->x, y = p->y;
+        int64_t const is_alive = (int64_t)((x >= e->min_x) && (x <= e->max_x)
+                                           && (y >= e->min_y) && (y <= e->max_y));
+        if (!is_alive) p->state = 0;
+        return;
+    }
+    default:
+        return;
+    }
+}
+
+/* Applies one element to one particle. Returns whether the class is
+ * statically thick (global aperture check follows, tracker.py:681-689).
+ * `src`/`isrc` locate the particle in its arrays (monitors copy the fields
+ * the push does not carry). */
+static int xto_apply(const xtg_element* e, const xtg_config* cfg, xto_part* p,
+                     const xtg_particles* src, int64_t isrc) {
+    int const backtrack = flag_set(p, XTG_FLAG_BACKTRACK);
+    switch (e->cls) {
+    case XTG_CLS_MARKER:
+        return 0;
+    case XTG_CLS_MONITOR: {
+        /* monitors/*.py: get_backtrack_element is a Marker */
+        const xtg_element_monitor* m = (const xtg_element_monitor*)(uintptr_t)e->aux;
+        if (backtrack) return 0;
+        if (m->kind == XTG_MON_PARTICLES) xto_monitor(&m->particles, p, src, isrc);
+        else if (m->kind == XTG_MON_LAST_TURNS) xto_last_turns(m, p);
+        else if (m->kind == XTG_MON_BEAM_POSITION || m->kind == XTG_MON_BEAM_SIZE) xto_bpm(m, p);
+        else if (m->kind == XTG_MON_BEAM_PROFILE) xto_profile(m, p);
+        return 0;
+    }
+    case XTG_CLS_DRIFT: {
+        /* drift.h:13-37 */
+        double length = e->length;
+        if (backtrack) length = -length;
+        int model;
+        if (cfg->use_exact_drifts) model = 2;
+        else {
+            model = e->model;
+            if (model == 0) model = 1;
+        }
+        if (model == 1) xto_drift_expanded(p, length);
+        else if (model == 2) xto_drift_exact(p, length);
+        return 1;
+    }
+    case XTG_CLS_LIMIT_ELLIPSE:
+    case XTG_CLS_LIMIT_POLYGON:
+    case XTG_CLS_LIMIT_RECT: {
+        /* track_local_particle_with_transformations.h:146-165 with only
+         * shift_x / shift_y nonzero (track_misalignments.h:38-112): the entry
+         * XYShift for the particle reaching the element, the exit XYShift
+         * only if it survives (the CPU per-particle blocks skip lost
+         * particles); both also when local apertures are ignored */
+        int const shifted = (e->shift_x != 0.0 || e->shift_y != 0.0);
+        if (shifted) {
+            double mx, my;
+            if (!backtrack) { mx = e->shift_x - 0.0; my = e->shift_y - 0.0; }
+            else { mx = -(0.0 - e->shift_x); my = -(0.0 - e->shift_y); }
+            p->x += -mx;
+            p->y += -my;
+        }
+        xto_aperture(e, p);
+        if (shifted && p->state > 0) {
+            double mx, my;
+            if (!backtrack) { mx = 0.0 - e->shift_x; my = 0.0 - e->shift_y; }
+            else { mx = -(e->shift_x - 0.0); my = -(e->shift_y - 0.0); }
+            p->x += -mx;
+            p->y += -my;
+        }
         return 0;
     }
     case XTG_CLS_DIPOLE_EDGE: {
@@ -1480,15 +1524,6 @@ static int xto_apply(const xtg_element* e, const xtg_config* cfg, xto_part* p,
                 if (sin_ > -99.) xto_yrotation(p, -sin_, cos_, -tan_);
             }
         }
-        return 0;
-    }
-    case XTG_CLS_LIMIT_RECT: {
-        /* limitrect.h:9-36 */
-        if (flag_set(p, XTG_FLAG_IGNORE_LOCAL_APERTURE)) return 0;
-        double const x = p->x, y = p->y;
-        int64_t const is_alive = (int64_t)((x >= e->min_x) && (x <= e->max_x)
-                                           && (y >= e->min_y) && (y <= e->max_y));
-        if (!is_alive) p->state = 0;
         return 0;
     }
     case XTG_CLS_CAVITY: {
@@ -1625,9 +1660,11 @@ int32_t xto_validate(const xtg_element* els, int64_t n, char* msg, int64_t msg_l
         else if (e->slice < 0 || e->slice > XTG_SLICE_EXIT) why = "unknown slice kind";
         else if (e->order < 0 || e->order >= XTG_MAX_KNL) why = "multipole order out of range";
         else if (e->order_rel < -1 || e->order_rel >= 20) why = "relative multipole order out of range (0..19)";
-        else if (e->shift_x != 0 || e->shift_y != 0 || e->shift_s != 0 || e->rot_x_rad != 0
-                 || e->rot_y_rad != 0 || e->rot_s_rad != 0 || e->rot_s_rad_no_frame != 0)
-            why = "misalignments (shift/rotation) are not supported";
+        else if (((e->shift_x != 0 || e->shift_y != 0) && e->cls != XTG_CLS_LIMIT_RECT &&
+                  e->cls != XTG_CLS_LIMIT_ELLIPSE && e->cls != XTG_CLS_LIMIT_POLYGON)
+                 || e->shift_s != 0 || e->rot_x_rad != 0 || e->rot_y_rad != 0 || e->rot_s_rad != 0
+                 || e->rot_s_rad_no_frame != 0)
+            why = "misalignments (shift/rotation) are not supported (transverse shifts: apertures only)";
         else if (e->cls >= XTG_CLS_MULTIPOLE && e->cls <= XTG_CLS_OCTUPOLE) {
             int64_t model = e->model;
             if (e->cls == XTG_CLS_MULTIPOLE && e->isthick <= 0) model = -1;

@@ -3,11 +3,11 @@ the reference's test data (test_data/sps_w_spacecharge/
 line_no_spacecharge_and_particle.json), loaded through
 xtrack_gb300.serialization (the reference's JSON format).
 
-The line's Drift, DipoleEdge, Multipole, LimitRect, LimitEllipse, Cavity
-and Marker elements are inside the push's element set; the one aperture
-with a transverse shift (a LimitRect with shift_x, misalignment
-transformations being outside the push) is dropped, leaving 8199. The
-fixture stores the packed raw element records, 128 particles spread
+Every element of the line is inside the push's element set: 8200 Drift,
+DipoleEdge, Multipole, LimitRect (one of them shifted in x), LimitEllipse,
+Cavity and Marker elements. Elements with transformations outside the
+push (longitudinal shifts, rotations, or shifts of non-apertures) would
+be dropped and listed; this line has none. The fixture stores the packed raw element records, 128 particles spread
 around the file's particle wide enough that the apertures take some of
 them, and their state after 20 turns of the reference-compiled code
 (oracle/_ref), so state, at_turn and at_element of real aperture losses
@@ -37,8 +37,15 @@ KEEP = ("x", "px", "y", "py", "zeta", "delta", "ptau", "rpp", "rvv", "s", "state
 TURNS = 20
 
 
-SHIFTS = ("shift_x", "shift_y", "shift_s", "rot_x_rad", "rot_y_rad", "rot_s_rad",
-          "rot_s_rad_no_frame")
+APERTURES = ("LimitRect", "LimitEllipse", "LimitPolygon")
+UNSUPPORTED = ("shift_s", "rot_x_rad", "rot_y_rad", "rot_s_rad", "rot_s_rad_no_frame")
+
+
+def _unsupported(e):
+    if any(e.get(k, 0) != 0 for k in UNSUPPORTED):
+        return True
+    shifted = e.get("shift_x", 0) != 0 or e.get("shift_y", 0) != 0
+    return shifted and e["__class__"] not in APERTURES
 
 
 def load_line():
@@ -46,7 +53,7 @@ def load_line():
         d = json.load(f)
     ln = d["line"]
     els = ln["elements"]
-    dropped = [n for n in ln["element_names"] if any(els[n].get(k, 0) != 0 for k in SHIFTS)]
+    dropped = [n for n in ln["element_names"] if _unsupported(els[n])]
     names = [n for n in ln["element_names"] if n not in dropped]
     sub = {"elements": {n: els[n] for n in set(names)}, "element_names": names}
     line = serialization.line_from_dict(sub)

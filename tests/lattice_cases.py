@@ -73,6 +73,11 @@ def element_zoo(seed=3):
     add("de_off", xt.DipoleEdge(k=5e-3, e1=0.02, model="suppressed"))
     add("ell", xt.LimitEllipse(a=0.03, b=0.02))
     add("rect", xt.LimitRect(min_x=-0.03, max_x=0.028, min_y=-0.02, max_y=0.021))
+    # shifted apertures (transformations of the reference with only shift_x,
+    # shift_y nonzero); particles lost there keep the shifted frame
+    add("rect_shift", xt.LimitRect(min_x=-0.02, max_x=0.02, min_y=-0.015, max_y=0.015,
+                                   shift_x=4e-3, shift_y=-1e-3))
+    add("ell_shift", xt.LimitEllipse(a=0.025, b=0.018, shift_y=2e-3))
     return xt.Line(elements=els, element_names=names)
 
 
@@ -156,3 +161,15 @@ def small_beam(n, p0c=7e12, seed=0, scale=1.0):
     return dict(p0c=p0c, x=rng.normal(0, 1e-3 * scale, n), px=rng.normal(0, 1e-5 * scale, n),
                 y=rng.normal(0, 1e-3 * scale, n), py=rng.normal(0, 1e-5 * scale, n),
                 zeta=rng.normal(0, 0.05 * scale, n), delta=rng.normal(0, 1e-4 * scale, n))
+
+
+def shifted_apertures():
+    """Drifts and transversely shifted apertures that a wide beam hits."""
+    els = [xt.Drift(length=0.5),
+           xt.LimitRect(min_x=-0.01, max_x=0.012, min_y=-0.008, max_y=0.008, shift_x=3e-3,
+                        shift_y=-1.5e-3),
+           xt.Drift(length=0.7),
+           xt.LimitEllipse(a=0.015, b=0.01, shift_x=-2e-3, shift_y=1e-3),
+           xt.Drift(length=0.3),
+           xt.LimitRect(min_x=-0.02, max_x=0.02, min_y=-0.02, max_y=0.02, shift_y=5e-3)]
+    return xt.Line(elements=els)

@@ -34,7 +34,7 @@ import pytest
 import pyoracle
 import xtrack_gb300 as xt
 from xtrack_gb300 import _abi, workloads
-from lattice_cases import element_zoo, sliced_line, small_beam
+from lattice_cases import element_zoo, shifted_apertures, sliced_line, small_beam
 from xtg_testutil import compare, compare_within_spread, fma_spread, gpu_track, make_monitor
 
 pytestmark = pytest.mark.gpu
@@ -349,6 +349,18 @@ def test_aperture_compare_edge_values(arith):
             for f in ("state", "at_element", "at_turn"):
                 assert np.array_equal(got[f], ref[f]), (glim, flags, f)
             assert len(set(ref["state"].tolist())) > 1
+
+
+@pytest.mark.parametrize("arith", ["exact", "fast"])
+@pytest.mark.parametrize("flags", [0, 1 << 0, 1 << 4])
+def test_shifted_apertures(arith, flags):
+    """Shifted apertures on the GPU against the oracle (itself pinned to the
+    reference's transformation wrapper)."""
+    recs, arrs, L = _setup(shifted_apertures(), small_beam(400, seed=13, scale=8.0))
+    got, ref = _run_both(recs, arrs, L, arith=arith, num_turns=2, track_flags=flags)
+    for f in ("state", "at_turn", "at_element"):
+        assert np.array_equal(got[f], ref[f]), f
+    compare(got, ref, 1e-14 if arith == "exact" else 1e-12)
 
 
 def test_batch_matches_per_seed_oracle():

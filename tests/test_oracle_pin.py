@@ -9,7 +9,7 @@ import pytest
 import pyoracle
 import xtrack_gb300 as xt
 from xtrack_gb300 import workloads
-from lattice_cases import element_zoo, fringe_zoo, sliced_line, small_beam
+from lattice_cases import element_zoo, fringe_zoo, shifted_apertures, sliced_line, small_beam
 
 pyoracle.ensure_built(with_ref=True)
 pytestmark = pytest.mark.skipif(not pyoracle.ref_available(),
@@ -91,6 +91,19 @@ def test_freeze_longitudinal(case, flags):
     # without the freeze the same call changes the longitudinal coordinates
     c, _ = _both(line, beam, num_turns=3, track_flags=flags)
     assert np.any(c["zeta"] != p0["zeta"])
+
+
+@pytest.mark.parametrize("flags", [0, 1 << 0, 1 << 4])
+def test_shifted_apertures(flags):
+    """Apertures with shift_x / shift_y through the reference's own
+    transformation wrapper: survivors are shifted back, particles lost
+    there keep the shifted frame, and with local apertures ignored the
+    shifts still apply; bit for bit."""
+    a, b = _both(shifted_apertures(), small_beam(400, seed=13, scale=8.0), num_turns=2,
+                 track_flags=flags)
+    _assert_identical(a, b)
+    if flags == 0:
+        assert 50 < np.sum(a["state"] == 0) < 350
 
 
 @pytest.mark.parametrize("thin", [True, False])

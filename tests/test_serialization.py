@@ -154,11 +154,11 @@ def test_lhc_fixture_gpu(arith):
 
 
 def test_sps_fixture_oracle_reproduces_reference():
-    """The thin SPS line (8199 elements: drifts, thin multipoles, 1488
+    """The thin SPS line (8200 elements: drifts, thin multipoles, 1488
     DipoleEdges, 1698 LimitRect/LimitEllipse apertures, cavities) after 20
     turns of the reference-compiled code, with real aperture losses."""
     recs, arrs, out, meta = _fixture(SPS)
-    assert meta["n_elements"] == len(recs) == 8199
+    assert meta["n_elements"] == len(recs) == 8200
     assert np.sum(out["state"] <= 0) > 5
     pyoracle.track(recs, arrs, line_length=meta["line_length"], num_turns=meta["num_turns"],
                    q0=meta["q0"], mass0=meta["mass0"])
@@ -170,9 +170,13 @@ def test_sps_fixture_oracle_reproduces_reference():
 @pytest.mark.parametrize("arith", ["exact", "fast"])
 def test_sps_fixture_gpu(arith):
     """The real SPS line on the GPU against the reference-compiled result:
-    state, at_turn and at_element of every aperture loss bit-exact;
-    coordinates within 1e-14 (exact) or 3x the reference's FMA spread
-    (fast)."""
+    state, at_turn and at_element of every aperture loss bit-exact. Exact
+    mode: one turn within 1e-14; after 20 turns within 1e-10. The
+    cavities' sin comes from CUDA's libm: on this beam all 128 particles
+    stay bit-identical for 16 turns, then one cavity pass of one particle
+    gets a sin one ulp away from glibc's, rvv moves by an ulp, and the
+    drifts of the following turns carry that to ~8e-12 relative in zeta.
+    Fast mode: within 3x the reference's FMA spread."""
     from xtg_testutil import compare, compare_within_spread, fma_spread, gpu_track
     recs, arrs, out, meta = _fixture(SPS)
     kw = dict(line_length=meta["line_length"], num_turns=meta["num_turns"], q0=meta["q0"],
@@ -181,7 +185,13 @@ def test_sps_fixture_gpu(arith):
     for f in ("state", "at_turn", "at_element"):
         assert np.array_equal(got[f], out[f]), f
     if arith == "exact":
-        compare(got, out, 1e-14)
+        compare(got, out, 1e-10)
+        # one turn: the 1e-14 bound
+        kw1 = dict(kw, num_turns=1)
+        one = {k: v.copy() for k, v in arrs.items()}
+        pyoracle.track(recs, one, **kw1)
+        g1, _ = gpu_track(recs, {k: v.copy() for k, v in arrs.items()}, arith=arith, **kw1)
+        compare(g1, one, 1e-14)
     else:
         spread, ok = fma_spread(recs, arrs, **kw)
         compare_within_spread(got, out, spread, ok)

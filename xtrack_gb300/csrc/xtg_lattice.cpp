@@ -417,9 +417,13 @@ int32_t validate_element(const xtg_element& e, int64_t idx, std::string* why) {
     if (e.order < 0 || e.order >= XTG_MAX_KNL) return fail("multipole order out of range");
     if (e.order_rel < -1 || e.order_rel >= 20)
         return fail("relative multipole order out of range (0..19)");
-    if (e.shift_x != 0 || e.shift_y != 0 || e.shift_s != 0 || e.rot_x_rad != 0 ||
-        e.rot_y_rad != 0 || e.rot_s_rad != 0 || e.rot_s_rad_no_frame != 0)
-        return fail("misalignments (shift/rotation) are not supported");
+    bool const aperture = e.cls == XTG_CLS_LIMIT_RECT || e.cls == XTG_CLS_LIMIT_ELLIPSE ||
+                          e.cls == XTG_CLS_LIMIT_POLYGON;
+    if (!aperture && (e.shift_x != 0 || e.shift_y != 0))
+        return fail("misalignments (shift/rotation) are not supported (transverse shifts: apertures only)");
+    if (e.shift_s != 0 || e.rot_x_rad != 0 || e.rot_y_rad != 0 || e.rot_s_rad != 0 ||
+        e.rot_s_rad_no_frame != 0)
+        return fail("misalignments (shift/rotation) are not supported (transverse shifts: apertures only)");
     if (e.cls >= XTG_CLS_MULTIPOLE && e.cls <= XTG_CLS_OCTUPOLE) {
         int64_t model = e.model;
         if (e.cls == XTG_CLS_MULTIPOLE && e.isthick <= 0) model = -1;
@@ -1056,6 +1060,30 @@ int32_t pack_lattice(const xtg_element* els, int64_t n, const xtg_config& cfg,
                 pack_magnet(e, backtrack, cfg.arith == XTG_ARITH_EXACT, &rb);
             }
             break;
+        }
+        if ((e.cls == XTG_CLS_LIMIT_RECT || e.cls == XTG_CLS_LIMIT_ELLIPSE ||
+             e.cls == XTG_CLS_LIMIT_POLYGON) && (e.shift_x != 0.0 || e.shift_y != 0.0)) {
+            // entry and exit XYShift of track_misalignment_entry/exit_straight
+            // with zero anchor, rotations and shift_s
+            double const mis_in_x = e.shift_x - 0.0, mis_in_y = e.shift_y - 0.0;
+            double const mis_out_x = 0.0 - e.shift_x, mis_out_y = 0.0 - e.shift_y;
+            ApertureShift sh;
+            if (!backtrack) {
+                sh.in_x = -mis_in_x;
+                sh.in_y = -mis_in_y;
+                sh.out_x = -mis_out_x;
+                sh.out_y = -mis_out_y;
+            } else {
+                sh.in_x = -(-mis_out_x);
+                sh.in_y = -(-mis_out_y);
+                sh.out_x = -(-mis_in_x);
+                sh.out_y = -(-mis_in_y);
+            }
+            rb.pad16();
+            size_t const off = rb.bytes.size();
+            rb.bytes.resize(off + sizeof(ApertureShift));
+            std::memcpy(rb.bytes.data() + off, &sh, sizeof(sh));
+            rb.head<RecHeader>()->flags |= F_SHIFTED;
         }
         rb.pad16();
         rb.head<RecHeader>()->nbytes = (int32_t)rb.bytes.size();

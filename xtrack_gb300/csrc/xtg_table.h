@@ -45,6 +45,8 @@ enum Op : int32_t {
 // RecHeader.flags
 enum : int32_t {
     F_GLOBAL_APER = 1,    // statically thick class: global aperture follows
+    F_SHIFTED = 2,        // aperture with a transverse shift: the last 32 bytes of
+                          // the record are the ApertureShift block
 };
 
 struct alignas(16) RecHeader {
@@ -70,6 +72,18 @@ struct alignas(16) LimitEllipseRec {
     double a_squ, b_squ;
     int64_t key_a_b_squ;
     int64_t reserved;
+};
+
+// Transverse shift of an aperture (track_local_particle_with_transformations.h
+// with only shift_x / shift_y nonzero; track_misalignments.h:38-112 and
+// track_xyshift.h): the values the entry and exit XYShift add to x and y,
+// as the reference forms them (-(dx - 0) at entry, -(0 - dx) at exit;
+// swapped and negated in backtracking tables). The entry applies to every
+// particle reaching the aperture, the exit only to those that survive it
+// (the CPU per-particle blocks skip lost particles), and both apply when
+// local apertures are ignored.
+struct ApertureShift {
+    double in_x, in_y, out_x, out_y;
 };
 
 // LimitRect (limitrect.h:9-36): the bounds as ordered integer keys of their

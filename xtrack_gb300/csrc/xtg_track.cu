@@ -357,6 +357,26 @@ __device__ __noinline__ void multi_element_monitor(const xtg_multi_element_monit
         }
     }
 }
+// Transverse shift of an aperture record (F_SHIFTED, ApertureShift in
+// xtg_table.h): the entry XYShift for the particle reaching the aperture,
+// the exit XYShift only if it survives; both also when local apertures are
+// ignored. The block is found again from the header at the exit, so that
+// nothing stays live across the check.
+__device__ __forceinline__ void aperture_shift_in(PState& p, const unsigned char* rec, const RecHeader& h) {
+    if (h.flags & F_SHIFTED) {
+        const ApertureShift& sh = *reinterpret_cast<const ApertureShift*>(rec + h.nbytes - sizeof(ApertureShift));
+        p.x = p.x + sh.in_x;
+        p.y = p.y + sh.in_y;
+    }
+}
+__device__ __forceinline__ void aperture_shift_out(PState& p, const unsigned char* rec, const RecHeader& h) {
+    if ((h.flags & F_SHIFTED) && p.state > 0) {
+        const ApertureShift& sh = *reinterpret_cast<const ApertureShift*>(rec + h.nbytes - sizeof(ApertureShift));
+        p.x = p.x + sh.out_x;
+        p.y = p.y + sh.out_y;
+    }
+}
+
 template <bool kExact>
 __device__ __forceinline__ bool apply_record(PState& p, const unsigned char* __restrict__ rec,
                                              const TrackArgs& a, const RfCtx& rf, int64_t i, int64_t pid) {
@@ -404,16 +424,19 @@ __device__ __forceinline__ bool apply_record(PState& p, const unsigned char* __r
     }
     case OP_LIMIT_ELLIPSE: {
         // limitellipse.h:12-38
+        aperture_shift_in(p, rec, h);
         if (!flag_on(a.track_flags, XTG_FLAG_IGNORE_LOCAL_APERTURE)) {
             const LimitEllipseRec& r = *reinterpret_cast<const LimitEllipseRec*>(rec);
             double const temp = p.x * p.x * r.b_squ + p.y * p.y * r.a_squ;
             int64_t const kt = ord_key(temp);
             if (!(kt >= lower_key(0.0) && kt <= r.key_a_b_squ)) p.state = 0;
         }
+        aperture_shift_out(p, rec, h);
         break;
     }
     case OP_LIMIT_RECT: {
         // limitrect.h:9-36
+        aperture_shift_in(p, rec, h);
         if (!flag_on(a.track_flags, XTG_FLAG_IGNORE_LOCAL_APERTURE)) {
             // the FP64 compares of the reference as integer compares of
             // ordered keys (ord_key, xtg_table.h): same outcome, NaN lost
@@ -423,10 +446,12 @@ __device__ __forceinline__ bool apply_record(PState& p, const unsigned char* __r
                                (ky <= r.key_max_y);
             if (!alive) p.state = 0;
         }
+        aperture_shift_out(p, rec, h);
         break;
     }
     case OP_LIMIT_POLYGON: {
         // limitpolygon.h:64-90 (crossing-number test)
+        aperture_shift_in(p, rec, h);
         if (!flag_on(a.track_flags, XTG_FLAG_IGNORE_LOCAL_APERTURE)) {
             const LimitPolygonRec& r = *reinterpret_cast<const LimitPolygonRec*>(rec);
             const double* vx = reinterpret_cast<const double*>(rec + sizeof(LimitPolygonRec));
@@ -446,6 +471,7 @@ __device__ __forceinline__ bool apply_record(PState& p, const unsigned char* __r
                 if (!alive) p.state = 0;
             }
         }
+        aperture_shift_out(p, rec, h);
         break;
     }
     case OP_MON_PARTICLES: {

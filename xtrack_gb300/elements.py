@@ -63,6 +63,9 @@ class BeamElement:
         rec["weight"] = 1.0
         rec["order_rel"] = -1
         self._fill(rec)
+        # transverse shift (apertures: track_local_particle_with_transformations.h)
+        rec["shift_x"] = getattr(self, "shift_x", 0.0)
+        rec["shift_y"] = getattr(self, "shift_y", 0.0)
         return rec
 
     def copy(self):
@@ -453,7 +456,10 @@ class LimitEllipse(BeamElement):
     """Elliptical aperture (limit_ellipse.py:12-94)."""
     _cls = _abi.CLS_LIMIT_ELLIPSE
 
-    def __init__(self, a=None, b=None, a_squ=None, b_squ=None, a_b_squ=None):
+    def __init__(self, a=None, b=None, a_squ=None, b_squ=None, a_b_squ=None, shift_x=0.0,
+                 shift_y=0.0):
+        self.shift_x = float(shift_x)
+        self.shift_y = float(shift_y)
         if a is None and a_squ is None:
             a = UNLIMITED
         if b is None and b_squ is None:
@@ -492,7 +498,10 @@ class LimitRect(BeamElement):
     """Rectangular aperture (limit_rect.py)."""
     _cls = _abi.CLS_LIMIT_RECT
 
-    def __init__(self, min_x=-UNLIMITED, max_x=UNLIMITED, min_y=-UNLIMITED, max_y=UNLIMITED):
+    def __init__(self, min_x=-UNLIMITED, max_x=UNLIMITED, min_y=-UNLIMITED, max_y=UNLIMITED,
+                 shift_x=0.0, shift_y=0.0):
+        self.shift_x = float(shift_x)
+        self.shift_y = float(shift_y)
         self.min_x = float(min_x)
         self.max_x = float(max_x)
         self.min_y = float(min_y)
@@ -610,7 +619,9 @@ class LimitPolygon(BeamElement):
     vertices (limitpolygon.h:13-90)."""
     _cls = _abi.CLS_LIMIT_POLYGON
 
-    def __init__(self, x_vertices=None, y_vertices=None):
+    def __init__(self, x_vertices=None, y_vertices=None, shift_x=0.0, shift_y=0.0):
+        self.shift_x = float(shift_x)
+        self.shift_y = float(shift_y)
         x = np.ascontiguousarray(x_vertices, dtype=np.float64)
         y = np.ascontiguousarray(y_vertices, dtype=np.float64)
         if x.shape != y.shape or x.ndim != 1 or len(x) < 3:

@@ -49,9 +49,9 @@ _ACCEPT = {
                  "edge_exit_active") + _MAGNET_KEYS,
     "Cavity": ("voltage", "frequency", "lag", "phase", "harmonic", "length", "absolute_time",
                "num_kicks", "model", "integrator"),
-    "LimitEllipse": ("a_squ", "b_squ", "a_b_squ", "a", "b"),
-    "LimitRect": ("min_x", "max_x", "min_y", "max_y"),
-    "LimitPolygon": ("x_vertices", "y_vertices"),
+    "LimitEllipse": ("a_squ", "b_squ", "a_b_squ", "a", "b", "shift_x", "shift_y"),
+    "LimitRect": ("min_x", "max_x", "min_y", "max_y", "shift_x", "shift_y"),
+    "LimitPolygon": ("x_vertices", "y_vertices", "shift_x", "shift_y"),
     "DipoleEdge": ("k", "e1", "e1_fd", "hgap", "fint", "model", "side"),
 }
 
@@ -74,7 +74,7 @@ def element_from_dict(dct, name="?"):
     for k, v in d.items():
         if k in _DERIVED:
             continue
-        if k in _NEUTRAL:
+        if k in _NEUTRAL and k not in _ACCEPT[cname]:
             if not _is_neutral(v, _NEUTRAL[k]):
                 raise ValueError(f"element {name!r} ({cname}): field {k}={v!r} is not supported "
                                  f"(only {_NEUTRAL[k]!r})")
@@ -116,14 +116,16 @@ def element_to_dict(e):
                    harmonic=e.harmonic, length=e.length, absolute_time=e.absolute_time,
                    num_kicks=e.num_kicks, model=e._model, integrator=e._integrator)
         return out
-    if isinstance(e, el.LimitEllipse):
-        out.update(a_squ=e.a_squ, b_squ=e.b_squ, a_b_squ=e.a_b_squ)
-        return out
-    if isinstance(e, el.LimitRect):
-        out.update(min_x=e.min_x, max_x=e.max_x, min_y=e.min_y, max_y=e.max_y)
-        return out
-    if isinstance(e, el.LimitPolygon):
-        out.update(x_vertices=e.x_vertices.tolist(), y_vertices=e.y_vertices.tolist())
+    if isinstance(e, (el.LimitEllipse, el.LimitRect, el.LimitPolygon)):
+        if isinstance(e, el.LimitEllipse):
+            out.update(a_squ=e.a_squ, b_squ=e.b_squ, a_b_squ=e.a_b_squ)
+        elif isinstance(e, el.LimitRect):
+            out.update(min_x=e.min_x, max_x=e.max_x, min_y=e.min_y, max_y=e.max_y)
+        else:
+            out.update(x_vertices=e.x_vertices.tolist(), y_vertices=e.y_vertices.tolist())
+        for f in ("shift_x", "shift_y"):
+            if getattr(e, f) != 0.0:
+                out[f] = getattr(e, f)
         return out
     if isinstance(e, el.DipoleEdge):
         # dipole_edge.py to_dict: nonzero scalars, model and side when not default
