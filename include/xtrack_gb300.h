@@ -59,7 +59,8 @@ extern "C" {
 #define XTG_CLS_MONITOR        10   /* monitors/*.py placed in the line      */
 #define XTG_CLS_LIMIT_POLYGON  11   /* limit_polygon.py, limitpolygon.h      */
 #define XTG_CLS_DIPOLE_EDGE    12   /* dipole_edge.py, dipoleedge.h          */
-#define XTG_NUM_CLS            13
+#define XTG_CLS_LIMIT_RECT_ELLIPSE 13 /* limit_rect_ellipse.py, limitrectellipse.h */
+#define XTG_NUM_CLS            14
 
 /* Slice kind of a record (slice classes of slice_elements_*.py). A slice
  * record carries its parent's parameters plus its own `weight`. */

@@ -200,6 +200,7 @@ XTR_CLASS(Octupole)
 XTR_CLASS(Cavity)
 XTR_CLASS(LimitEllipse)
 XTR_CLASS(LimitRect)
+XTR_CLASS(LimitRectEllipse)
 XTR_CLASS(ThickSliceBend) XTR_CLASS(ThinSliceBend) XTR_CLASS(DriftSliceBend)
 XTR_CLASS(ThinSliceBendEntry) XTR_CLASS(ThinSliceBendExit)
 XTR_CLASS(ThickSliceQuadrupole) XTR_CLASS(ThinSliceQuadrupole) XTR_CLASS(DriftSliceQuadrupole)
@@ -234,6 +235,7 @@ XTR_GET_I(DipoleEdge, model, el->model) XTR_GET_I(DipoleEdge, side, el->side)
 #include "xtrack/beam_elements/elements_src/limitellipse.h"
 #include "xtrack/beam_elements/elements_src/limitrect.h"
 #include "xtrack/beam_elements/elements_src/dipoleedge.h"
+#include "xtrack/beam_elements/elements_src/limitrectellipse.h"
 
 /* The apertures through the reference's transformation wrapper, as its
  * kernel calls every element (base_element.py:83-126): the entry and exit
@@ -244,6 +246,11 @@ XTR_GET_I(DipoleEdge, model, el->model) XTR_GET_I(DipoleEdge, side, el->side)
 #undef ALLOW_ROT_AND_SHIFT
 #undef ELEMENT_NAME
 #define ELEMENT_NAME LimitEllipse
+#define ALLOW_ROT_AND_SHIFT 1
+#include "xtrack/headers/track_local_particle_with_transformations.h"
+#undef ALLOW_ROT_AND_SHIFT
+#undef ELEMENT_NAME
+#define ELEMENT_NAME LimitRectEllipse
 #define ALLOW_ROT_AND_SHIFT 1
 #include "xtrack/headers/track_local_particle_with_transformations.h"
 #undef ALLOW_ROT_AND_SHIFT
@@ -294,6 +301,7 @@ static int xtr_apply(const xtg_element* e, LocalParticle* lp) {
     case XTG_CLS_LIMIT_ELLIPSE: LimitEllipse_track_local_particle_with_transformations(e, lp); return 0;
     case XTG_CLS_LIMIT_RECT: LimitRect_track_local_particle_with_transformations(e, lp); return 0;
     case XTG_CLS_DIPOLE_EDGE: DipoleEdge_track_local_particle(e, lp); return 0;
+    case XTG_CLS_LIMIT_RECT_ELLIPSE: LimitRectEllipse_track_local_particle_with_transformations(e, lp); return 0;
     case XTG_CLS_MULTIPOLE: XTR_SLICES(Multipole, 0) return 0;
     case XTG_CLS_BEND: XTR_EDGES(Bend) XTR_SLICES(Bend, 1) return 0;
     case XTG_CLS_QUADRUPOLE: XTR_EDGES(Quadrupole) XTR_SLICES(Quadrupole, 1) return 0;

@@ -1364,6 +1364,17 @@ static void xto_profile(const xtg_element_monitor* m, const xto_part* p) {
  * particle's current x, y (limitellipse.h, limitpolygon.h, limitrect.h). */
 static void xto_aperture(const xtg_element* e, xto_part* p) {
     switch (e->cls) {
+    case XTG_CLS_LIMIT_RECT_ELLIPSE: {
+        /* limitrectellipse.h:14-44 */
+        if (flag_set(p, XTG_FLAG_IGNORE_LOCAL_APERTURE)) return;
+        double const max_x = e->max_x, max_y = e->max_y;
+        double const x = p->x, y = p->y;
+        double const temp = x * x * e->b_squ + y * y * e->a_squ;
+        int64_t const is_alive = (int64_t)((x <= max_x) && (x >= -max_x) && (y <= max_y) &&
+                                           (y >= -max_y) && (temp <= e->a_b_squ));
+        if (!is_alive) p->state = 0;
+        return;
+    }
     case XTG_CLS_LIMIT_ELLIPSE: {
         /* limitellipse.h:12-38 */
         if (flag_set(p, XTG_FLAG_IGNORE_LOCAL_APERTURE)) return;
@@ -1466,6 +1477,7 @@ static int xto_apply(const xtg_element* e, const xtg_config* cfg, xto_part* p,
     }
     case XTG_CLS_LIMIT_ELLIPSE:
     case XTG_CLS_LIMIT_POLYGON:
+    case XTG_CLS_LIMIT_RECT_ELLIPSE:
     case XTG_CLS_LIMIT_RECT: {
         /* track_local_particle_with_transformations.h:146-165 with only
          * shift_x / shift_y nonzero (track_misalignments.h:38-112): the entry
@@ -1661,7 +1673,8 @@ int32_t xto_validate(const xtg_element* els, int64_t n, char* msg, int64_t msg_l
         else if (e->order < 0 || e->order >= XTG_MAX_KNL) why = "multipole order out of range";
         else if (e->order_rel < -1 || e->order_rel >= 20) why = "relative multipole order out of range (0..19)";
         else if (((e->shift_x != 0 || e->shift_y != 0) && e->cls != XTG_CLS_LIMIT_RECT &&
-                  e->cls != XTG_CLS_LIMIT_ELLIPSE && e->cls != XTG_CLS_LIMIT_POLYGON)
+                  e->cls != XTG_CLS_LIMIT_ELLIPSE && e->cls != XTG_CLS_LIMIT_POLYGON &&
+                  e->cls != XTG_CLS_LIMIT_RECT_ELLIPSE)
                  || e->shift_s != 0 || e->rot_x_rad != 0 || e->rot_y_rad != 0 || e->rot_s_rad != 0
                  || e->rot_s_rad_no_frame != 0)
             why = "misalignments (shift/rotation) are not supported (transverse shifts: apertures only)";

@@ -78,6 +78,7 @@ def element_zoo(seed=3):
     add("rect_shift", xt.LimitRect(min_x=-0.02, max_x=0.02, min_y=-0.015, max_y=0.015,
                                    shift_x=4e-3, shift_y=-1e-3))
     add("ell_shift", xt.LimitEllipse(a=0.025, b=0.018, shift_y=2e-3))
+    add("rect_ell", xt.LimitRectEllipse(max_x=0.022, max_y=0.017, a=0.026, b=0.02))
     return xt.Line(elements=els, element_names=names)
 
 
@@ -171,5 +172,7 @@ def shifted_apertures():
            xt.Drift(length=0.7),
            xt.LimitEllipse(a=0.015, b=0.01, shift_x=-2e-3, shift_y=1e-3),
            xt.Drift(length=0.3),
-           xt.LimitRect(min_x=-0.02, max_x=0.02, min_y=-0.02, max_y=0.02, shift_y=5e-3)]
+           xt.LimitRect(min_x=-0.02, max_x=0.02, min_y=-0.02, max_y=0.02, shift_y=5e-3),
+           xt.Drift(length=0.2),
+           xt.LimitRectEllipse(max_x=0.016, max_y=0.013, a=0.019, b=0.016, shift_x=1e-3)]
     return xt.Line(elements=els)

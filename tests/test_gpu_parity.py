@@ -333,7 +333,9 @@ def test_aperture_compare_edge_values(arith):
     rects = [xt.LimitRect(min_x=0.0, max_x=0.01, min_y=-0.02, max_y=-0.0), xt.Drift(length=0.0),
              xt.LimitRect(min_x=-0.0, max_x=0.02, min_y=-0.02, max_y=0.0), xt.Drift(length=0.0)]
     ellipses = [xt.LimitEllipse(a=0.01, b=0.02), xt.Drift(length=0.0),
-                xt.LimitEllipse(a=0.02, b=0.004), xt.Drift(length=0.0)]
+                xt.LimitEllipse(a=0.02, b=0.004), xt.Drift(length=0.0),
+                xt.LimitRectEllipse(max_x=0.01, max_y=0.004, a=0.02, b=0.0041),
+                xt.Drift(length=0.0)]
     beam = xt.Particles(device="cpu", p0c=7e12, x=xs.ravel(), y=ys.ravel(), px=np.zeros(n),
                         py=np.zeros(n))
     arrs = pyoracle.host_arrays(beam.to_numpy())

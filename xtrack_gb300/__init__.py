@@ -7,7 +7,8 @@ library ``libxtrack_gb300.so`` (see include/xtrack_gb300.h).
 """
 from .particles import Particles, PROTON_MASS_EV, ELECTRON_MASS_EV, LAST_INVALID_STATE
 from .elements import (Marker, Drift, Multipole, Bend, Quadrupole, Sextupole, Octupole,
-                       Cavity, LimitEllipse, LimitRect, LimitPolygon, DipoleEdge, BeamElement)
+                       Cavity, LimitEllipse, LimitRect, LimitRectEllipse, LimitPolygon, DipoleEdge,
+                       BeamElement)
 from .elements import *  # noqa: F401,F403  (slice classes)
 from .monitors import (ParticlesMonitor, LastTurnsMonitor, BeamPositionMonitor, BeamSizeMonitor,
                        BeamProfileMonitor, MultiElementMonitor)

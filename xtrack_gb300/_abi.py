@@ -40,6 +40,7 @@ CLS_LIMIT_RECT = 9
 CLS_MONITOR = 10
 CLS_LIMIT_POLYGON = 11
 CLS_DIPOLE_EDGE = 12
+CLS_LIMIT_RECT_ELLIPSE = 13
 
 SLICE_NONE = 0
 SLICE_THICK = 1

@@ -418,7 +418,7 @@ int32_t validate_element(const xtg_element& e, int64_t idx, std::string* why) {
     if (e.order_rel < -1 || e.order_rel >= 20)
         return fail("relative multipole order out of range (0..19)");
     bool const aperture = e.cls == XTG_CLS_LIMIT_RECT || e.cls == XTG_CLS_LIMIT_ELLIPSE ||
-                          e.cls == XTG_CLS_LIMIT_POLYGON;
+                          e.cls == XTG_CLS_LIMIT_POLYGON || e.cls == XTG_CLS_LIMIT_RECT_ELLIPSE;
     if (!aperture && (e.shift_x != 0 || e.shift_y != 0))
         return fail("misalignments (shift/rotation) are not supported (transverse shifts: apertures only)");
     if (e.shift_s != 0 || e.rot_x_rad != 0 || e.rot_y_rad != 0 || e.rot_s_rad != 0 ||
@@ -1032,6 +1032,19 @@ int32_t pack_lattice(const xtg_element* els, int64_t n, const xtg_config& cfg,
             }
             break;
         }
+        case XTG_CLS_LIMIT_RECT_ELLIPSE: {
+            rb.init(sizeof(LimitRectEllipseRec));
+            LimitRectEllipseRec* r = rb.head<LimitRectEllipseRec>();
+            r->h.op = OP_LIMIT_RECT_ELLIPSE;
+            r->key_min_x = lower_key(-e.max_x);
+            r->key_max_x = upper_key(e.max_x);
+            r->key_min_y = lower_key(-e.max_y);
+            r->key_max_y = upper_key(e.max_y);
+            r->a_squ = e.a_squ;
+            r->b_squ = e.b_squ;
+            r->key_a_b_squ = upper_key(e.a_b_squ);
+            break;
+        }
         case XTG_CLS_LIMIT_RECT: {
             rb.init(sizeof(LimitRectRec));
             LimitRectRec* r = rb.head<LimitRectRec>();
@@ -1062,7 +1075,8 @@ int32_t pack_lattice(const xtg_element* els, int64_t n, const xtg_config& cfg,
             break;
         }
         if ((e.cls == XTG_CLS_LIMIT_RECT || e.cls == XTG_CLS_LIMIT_ELLIPSE ||
-             e.cls == XTG_CLS_LIMIT_POLYGON) && (e.shift_x != 0.0 || e.shift_y != 0.0)) {
+             e.cls == XTG_CLS_LIMIT_POLYGON || e.cls == XTG_CLS_LIMIT_RECT_ELLIPSE) &&
+            (e.shift_x != 0.0 || e.shift_y != 0.0)) {
             // entry and exit XYShift of track_misalignment_entry/exit_straight
             // with zero anchor, rotations and shift_s
             double const mis_in_x = e.shift_x - 0.0, mis_in_y = e.shift_y - 0.0;
@@ -1115,6 +1129,7 @@ double canonical_flops(const unsigned char* rec) {
         return r->exact ? drift_exact : drift_exp;
     }
     case OP_LIMIT_ELLIPSE:
+    case OP_LIMIT_RECT_ELLIPSE:
         return 5.0;                    // 2 mul, 1 fma-free mul-add pair
     case OP_LIMIT_RECT:
         return 0.0;

@@ -40,6 +40,7 @@ enum Op : int32_t {
     OP_MON_PROFILE = 10,
     OP_LIMIT_POLYGON = 11,
     OP_DIPOLE_EDGE = 12,  // DipoleEdge (dipoleedge.h): linear or full model
+    OP_LIMIT_RECT_ELLIPSE = 13,
 };
 
 // RecHeader.flags
@@ -117,6 +118,16 @@ XTG_HD_INLINE int64_t upper_key(double hi) {
     if (hi != hi) return (int64_t)(-0x7FFFFFFFFFFFFFFFLL - 1);
     return ord_key(hi == 0.0 ? 0.0 : hi);
 }
+
+// LimitRectEllipse (limitrectellipse.h:14-44): the symmetric rectangle
+// (+-max_x, +-max_y) and the ellipse, all compares on ordered keys.
+struct alignas(16) LimitRectEllipseRec {
+    RecHeader h;
+    int64_t key_min_x, key_max_x, key_min_y, key_max_y;
+    double a_squ, b_squ;
+    int64_t key_a_b_squ;
+    int64_t reserved;
+};
 
 // LimitPolygon (limitpolygon.h:13-90): x vertices then y vertices follow.
 struct alignas(16) LimitPolygonRec {

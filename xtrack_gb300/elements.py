@@ -494,6 +494,51 @@ class LimitEllipse(BeamElement):
         return [("a", self.a), ("b", self.b)]
 
 
+class LimitRectEllipse(BeamElement):
+    """Intersection of a symmetric rectangle and an ellipse
+    (limit_rect_ellipse.py; limitrectellipse.h:14-44): lost outside
+    |x| <= max_x, |y| <= max_y or x^2 b^2 + y^2 a^2 <= a^2 b^2."""
+    _cls = _abi.CLS_LIMIT_RECT_ELLIPSE
+
+    def __init__(self, max_x=UNLIMITED, max_y=UNLIMITED, a_squ=None, b_squ=None, a=None, b=None,
+                 a_b_squ=None, shift_x=0.0, shift_y=0.0):
+        self.shift_x = float(shift_x)
+        self.shift_y = float(shift_y)
+        if a is None and a_squ is None:
+            a = UNLIMITED
+        if b is None and b_squ is None:
+            b = UNLIMITED
+        if a is not None:
+            a_squ = a * a
+        if b is not None:
+            b_squ = b * b
+        if max_x < 0.0 or max_y < 0.0:
+            raise ValueError("max_x and max_y have to be positive definite")
+        if a_squ < 0.0 or b_squ < 0.0:
+            raise ValueError("a_squ and b_squ have to be positive definite")
+        self.max_x = float(max_x)
+        self.max_y = float(max_y)
+        self.a_squ = float(a_squ)
+        self.b_squ = float(b_squ)
+        self.a_b_squ = float(a_squ * b_squ if a_b_squ is None else a_b_squ)
+
+    @property
+    def a(self):
+        return math.sqrt(self.a_squ)
+
+    @property
+    def b(self):
+        return math.sqrt(self.b_squ)
+
+    def _fill(self, rec):
+        rec["cls"] = self._cls
+        for f in ("max_x", "max_y", "a_squ", "b_squ", "a_b_squ"):
+            rec[f] = getattr(self, f)
+
+    def _repr_items(self):
+        return [("max_x", self.max_x), ("max_y", self.max_y), ("a", self.a), ("b", self.b)]
+
+
 class LimitRect(BeamElement):
     """Rectangular aperture (limit_rect.py)."""
     _cls = _abi.CLS_LIMIT_RECT
@@ -761,5 +806,6 @@ def slice_class(parent, prefix, suffix=""):
 
 
 __all__ = ["Marker", "Drift", "Multipole", "Bend", "Quadrupole", "Sextupole", "Octupole",
-           "Cavity", "LimitEllipse", "LimitRect", "LimitPolygon", "DipoleEdge", "BeamElement",
+           "Cavity", "LimitEllipse", "LimitRect", "LimitRectEllipse", "LimitPolygon", "DipoleEdge",
+           "BeamElement",
            "slice_class"] + sorted(_SLICE_CLASSES)

@@ -51,6 +51,8 @@ _ACCEPT = {
                "num_kicks", "model", "integrator"),
     "LimitEllipse": ("a_squ", "b_squ", "a_b_squ", "a", "b", "shift_x", "shift_y"),
     "LimitRect": ("min_x", "max_x", "min_y", "max_y", "shift_x", "shift_y"),
+    "LimitRectEllipse": ("max_x", "max_y", "a_squ", "b_squ", "a_b_squ", "a", "b", "shift_x",
+                         "shift_y"),
     "LimitPolygon": ("x_vertices", "y_vertices", "shift_x", "shift_y"),
     "DipoleEdge": ("k", "e1", "e1_fd", "hgap", "fint", "model", "side"),
 }
@@ -93,7 +95,8 @@ def element_from_dict(dct, name="?"):
         kw["k"] = d["h"]
     if cname == "Multipole" and "isthick" in kw:
         kw["isthick"] = bool(kw["isthick"])
-    if cname == "LimitEllipse" and ("a" in kw or "b" in kw) and "a_squ" in kw:
+    if cname in ("LimitEllipse", "LimitRectEllipse") and ("a" in kw or "b" in kw) and \
+            "a_squ" in kw:
         kw.pop("a", None)
         kw.pop("b", None)
     klass = getattr(el, cname)
@@ -116,8 +119,11 @@ def element_to_dict(e):
                    harmonic=e.harmonic, length=e.length, absolute_time=e.absolute_time,
                    num_kicks=e.num_kicks, model=e._model, integrator=e._integrator)
         return out
-    if isinstance(e, (el.LimitEllipse, el.LimitRect, el.LimitPolygon)):
-        if isinstance(e, el.LimitEllipse):
+    if isinstance(e, (el.LimitEllipse, el.LimitRect, el.LimitPolygon, el.LimitRectEllipse)):
+        if isinstance(e, el.LimitRectEllipse):
+            out.update(max_x=e.max_x, max_y=e.max_y, a_squ=e.a_squ, b_squ=e.b_squ,
+                       a_b_squ=e.a_b_squ)
+        elif isinstance(e, el.LimitEllipse):
             out.update(a_squ=e.a_squ, b_squ=e.b_squ, a_b_squ=e.a_b_squ)
         elif isinstance(e, el.LimitRect):
             out.update(min_x=e.min_x, max_x=e.max_x, min_y=e.min_y, max_y=e.max_y)
