@@ -102,6 +102,39 @@ def test_misaligned_record_rejected():
     assert st == _abi.XTG_E_UNSUPPORTED and "misalignment" in _abi.last_error(lib)
 
 
+@pytest.mark.parametrize("field,value,msg", [("model", 5, "DipoleEdge model"),
+                                             ("side", 2, "DipoleEdge side")])
+def test_invalid_dipole_edge_rejected(field, value, msg):
+    recs = xt.Line(elements=[xt.DipoleEdge(k=1e-3, e1=0.01)])._element_records()
+    recs[0][field] = value
+    lib = _abi.load_library()
+    h = ctypes.c_void_p()
+    st = lib.xtg_lattice_create(recs.ctypes.data_as(ctypes.c_void_p), 1,
+                                ctypes.byref(_abi.XtgConfig()), ctypes.byref(h))
+    assert st == _abi.XTG_E_UNSUPPORTED and msg in _abi.last_error(lib)
+
+
+def test_aperture_shifts_validated():
+    """Transverse shifts pass for apertures; rotations and longitudinal
+    shifts do not, nor shifts of other classes."""
+    line = xt.Line(elements=[xt.LimitRect(min_x=-0.01, max_x=0.01, shift_x=1e-3),
+                             xt.LimitRectEllipse(max_x=0.01, max_y=0.01, a=0.02, b=0.02,
+                                                 shift_y=-1e-3)])
+    recs = line._element_records()
+    lib = _abi.load_library()
+    cfg = _abi.XtgConfig()
+    assert pyoracle.validate(recs)[0] == _abi.XTG_OK
+    for field in ("rot_s_rad", "shift_s"):
+        bad = recs.copy()
+        bad[0][field] = 1e-3
+        st, msg = pyoracle.validate(bad)
+        assert st == _abi.XTG_E_UNSUPPORTED and "misalignment" in msg
+        h = ctypes.c_void_p()
+        st = lib.xtg_lattice_create(bad.ctypes.data_as(ctypes.c_void_p), 2, ctypes.byref(cfg),
+                                    ctypes.byref(h))
+        assert st == _abi.XTG_E_UNSUPPORTED and "misalignment" in _abi.last_error(lib)
+
+
 def test_null_arguments_return_errors():
     lib = _abi.load_library()
     assert lib.xtg_lattice_create(None, 0, None, None) == _abi.XTG_E_NULL
