@@ -14,10 +14,14 @@
 //    takes item b first (blocks are dispatched breadth-first over the SMs,
 //    so a round with fewer items than resident blocks spreads evenly and no
 //    FP64 pipe carries two warps while another idles), later items come
-//    from an atomic counter. Each thread
-//    owns one particle, keeps its coordinates in registers for the whole
-//    round and walks the packed element table (xtg_table.h) with
-//    warp-uniform records and a warp-uniform switch on the element type;
+//    from an atomic counter. Each thread owns one particle, keeps its
+//    coordinates in registers for the whole round and walks the packed
+//    element table (xtg_table.h) with warp-uniform records and a
+//    warp-uniform switch on the element type;
+//  * FP64 is the narrow pipe of this part, so nothing that is not
+//    arithmetic goes there: aperture and global-aperture tests compare
+//    ordered integer keys of the IEEE bit patterns (ord_key), with the
+//    FP64 compare's outcome for signed zeros and NaN;
 //  * the element table is staged in shared memory: with one bulk copy per
 //    lattice when the tracked range fits, otherwise streamed in chunks
 //    through a double-buffered cp.async.bulk + mbarrier pipeline. Every wait
@@ -120,8 +124,8 @@ struct TrackArgs {
     int32_t backtrack;
     int32_t has_global;
     int32_t preserve_angle;
-    double global_lim;
-    int64_t global_key_lo, global_key_hi;   // lower_key(-global_lim), upper_key(global_lim)
+    // global aperture |x|, |y| <= limit as ordered keys: lower_key(-limit), upper_key(limit)
+    int64_t global_key_lo, global_key_hi;
     int64_t num_ele_line;
     double line_length;
     uint64_t track_flags;
@@ -1262,9 +1266,8 @@ static int32_t track_impl(ExecCtx* C, const xtg_particles* particles, const int3
     a.backtrack = backtrack ? 1 : 0;
     a.has_global = C->config.has_global_xy_limit;
     a.preserve_angle = C->config.cavity_preserve_angle;
-    a.global_lim = C->config.global_xy_limit;
-    a.global_key_lo = lower_key(-a.global_lim);
-    a.global_key_hi = upper_key(a.global_lim);
+    a.global_key_lo = lower_key(-C->config.global_xy_limit);
+    a.global_key_hi = upper_key(C->config.global_xy_limit);
     a.num_ele_line = num_ele_line;
     a.line_length = line_length;
     a.track_flags = track_flags;
@@ -1560,9 +1563,8 @@ int32_t xtg_track_noalloc(const xtg_lattice* lattice, const xtg_particles* parti
     a.backtrack = backtrack ? 1 : 0;
     a.has_global = C->config.has_global_xy_limit;
     a.preserve_angle = C->config.cavity_preserve_angle;
-    a.global_lim = C->config.global_xy_limit;
-    a.global_key_lo = lower_key(-a.global_lim);
-    a.global_key_hi = upper_key(a.global_lim);
+    a.global_key_lo = lower_key(-C->config.global_xy_limit);
+    a.global_key_hi = upper_key(C->config.global_xy_limit);
     a.num_ele_line = num_ele_line;
     a.line_length = line_length;
     a.track_flags = track_flags;
