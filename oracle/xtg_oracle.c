@@ -1360,6 +1360,15 @@ static void xto_profile(const xtg_element_monitor* m, const xto_part* p) {
     }
 }
 
+/* track_srotation.h:9-37 (no spin) */
+static void xto_srotation(xto_part* p, double sin_z, double cos_z) {
+    double const x = p->x, y = p->y, px = p->px, py = p->py;
+    p->x = cos_z * x + sin_z * y;
+    p->y = -sin_z * x + cos_z * y;
+    p->px = cos_z * px + sin_z * py;
+    p->py = -sin_z * px + cos_z * py;
+}
+
 /* The aperture check of one LimitEllipse / LimitPolygon / LimitRect on the
  * particle's current x, y (limitellipse.h, limitpolygon.h, limitrect.h). */
 static void xto_aperture(const xtg_element* e, xto_part* p) {
@@ -1484,17 +1493,22 @@ static int xto_apply(const xtg_element* e, const xtg_config* cfg, xto_part* p,
          * XYShift for the particle reaching the element, the exit XYShift
          * only if it survives (the CPU per-particle blocks skip lost
          * particles); both also when local apertures are ignored */
-        int const shifted = (e->shift_x != 0.0 || e->shift_y != 0.0);
+        double const psi_nf = e->rot_s_rad_no_frame, psi_wf = e->rot_s_rad;
+        int const shifted = (e->shift_x != 0.0 || e->shift_y != 0.0 || psi_nf != 0.0 || psi_wf != 0.0);
         if (shifted) {
             double mx, my;
             if (!backtrack) { mx = e->shift_x - 0.0; my = e->shift_y - 0.0; }
             else { mx = -(0.0 - e->shift_x); my = -(0.0 - e->shift_y); }
             p->x += -mx;
             p->y += -my;
+            if (psi_nf != 0.0) xto_srotation(p, sin(psi_nf), cos(psi_nf));
+            if (psi_wf != 0.0) xto_srotation(p, sin(psi_wf), cos(psi_wf));
         }
         xto_aperture(e, p);
         if (shifted && p->state > 0) {
             double mx, my;
+            if (psi_wf != 0.0) xto_srotation(p, sin(-psi_wf), cos(-psi_wf));
+            if (psi_nf != 0.0) xto_srotation(p, sin(-psi_nf), cos(-psi_nf));
             if (!backtrack) { mx = 0.0 - e->shift_x; my = 0.0 - e->shift_y; }
             else { mx = -(e->shift_x - 0.0); my = -(e->shift_y - 0.0); }
             p->x += -mx;
@@ -1672,12 +1686,11 @@ int32_t xto_validate(const xtg_element* els, int64_t n, char* msg, int64_t msg_l
         else if (e->slice < 0 || e->slice > XTG_SLICE_EXIT) why = "unknown slice kind";
         else if (e->order < 0 || e->order >= XTG_MAX_KNL) why = "multipole order out of range";
         else if (e->order_rel < -1 || e->order_rel >= 20) why = "relative multipole order out of range (0..19)";
-        else if (((e->shift_x != 0 || e->shift_y != 0) && e->cls != XTG_CLS_LIMIT_RECT &&
-                  e->cls != XTG_CLS_LIMIT_ELLIPSE && e->cls != XTG_CLS_LIMIT_POLYGON &&
-                  e->cls != XTG_CLS_LIMIT_RECT_ELLIPSE)
-                 || e->shift_s != 0 || e->rot_x_rad != 0 || e->rot_y_rad != 0 || e->rot_s_rad != 0
-                 || e->rot_s_rad_no_frame != 0)
-            why = "misalignments (shift/rotation) are not supported (transverse shifts: apertures only)";
+        else if (((e->shift_x != 0 || e->shift_y != 0 || e->rot_s_rad != 0 || e->rot_s_rad_no_frame != 0)
+                  && e->cls != XTG_CLS_LIMIT_RECT && e->cls != XTG_CLS_LIMIT_ELLIPSE
+                  && e->cls != XTG_CLS_LIMIT_POLYGON && e->cls != XTG_CLS_LIMIT_RECT_ELLIPSE)
+                 || e->shift_s != 0 || e->rot_x_rad != 0 || e->rot_y_rad != 0)
+            why = "misalignments (shift/rotation) are not supported (transverse shifts and tilts: apertures only)";
         else if (e->cls >= XTG_CLS_MULTIPOLE && e->cls <= XTG_CLS_OCTUPOLE) {
             int64_t model = e->model;
             if (e->cls == XTG_CLS_MULTIPOLE && e->isthick <= 0) model = -1;

@@ -174,5 +174,11 @@ def shifted_apertures():
            xt.Drift(length=0.3),
            xt.LimitRect(min_x=-0.02, max_x=0.02, min_y=-0.02, max_y=0.02, shift_y=5e-3),
            xt.Drift(length=0.2),
-           xt.LimitRectEllipse(max_x=0.016, max_y=0.013, a=0.019, b=0.016, shift_x=1e-3)]
+           xt.LimitRectEllipse(max_x=0.016, max_y=0.013, a=0.019, b=0.016, shift_x=1e-3),
+           xt.Drift(length=0.25),
+           # tilted apertures: rot_s_rad, rot_s_rad_no_frame, with and without shifts
+           xt.LimitRect(min_x=-0.012, max_x=0.012, min_y=-0.006, max_y=0.006, rot_s_rad=0.3),
+           xt.Drift(length=0.1),
+           xt.LimitEllipse(a=0.016, b=0.008, rot_s_rad_no_frame=-0.2, rot_s_rad=0.05,
+                           shift_x=5e-4)]
     return xt.Line(elements=els)

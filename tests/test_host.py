@@ -115,22 +115,23 @@ def test_invalid_dipole_edge_rejected(field, value, msg):
 
 
 def test_aperture_shifts_validated():
-    """Transverse shifts pass for apertures; rotations and longitudinal
-    shifts do not, nor shifts of other classes."""
-    line = xt.Line(elements=[xt.LimitRect(min_x=-0.01, max_x=0.01, shift_x=1e-3),
+    """Transverse shifts and tilts pass for apertures; other rotations and
+    longitudinal shifts do not, nor shifts or tilts of other classes."""
+    line = xt.Line(elements=[xt.LimitRect(min_x=-0.01, max_x=0.01, shift_x=1e-3, rot_s_rad=0.1),
                              xt.LimitRectEllipse(max_x=0.01, max_y=0.01, a=0.02, b=0.02,
-                                                 shift_y=-1e-3)])
+                                                 shift_y=-1e-3),
+                             xt.Drift(length=1.0)])
     recs = line._element_records()
     lib = _abi.load_library()
     cfg = _abi.XtgConfig()
     assert pyoracle.validate(recs)[0] == _abi.XTG_OK
-    for field in ("rot_s_rad", "shift_s"):
+    for i, field in ((0, "rot_x_rad"), (0, "shift_s"), (2, "rot_s_rad"), (2, "shift_x")):
         bad = recs.copy()
-        bad[0][field] = 1e-3
+        bad[i][field] = 1e-3
         st, msg = pyoracle.validate(bad)
         assert st == _abi.XTG_E_UNSUPPORTED and "misalignment" in msg
         h = ctypes.c_void_p()
-        st = lib.xtg_lattice_create(bad.ctypes.data_as(ctypes.c_void_p), 2, ctypes.byref(cfg),
+        st = lib.xtg_lattice_create(bad.ctypes.data_as(ctypes.c_void_p), 3, ctypes.byref(cfg),
                                     ctypes.byref(h))
         assert st == _abi.XTG_E_UNSUPPORTED and "misalignment" in _abi.last_error(lib)
 

@@ -421,9 +421,10 @@ int32_t validate_element(const xtg_element& e, int64_t idx, std::string* why) {
                           e.cls == XTG_CLS_LIMIT_POLYGON || e.cls == XTG_CLS_LIMIT_RECT_ELLIPSE;
     if (!aperture && (e.shift_x != 0 || e.shift_y != 0))
         return fail("misalignments (shift/rotation) are not supported (transverse shifts: apertures only)");
-    if (e.shift_s != 0 || e.rot_x_rad != 0 || e.rot_y_rad != 0 || e.rot_s_rad != 0 ||
-        e.rot_s_rad_no_frame != 0)
-        return fail("misalignments (shift/rotation) are not supported (transverse shifts: apertures only)");
+    if (!aperture && (e.rot_s_rad != 0 || e.rot_s_rad_no_frame != 0))
+        return fail("misalignments (shift/rotation) are not supported (transverse shifts and tilts: apertures only)");
+    if (e.shift_s != 0 || e.rot_x_rad != 0 || e.rot_y_rad != 0)
+        return fail("misalignments (shift/rotation) are not supported (transverse shifts and tilts: apertures only)");
     if (e.cls >= XTG_CLS_MULTIPOLE && e.cls <= XTG_CLS_OCTUPOLE) {
         int64_t model = e.model;
         if (e.cls == XTG_CLS_MULTIPOLE && e.isthick <= 0) model = -1;
@@ -1076,12 +1077,37 @@ int32_t pack_lattice(const xtg_element* els, int64_t n, const xtg_config& cfg,
         }
         if ((e.cls == XTG_CLS_LIMIT_RECT || e.cls == XTG_CLS_LIMIT_ELLIPSE ||
              e.cls == XTG_CLS_LIMIT_POLYGON || e.cls == XTG_CLS_LIMIT_RECT_ELLIPSE) &&
-            (e.shift_x != 0.0 || e.shift_y != 0.0)) {
-            // entry and exit XYShift of track_misalignment_entry/exit_straight
-            // with zero anchor, rotations and shift_s
+            (e.shift_x != 0.0 || e.shift_y != 0.0 || e.rot_s_rad != 0.0 || e.rot_s_rad_no_frame != 0.0)) {
+            // entry and exit of track_misalignment_entry/exit_straight with
+            // zero anchor, shift_s, rot_x_rad and rot_y_rad
             double const mis_in_x = e.shift_x - 0.0, mis_in_y = e.shift_y - 0.0;
             double const mis_out_x = 0.0 - e.shift_x, mis_out_y = 0.0 - e.shift_y;
             ApertureShift sh;
+            std::memset(&sh, 0, sizeof(sh));
+            // S_ROTATE(psi_no_frame), S_ROTATE(psi_with_frame) at the entry;
+            // S_ROTATE(-psi_with_frame), S_ROTATE(-psi_no_frame) at the exit
+            // (the same order in backtracking tables)
+            double const psi_nf = e.rot_s_rad_no_frame, psi_wf = e.rot_s_rad;
+            if (psi_nf != 0.0) {
+                sh.rot_in[sh.n_rot_in][0] = std::sin(psi_nf);
+                sh.rot_in[sh.n_rot_in][1] = std::cos(psi_nf);
+                sh.n_rot_in++;
+            }
+            if (psi_wf != 0.0) {
+                sh.rot_in[sh.n_rot_in][0] = std::sin(psi_wf);
+                sh.rot_in[sh.n_rot_in][1] = std::cos(psi_wf);
+                sh.n_rot_in++;
+            }
+            if (psi_wf != 0.0) {
+                sh.rot_out[sh.n_rot_out][0] = std::sin(-psi_wf);
+                sh.rot_out[sh.n_rot_out][1] = std::cos(-psi_wf);
+                sh.n_rot_out++;
+            }
+            if (psi_nf != 0.0) {
+                sh.rot_out[sh.n_rot_out][0] = std::sin(-psi_nf);
+                sh.rot_out[sh.n_rot_out][1] = std::cos(-psi_nf);
+                sh.n_rot_out++;
+            }
             if (!backtrack) {
                 sh.in_x = -mis_in_x;
                 sh.in_y = -mis_in_y;

@@ -366,19 +366,54 @@ __device__ __noinline__ void multi_element_monitor(const xtg_multi_element_monit
 // the exit XYShift only if it survives; both also when local apertures are
 // ignored. The block is found again from the header at the exit, so that
 // nothing stays live across the check.
-__device__ __forceinline__ void aperture_shift_in(PState& p, const unsigned char* rec, const RecHeader& h) {
-    if (h.flags & F_SHIFTED) {
-        const ApertureShift& sh = *reinterpret_cast<const ApertureShift*>(rec + h.nbytes - sizeof(ApertureShift));
-        p.x = p.x + sh.in_x;
-        p.y = p.y + sh.in_y;
+// limitpolygon.h:64-90: the crossing-number test with the inscribed-circle
+// shortcut of the CPU build; out of line (polygons are rare in a turn)
+__device__ __noinline__ bool polygon_alive(double x, double y, const unsigned char* __restrict__ rec) {
+    const LimitPolygonRec& r = *reinterpret_cast<const LimitPolygonRec*>(rec);
+    const double* vx = reinterpret_cast<const double*>(rec + sizeof(LimitPolygonRec));
+    const double* vy = vx + r.n;
+    if (!(x * x + y * y > r.inner_radius_sq)) return true;
+    int64_t ii = 0, jj = r.n - 1;
+    bool alive = false;
+    while (ii < r.n) {
+        double const vx_ii = vx[ii], vx_jj = vx[jj], vy_ii = vy[ii], vy_jj = vy[jj];
+        if (((vy_ii > y) != (vy_jj > y)) && (x < (vx_jj - vx_ii) * (y - vy_ii) / (vy_jj - vy_ii) + vx_ii))
+            alive = !alive;
+        jj = ii;
+        ii++;
     }
+    return alive;
+}
+
+// track_srotation.h:9-37 (no spin)
+__device__ __forceinline__ void s_rotation(PState& p, double sin_z, double cos_z) {
+    double const x = p.x, y = p.y, px = p.px, py = p.py;
+    p.x = cos_z * x + sin_z * y;
+    p.y = -sin_z * x + cos_z * y;
+    p.px = cos_z * px + sin_z * py;
+    p.py = -sin_z * px + cos_z * py;
+}
+// Entry and exit of a transformed aperture; out of line, so that the
+// common untransformed aperture keeps a flag test only.
+XTG_COLD PState aperture_transform_in(PState p, const ApertureShift* __restrict__ sh) {
+    p.x = p.x + sh->in_x;
+    p.y = p.y + sh->in_y;
+    for (int k = 0; k < sh->n_rot_in; k++) s_rotation(p, sh->rot_in[k][0], sh->rot_in[k][1]);
+    return p;
+}
+XTG_COLD PState aperture_transform_out(PState p, const ApertureShift* __restrict__ sh) {
+    for (int k = 0; k < sh->n_rot_out; k++) s_rotation(p, sh->rot_out[k][0], sh->rot_out[k][1]);
+    p.x = p.x + sh->out_x;
+    p.y = p.y + sh->out_y;
+    return p;
+}
+__device__ __forceinline__ void aperture_shift_in(PState& p, const unsigned char* rec, const RecHeader& h) {
+    if (h.flags & F_SHIFTED)
+        p = aperture_transform_in(p, reinterpret_cast<const ApertureShift*>(rec + h.nbytes - sizeof(ApertureShift)));
 }
 __device__ __forceinline__ void aperture_shift_out(PState& p, const unsigned char* rec, const RecHeader& h) {
-    if ((h.flags & F_SHIFTED) && p.state > 0) {
-        const ApertureShift& sh = *reinterpret_cast<const ApertureShift*>(rec + h.nbytes - sizeof(ApertureShift));
-        p.x = p.x + sh.out_x;
-        p.y = p.y + sh.out_y;
-    }
+    if ((h.flags & F_SHIFTED) && p.state > 0)
+        p = aperture_transform_out(p, reinterpret_cast<const ApertureShift*>(rec + h.nbytes - sizeof(ApertureShift)));
 }
 
 template <bool kExact>
@@ -471,25 +506,8 @@ __device__ __forceinline__ bool apply_record(PState& p, const unsigned char* __r
     case OP_LIMIT_POLYGON: {
         // limitpolygon.h:64-90 (crossing-number test)
         aperture_shift_in(p, rec, h);
-        if (!flag_on(a.track_flags, XTG_FLAG_IGNORE_LOCAL_APERTURE)) {
-            const LimitPolygonRec& r = *reinterpret_cast<const LimitPolygonRec*>(rec);
-            const double* vx = reinterpret_cast<const double*>(rec + sizeof(LimitPolygonRec));
-            const double* vy = vx + r.n;
-            double const x = p.x, y = p.y;
-            if (x * x + y * y > r.inner_radius_sq) {
-                int64_t ii = 0, jj = r.n - 1;
-                bool alive = false;
-                while (ii < r.n) {
-                    double const vx_ii = vx[ii], vx_jj = vx[jj], vy_ii = vy[ii], vy_jj = vy[jj];
-                    if (((vy_ii > y) != (vy_jj > y)) &&
-                        (x < (vx_jj - vx_ii) * (y - vy_ii) / (vy_jj - vy_ii) + vx_ii))
-                        alive = !alive;
-                    jj = ii;
-                    ii++;
-                }
-                if (!alive) p.state = 0;
-            }
-        }
+        if (!flag_on(a.track_flags, XTG_FLAG_IGNORE_LOCAL_APERTURE) && !polygon_alive(p.x, p.y, rec))
+            p.state = 0;
         aperture_shift_out(p, rec, h);
         break;
     }

@@ -63,9 +63,10 @@ class BeamElement:
         rec["weight"] = 1.0
         rec["order_rel"] = -1
         self._fill(rec)
-        # transverse shift (apertures: track_local_particle_with_transformations.h)
-        rec["shift_x"] = getattr(self, "shift_x", 0.0)
-        rec["shift_y"] = getattr(self, "shift_y", 0.0)
+        # transverse shift and tilt (apertures:
+        # track_local_particle_with_transformations.h)
+        for f in ("shift_x", "shift_y", "rot_s_rad", "rot_s_rad_no_frame"):
+            rec[f] = getattr(self, f, 0.0)
         return rec
 
     def copy(self):
@@ -457,9 +458,12 @@ class LimitEllipse(BeamElement):
     _cls = _abi.CLS_LIMIT_ELLIPSE
 
     def __init__(self, a=None, b=None, a_squ=None, b_squ=None, a_b_squ=None, shift_x=0.0,
-                 shift_y=0.0):
+                 shift_y=0.0, rot_s_rad=0.0,
+                 rot_s_rad_no_frame=0.0):
         self.shift_x = float(shift_x)
         self.shift_y = float(shift_y)
+        self.rot_s_rad = float(rot_s_rad)
+        self.rot_s_rad_no_frame = float(rot_s_rad_no_frame)
         if a is None and a_squ is None:
             a = UNLIMITED
         if b is None and b_squ is None:
@@ -501,9 +505,12 @@ class LimitRectEllipse(BeamElement):
     _cls = _abi.CLS_LIMIT_RECT_ELLIPSE
 
     def __init__(self, max_x=UNLIMITED, max_y=UNLIMITED, a_squ=None, b_squ=None, a=None, b=None,
-                 a_b_squ=None, shift_x=0.0, shift_y=0.0):
+                 a_b_squ=None, shift_x=0.0, shift_y=0.0, rot_s_rad=0.0,
+                 rot_s_rad_no_frame=0.0):
         self.shift_x = float(shift_x)
         self.shift_y = float(shift_y)
+        self.rot_s_rad = float(rot_s_rad)
+        self.rot_s_rad_no_frame = float(rot_s_rad_no_frame)
         if a is None and a_squ is None:
             a = UNLIMITED
         if b is None and b_squ is None:
@@ -544,9 +551,12 @@ class LimitRect(BeamElement):
     _cls = _abi.CLS_LIMIT_RECT
 
     def __init__(self, min_x=-UNLIMITED, max_x=UNLIMITED, min_y=-UNLIMITED, max_y=UNLIMITED,
-                 shift_x=0.0, shift_y=0.0):
+                 shift_x=0.0, shift_y=0.0, rot_s_rad=0.0,
+                 rot_s_rad_no_frame=0.0):
         self.shift_x = float(shift_x)
         self.shift_y = float(shift_y)
+        self.rot_s_rad = float(rot_s_rad)
+        self.rot_s_rad_no_frame = float(rot_s_rad_no_frame)
         self.min_x = float(min_x)
         self.max_x = float(max_x)
         self.min_y = float(min_y)
@@ -664,9 +674,12 @@ class LimitPolygon(BeamElement):
     vertices (limitpolygon.h:13-90)."""
     _cls = _abi.CLS_LIMIT_POLYGON
 
-    def __init__(self, x_vertices=None, y_vertices=None, shift_x=0.0, shift_y=0.0):
+    def __init__(self, x_vertices=None, y_vertices=None, shift_x=0.0, shift_y=0.0, rot_s_rad=0.0,
+                 rot_s_rad_no_frame=0.0):
         self.shift_x = float(shift_x)
         self.shift_y = float(shift_y)
+        self.rot_s_rad = float(rot_s_rad)
+        self.rot_s_rad_no_frame = float(rot_s_rad_no_frame)
         x = np.ascontiguousarray(x_vertices, dtype=np.float64)
         y = np.ascontiguousarray(y_vertices, dtype=np.float64)
         if x.shape != y.shape or x.ndim != 1 or len(x) < 3:

@@ -49,11 +49,14 @@ _ACCEPT = {
                  "edge_exit_active") + _MAGNET_KEYS,
     "Cavity": ("voltage", "frequency", "lag", "phase", "harmonic", "length", "absolute_time",
                "num_kicks", "model", "integrator"),
-    "LimitEllipse": ("a_squ", "b_squ", "a_b_squ", "a", "b", "shift_x", "shift_y"),
-    "LimitRect": ("min_x", "max_x", "min_y", "max_y", "shift_x", "shift_y"),
+    "LimitEllipse": ("a_squ", "b_squ", "a_b_squ", "a", "b", "shift_x", "shift_y", "rot_s_rad",
+                     "rot_s_rad_no_frame"),
+    "LimitRect": ("min_x", "max_x", "min_y", "max_y", "shift_x", "shift_y", "rot_s_rad",
+                     "rot_s_rad_no_frame"),
     "LimitRectEllipse": ("max_x", "max_y", "a_squ", "b_squ", "a_b_squ", "a", "b", "shift_x",
-                         "shift_y"),
-    "LimitPolygon": ("x_vertices", "y_vertices", "shift_x", "shift_y"),
+                         "shift_y", "rot_s_rad", "rot_s_rad_no_frame"),
+    "LimitPolygon": ("x_vertices", "y_vertices", "shift_x", "shift_y", "rot_s_rad",
+                     "rot_s_rad_no_frame"),
     "DipoleEdge": ("k", "e1", "e1_fd", "hgap", "fint", "model", "side"),
 }
 
@@ -129,7 +132,7 @@ def element_to_dict(e):
             out.update(min_x=e.min_x, max_x=e.max_x, min_y=e.min_y, max_y=e.max_y)
         else:
             out.update(x_vertices=e.x_vertices.tolist(), y_vertices=e.y_vertices.tolist())
-        for f in ("shift_x", "shift_y"):
+        for f in ("shift_x", "shift_y", "rot_s_rad", "rot_s_rad_no_frame"):
             if getattr(e, f) != 0.0:
                 out[f] = getattr(e, f)
         return out
