@@ -18,6 +18,8 @@ from lattice_cases import element_zoo, fringe_zoo, shifted_apertures, sliced_lin
 HERE = os.path.dirname(os.path.abspath(__file__))
 LHC = os.path.join(HERE, "golden", "lhc", "hllhc14_thin_64p_10t.npz")
 SPS = os.path.join(HERE, "golden", "sps", "sps_thin_128p_20t.npz")
+PSB = os.path.join(HERE, "golden", "psb", "psb_injection_128p_20t.npz")
+CLIC_DR = os.path.join(HERE, "golden", "clic_dr", "clic_dr_64p_5t.npz")
 
 
 def _same_records(a, b):
@@ -153,13 +155,20 @@ def test_lhc_fixture_gpu(arith):
         compare_within_spread(got, out, spread, ok)
 
 
-def test_sps_fixture_oracle_reproduces_reference():
-    """The thin SPS line (8200 elements: drifts, thin multipoles, 1488
-    DipoleEdges, 1698 LimitRect/LimitEllipse apertures, cavities) after 20
-    turns of the reference-compiled code, with real aperture losses."""
-    recs, arrs, out, meta = _fixture(SPS)
-    assert meta["n_elements"] == len(recs) == 8200
-    assert np.sum(out["state"] <= 0) > 5
+REAL = {"sps": (SPS, 8200), "psb": (PSB, 604), "clic_dr": (CLIC_DR, 36954)}
+
+
+@pytest.mark.parametrize("name", list(REAL))
+def test_real_lattice_fixture_oracle_reproduces_reference(name):
+    """Real lattices of the reference's test data after their turns of the
+    reference-compiled code: the thin SPS line (8200 elements, 1698
+    apertures, real losses), the PS Booster injection line (604 elements)
+    and the CLIC damping ring (36954 elements, electrons)."""
+    path, n_el = REAL[name]
+    recs, arrs, out, meta = _fixture(path)
+    assert meta["n_elements"] == len(recs) == n_el and not meta["dropped"]
+    if name == "sps":
+        assert np.sum(out["state"] <= 0) > 5
     pyoracle.track(recs, arrs, line_length=meta["line_length"], num_turns=meta["num_turns"],
                    q0=meta["q0"], mass0=meta["mass0"])
     for k, v in out.items():
@@ -168,17 +177,18 @@ def test_sps_fixture_oracle_reproduces_reference():
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("arith", ["exact", "fast"])
-def test_sps_fixture_gpu(arith):
-    """The real SPS line on the GPU against the reference-compiled result:
-    state, at_turn and at_element of every aperture loss bit-exact. Exact
-    mode: one turn within 1e-14; after 20 turns within 1e-10. The
-    cavities' sin comes from CUDA's libm: on this beam all 128 particles
-    stay bit-identical for 16 turns, then one cavity pass of one particle
-    gets a sin one ulp away from glibc's, rvv moves by an ulp, and the
-    drifts of the following turns carry that to ~8e-12 relative in zeta.
-    Fast mode: within 3x the reference's FMA spread."""
+@pytest.mark.parametrize("name", list(REAL))
+def test_real_lattice_fixture_gpu(name, arith):
+    """The real lattices on the GPU against the reference-compiled result:
+    state, at_turn and at_element bit-exact. Exact mode: one turn within
+    1e-14; all turns within 1e-10. The cavities' sin comes from CUDA's libm:
+    on the SPS beam all 128 particles stay bit-identical for 16 turns, then
+    one cavity pass of one particle gets a sin one ulp away from glibc's,
+    rvv moves by an ulp, and the drifts of the following turns carry that
+    to ~8e-12 relative in zeta. Fast mode: within 3x the reference's FMA
+    spread."""
     from xtg_testutil import compare, compare_within_spread, fma_spread, gpu_track
-    recs, arrs, out, meta = _fixture(SPS)
+    recs, arrs, out, meta = _fixture(REAL[name][0])
     kw = dict(line_length=meta["line_length"], num_turns=meta["num_turns"], q0=meta["q0"],
               mass0=meta["mass0"])
     got, _ = gpu_track(recs, {k: v.copy() for k, v in arrs.items()}, arith=arith, **kw)
@@ -186,7 +196,6 @@ def test_sps_fixture_gpu(arith):
         assert np.array_equal(got[f], out[f]), f
     if arith == "exact":
         compare(got, out, 1e-10)
-        # one turn: the 1e-14 bound
         kw1 = dict(kw, num_turns=1)
         one = {k: v.copy() for k, v in arrs.items()}
         pyoracle.track(recs, one, **kw1)
