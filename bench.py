@@ -589,15 +589,27 @@ def run_toy_ring(args):
     print(json.dumps(out))
 
 
+# name: (fixture under tests/golden, description, beam sigmas of the bench's synthetic beam)
+REAL_LATTICES = {
+    "sps": (os.path.join("sps", "sps_thin_128p_20t.npz"), "thin SPS line",
+            {"x": 6e-3, "px": 1.5e-4, "y": 5e-3, "py": 1.5e-4, "zeta": 0.05, "delta": 5e-4}),
+    "psb": (os.path.join("psb", "psb_injection_128p_20t.npz"), "PS Booster injection line",
+            {"x": 2e-3, "px": 2e-4, "y": 2e-3, "py": 2e-4, "zeta": 1.0, "delta": 1e-3}),
+    "clic_dr": (os.path.join("clic_dr", "clic_dr_64p_5t.npz"), "CLIC damping ring",
+                {"x": 5e-5, "px": 5e-6, "y": 1e-5, "py": 1e-6, "zeta": 1e-3, "delta": 1e-3}),
+}
+
+
 def run_real_lattice(args):
-    """A real machine: the thin SPS line of the reference's test data
-    (8200 elements: drifts, thin multipoles, 1488 DipoleEdges, 1698
-    apertures, cavities; packed records of the committed parity fixture
-    tests/golden/sps), --particles protons around the fixture's particle
-    with its spread (some are lost on the apertures), one turn per step,
-    through the C-ABI (xtg_lattice_create / xtg_track) with CUDA events;
-    the oracle's port of the reference OpenMP path on the host cores as
-    the CPU baseline."""
+    """A real machine from the reference's test data, as packed records of
+    a committed parity fixture (tests/golden): the thin SPS line (8200
+    elements: drifts, thin multipoles, 1488 DipoleEdges, 1698 apertures,
+    cavities), the PS Booster injection line (604 elements) or the CLIC
+    damping ring (36954 elements, electrons). --particles particles around
+    the fixture's particle with a Gaussian spread (on the SPS some are lost
+    on the apertures), one turn per step, through the C-ABI
+    (xtg_lattice_create / xtg_track) with CUDA events; the oracle's port of
+    the reference OpenMP path on the host cores as the CPU baseline."""
     import ctypes
 
     import torch
@@ -610,13 +622,13 @@ def run_real_lattice(args):
         return
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    d = np.load(os.path.join(ROOT, "tests", "golden", "sps", "sps_thin_128p_20t.npz"))
+    fixture, what, sig = REAL_LATTICES[args.lattice]
+    d = np.load(os.path.join(ROOT, "tests", "golden", fixture))
     meta = json.loads(str(d["meta"]))
     recs = np.ascontiguousarray(d["records"])
     n_el, L = len(recs), float(meta["line_length"])
     p0 = {k[3:]: d[k] for k in d.files if k.startswith("in_")}
     rng = np.random.default_rng(16)
-    sig = {"x": 6e-3, "px": 1.5e-4, "y": 5e-3, "py": 1.5e-4, "zeta": 0.05, "delta": 5e-4}
     base = {k: float(np.mean(p0[k])) for k in sig}
 
     def beam(n, device):
@@ -648,11 +660,12 @@ def run_real_lattice(args):
     torch.cuda.synchronize(dev)
     alive0 = int((p.state > 0).sum())
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        step()
-    e1.record(stream)
-    e1.synchronize()
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        e1.synchronize()
     _abi.check(lib.xtg_device_status(h), lib)
     ms = e0.elapsed_time(e1)
     alive1 = int((p.state > 0).sum())
@@ -662,7 +675,7 @@ def run_real_lattice(args):
     lib.xtg_lattice_destroy(h)
     # CPU: the oracle port on all host cores, one turn of a sample
     pyoracle.ensure_built(with_ref=False)
-    n_cpu = 20000
+    n_cpu = max(1000, int(20000 * 8200 / n_el) // 1000 * 1000)
     arrs = pyoracle.host_arrays(beam(n_cpu, "cpu").to_numpy())
     t0 = time.perf_counter()
     pyoracle.track(recs, arrs, line_length=L, num_turns=1, q0=meta["q0"], mass0=meta["mass0"],
@@ -670,10 +683,10 @@ def run_real_lattice(args):
     dt = time.perf_counter() - t0
     cpu = float(np.sum(arrs["state"] > 0)) / dt
     achieved = value * flops_pt / 1e12
-    out = {"metric": "real-lattice particle-turns/s (thin SPS line)", "value": value,
+    out = {"metric": f"real-lattice particle-turns/s ({what})", "value": value,
            "unit": "particle-turns/s", "higher_is_better": True, "n_gpus": 1, "dtype": "f64",
            "data": "synthetic beam on a real lattice", "arith": args.arith,
-           "config": {"workload": f"thin SPS line of the reference's test data ({n_el} elements)",
+           "config": {"workload": f"{what} of the reference's test data ({n_el} elements)",
                       "particles": args.particles, "turns_per_step": 1},
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
            "alive_before": alive0, "alive_after": alive1,
@@ -682,7 +695,8 @@ def run_real_lattice(args):
                         "flops_per_particle_turn": flops_pt},
            "cpu_baseline": {"value": cpu, "unit": "particle-turns/s",
                             "cores": pyoracle.max_threads(), "kind": "port",
-                            "sample": f"{n_cpu} particles x 1 turn ({dt:.2f} s, OpenMP)"}}
+                            "sample": f"{n_cpu} particles x 1 turn ({dt:.2f} s, OpenMP)"},
+           "clocks": clk.summary()}
     print(json.dumps(out))
 
 
@@ -756,6 +770,8 @@ def main():
     ap.add_argument("--workload", default="thick_ring",
                     choices=["thick_ring", "da_screen", "turn_latency", "batch_scan", "toy_ring",
                              "real_lattice"])
+    ap.add_argument("--lattice", default="sps", choices=sorted(REAL_LATTICES),
+                    help="real_lattice workload: which fixture's line")
     ap.add_argument("--toy-particles", dest="toy_particles", type=int, default=10000)
     ap.add_argument("--toy-turns", dest="toy_turns", type=int, default=1000)
     ap.add_argument("--toy-cpu-turns", dest="toy_cpu_turns", type=int, default=1000)
