@@ -220,6 +220,11 @@ XTR_GET_D(DipoleEdge, k, el->k) XTR_GET_D(DipoleEdge, e1, el->e1)
 XTR_GET_D(DipoleEdge, fint, el->fint) XTR_GET_D(DipoleEdge, hgap, el->hgap)
 XTR_GET_D(DipoleEdge, delta_taper, 0.)
 XTR_GET_I(DipoleEdge, model, el->model) XTR_GET_I(DipoleEdge, side, el->side)
+XTR_GET_D(DipoleEdge, shift_x, el->shift_x) XTR_GET_D(DipoleEdge, shift_y, el->shift_y)
+XTR_GET_D(DipoleEdge, shift_s, el->shift_s) XTR_GET_D(DipoleEdge, rot_x_rad, el->rot_x_rad)
+XTR_GET_D(DipoleEdge, rot_y_rad, el->rot_y_rad) XTR_GET_D(DipoleEdge, rot_s_rad, el->rot_s_rad)
+XTR_GET_D(DipoleEdge, rot_s_rad_no_frame, el->rot_s_rad_no_frame)
+XTR_GET_D(DipoleEdge, rot_shift_anchor, 0.)
 
 /* ---- the reference's element code, compiled as-is --------------------- */
 #include "xtrack/headers/constants.h"
@@ -251,6 +256,20 @@ XTR_GET_I(DipoleEdge, model, el->model) XTR_GET_I(DipoleEdge, side, el->side)
 #undef ALLOW_ROT_AND_SHIFT
 #undef ELEMENT_NAME
 #define ELEMENT_NAME LimitRectEllipse
+#define ALLOW_ROT_AND_SHIFT 1
+#include "xtrack/headers/track_local_particle_with_transformations.h"
+#undef ALLOW_ROT_AND_SHIFT
+#undef ELEMENT_NAME
+/* Multipole: `isthick` in its fields (IS_THICK_DYNAMIC), no `h` (straight);
+ * DipoleEdge: no length, no `h` (base_element.py:83-126) */
+#define ELEMENT_NAME Multipole
+#define ALLOW_ROT_AND_SHIFT 1
+#define IS_THICK_DYNAMIC 1
+#include "xtrack/headers/track_local_particle_with_transformations.h"
+#undef IS_THICK_DYNAMIC
+#undef ALLOW_ROT_AND_SHIFT
+#undef ELEMENT_NAME
+#define ELEMENT_NAME DipoleEdge
 #define ALLOW_ROT_AND_SHIFT 1
 #include "xtrack/headers/track_local_particle_with_transformations.h"
 #undef ALLOW_ROT_AND_SHIFT
@@ -300,9 +319,11 @@ static int xtr_apply(const xtg_element* e, LocalParticle* lp) {
     case XTG_CLS_DRIFT: Drift_track_local_particle(e, lp); return 1;
     case XTG_CLS_LIMIT_ELLIPSE: LimitEllipse_track_local_particle_with_transformations(e, lp); return 0;
     case XTG_CLS_LIMIT_RECT: LimitRect_track_local_particle_with_transformations(e, lp); return 0;
-    case XTG_CLS_DIPOLE_EDGE: DipoleEdge_track_local_particle(e, lp); return 0;
+    case XTG_CLS_DIPOLE_EDGE: DipoleEdge_track_local_particle_with_transformations(e, lp); return 0;
     case XTG_CLS_LIMIT_RECT_ELLIPSE: LimitRectEllipse_track_local_particle_with_transformations(e, lp); return 0;
-    case XTG_CLS_MULTIPOLE: XTR_SLICES(Multipole, 0) return 0;
+    case XTG_CLS_MULTIPOLE:
+        if (e->slice == XTG_SLICE_NONE) { Multipole_track_local_particle_with_transformations(e, lp); return 0; }
+        XTR_SLICES(Multipole, 0) return 0;
     case XTG_CLS_BEND: XTR_EDGES(Bend) XTR_SLICES(Bend, 1) return 0;
     case XTG_CLS_QUADRUPOLE: XTR_EDGES(Quadrupole) XTR_SLICES(Quadrupole, 1) return 0;
     case XTG_CLS_SEXTUPOLE: XTR_EDGES(Sextupole) XTR_SLICES(Sextupole, 1) return 0;

@@ -1450,12 +1450,62 @@ static void xto_aperture(const xtg_element* e, xto_part* p) {
     }
 }
 
+/* Transverse shift and s-tilt of an element of zero length and straight
+ * frame: track_misalignment_entry/exit_straight (track_misalignments.h:
+ * 38-130) with zero length, anchor, shift_s, rot_x_rad and rot_y_rad. The
+ * entry XYShift, then S_ROTATE by rot_s_rad_no_frame and by rot_s_rad;
+ * the exit S_ROTATE by -rot_s_rad and -rot_s_rad_no_frame, then the XYShift
+ * (the roles swap in backtracking). */
+static int xto_shifted(const xtg_element* e) {
+    return e->shift_x != 0.0 || e->shift_y != 0.0 || e->rot_s_rad_no_frame != 0.0 || e->rot_s_rad != 0.0;
+}
+static void xto_shift_in(const xtg_element* e, xto_part* p, int backtrack) {
+    double const psi_nf = e->rot_s_rad_no_frame, psi_wf = e->rot_s_rad;
+    double mx, my;
+    if (!backtrack) { mx = e->shift_x - 0.0; my = e->shift_y - 0.0; }
+    else { mx = -(0.0 - e->shift_x); my = -(0.0 - e->shift_y); }
+    p->x += -mx;
+    p->y += -my;
+    if (psi_nf != 0.0) xto_srotation(p, sin(psi_nf), cos(psi_nf));
+    if (psi_wf != 0.0) xto_srotation(p, sin(psi_wf), cos(psi_wf));
+}
+static void xto_shift_out(const xtg_element* e, xto_part* p, int backtrack) {
+    double const psi_nf = e->rot_s_rad_no_frame, psi_wf = e->rot_s_rad;
+    double mx, my;
+    if (psi_wf != 0.0) xto_srotation(p, sin(-psi_wf), cos(-psi_wf));
+    if (psi_nf != 0.0) xto_srotation(p, sin(-psi_nf), cos(-psi_nf));
+    if (!backtrack) { mx = 0.0 - e->shift_x; my = 0.0 - e->shift_y; }
+    else { mx = -(e->shift_x - 0.0); my = -(e->shift_y - 0.0); }
+    p->x += -mx;
+    p->y += -my;
+}
+
+static int xto_apply_local(const xtg_element* e, const xtg_config* cfg, xto_part* p,
+                           const xtg_particles* src, int64_t isrc);
+
 /* Applies one element to one particle. Returns whether the class is
  * statically thick (global aperture check follows, tracker.py:681-689).
  * `src`/`isrc` locate the particle in its arrays (monitors copy the fields
- * the push does not carry). */
+ * the push does not carry). A thin Multipole (no `h` field: straight;
+ * `isthick` 0: zero length) or a DipoleEdge with a transverse shift or tilt
+ * runs inside the transforms of track_local_particle_with_transformations.h:
+ * 146-165; the exit only for a particle that survives. Apertures apply
+ * theirs around the test itself. */
 static int xto_apply(const xtg_element* e, const xtg_config* cfg, xto_part* p,
                      const xtg_particles* src, int64_t isrc) {
+    if (((e->cls == XTG_CLS_MULTIPOLE && e->isthick <= 0 && e->slice == XTG_SLICE_NONE) ||
+         e->cls == XTG_CLS_DIPOLE_EDGE) && xto_shifted(e)) {
+        int const backtrack = flag_set(p, XTG_FLAG_BACKTRACK);
+        xto_shift_in(e, p, backtrack);
+        int const thick = xto_apply_local(e, cfg, p, src, isrc);
+        if (p->state > 0) xto_shift_out(e, p, backtrack);
+        return thick;
+    }
+    return xto_apply_local(e, cfg, p, src, isrc);
+}
+
+static int xto_apply_local(const xtg_element* e, const xtg_config* cfg, xto_part* p,
+                           const xtg_particles* src, int64_t isrc) {
     int const backtrack = flag_set(p, XTG_FLAG_BACKTRACK);
     switch (e->cls) {
     case XTG_CLS_MARKER:
@@ -1493,27 +1543,10 @@ static int xto_apply(const xtg_element* e, const xtg_config* cfg, xto_part* p,
          * XYShift for the particle reaching the element, the exit XYShift
          * only if it survives (the CPU per-particle blocks skip lost
          * particles); both also when local apertures are ignored */
-        double const psi_nf = e->rot_s_rad_no_frame, psi_wf = e->rot_s_rad;
-        int const shifted = (e->shift_x != 0.0 || e->shift_y != 0.0 || psi_nf != 0.0 || psi_wf != 0.0);
-        if (shifted) {
-            double mx, my;
-            if (!backtrack) { mx = e->shift_x - 0.0; my = e->shift_y - 0.0; }
-            else { mx = -(0.0 - e->shift_x); my = -(0.0 - e->shift_y); }
-            p->x += -mx;
-            p->y += -my;
-            if (psi_nf != 0.0) xto_srotation(p, sin(psi_nf), cos(psi_nf));
-            if (psi_wf != 0.0) xto_srotation(p, sin(psi_wf), cos(psi_wf));
-        }
+        int const shifted = xto_shifted(e);
+        if (shifted) xto_shift_in(e, p, backtrack);
         xto_aperture(e, p);
-        if (shifted && p->state > 0) {
-            double mx, my;
-            if (psi_wf != 0.0) xto_srotation(p, sin(-psi_wf), cos(-psi_wf));
-            if (psi_nf != 0.0) xto_srotation(p, sin(-psi_nf), cos(-psi_nf));
-            if (!backtrack) { mx = 0.0 - e->shift_x; my = 0.0 - e->shift_y; }
-            else { mx = -(e->shift_x - 0.0); my = -(e->shift_y - 0.0); }
-            p->x += -mx;
-            p->y += -my;
-        }
+        if (shifted && p->state > 0) xto_shift_out(e, p, backtrack);
         return 0;
     }
     case XTG_CLS_DIPOLE_EDGE: {
@@ -1688,9 +1721,12 @@ int32_t xto_validate(const xtg_element* els, int64_t n, char* msg, int64_t msg_l
         else if (e->order_rel < -1 || e->order_rel >= 20) why = "relative multipole order out of range (0..19)";
         else if (((e->shift_x != 0 || e->shift_y != 0 || e->rot_s_rad != 0 || e->rot_s_rad_no_frame != 0)
                   && e->cls != XTG_CLS_LIMIT_RECT && e->cls != XTG_CLS_LIMIT_ELLIPSE
-                  && e->cls != XTG_CLS_LIMIT_POLYGON && e->cls != XTG_CLS_LIMIT_RECT_ELLIPSE)
+                  && e->cls != XTG_CLS_LIMIT_POLYGON && e->cls != XTG_CLS_LIMIT_RECT_ELLIPSE
+                  && e->cls != XTG_CLS_DIPOLE_EDGE
+                  && !(e->cls == XTG_CLS_MULTIPOLE && e->isthick <= 0 && e->slice == XTG_SLICE_NONE))
                  || e->shift_s != 0 || e->rot_x_rad != 0 || e->rot_y_rad != 0)
-            why = "misalignments (shift/rotation) are not supported (transverse shifts and tilts: apertures only)";
+            why = "misalignments (shift/rotation) are not supported (transverse shifts and tilts: "
+                  "apertures, thin Multipoles and DipoleEdges only)";
         else if (e->cls >= XTG_CLS_MULTIPOLE && e->cls <= XTG_CLS_OCTUPOLE) {
             int64_t model = e->model;
             if (e->cls == XTG_CLS_MULTIPOLE && e->isthick <= 0) model = -1;

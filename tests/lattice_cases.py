@@ -182,3 +182,28 @@ def shifted_apertures():
            xt.LimitEllipse(a=0.016, b=0.008, rot_s_rad_no_frame=-0.2, rot_s_rad=0.05,
                            shift_x=5e-4)]
     return xt.Line(elements=els)
+
+
+def shifted_thin_elements():
+    """Thin multipoles and dipole edges with transverse shifts and tilts
+    (skew and shifted kicks as MAD-X thin lattices give them), among drifts
+    and an aperture that a wide beam hits."""
+    els = [xt.Drift(length=0.4),
+           xt.Multipole(knl=[0.0, 0.08, 0.5], ksl=[0.0, 0.01], shift_x=1e-3, shift_y=-5e-4),
+           xt.Drift(length=0.3),
+           xt.Multipole(knl=[0.0, -0.06], rot_s_rad=0.4),                      # tilted quad
+           xt.Drift(length=0.3),
+           xt.Multipole(knl=[2e-3], hxl=2e-3, length=0.5, rot_s_rad=-0.1, shift_x=-2e-4),
+           xt.Drift(length=0.2),
+           xt.Multipole(knl=[0.0, 0.0, 0.0], shift_x=7e-4, rot_s_rad_no_frame=0.2),  # no strength
+           xt.DipoleEdge(k=0.02, e1=0.1, hgap=0.03, fint=0.5, shift_x=5e-4, shift_y=3e-4),
+           xt.Drift(length=0.3),
+           xt.DipoleEdge(k=0.02, e1=-0.05, model="full", side="exit", rot_s_rad=0.25),
+           xt.Drift(length=0.2),
+           xt.DipoleEdge(k=0.02, e1=0.1, model="suppressed", shift_y=-4e-4, rot_s_rad=0.1),
+           xt.Drift(length=0.3),
+           xt.LimitRect(min_x=-0.015, max_x=0.015, min_y=-0.01, max_y=0.01),
+           xt.Drift(length=0.2),
+           xt.Multipole(knl=[0.0, 0.05, -0.3, 2.0], ksl=[0.0, 0.0, 0.1], shift_y=2e-3,
+                        rot_s_rad=0.7, rot_s_rad_no_frame=-0.3)]
+    return xt.Line(elements=els)

@@ -365,6 +365,20 @@ def test_shifted_apertures(arith, flags):
     compare(got, ref, 1e-14 if arith == "exact" else 1e-12)
 
 
+@pytest.mark.parametrize("arith", ["exact", "fast"])
+@pytest.mark.parametrize("flags", [0, 1 << 0, 1 << 4])
+def test_shifted_thin_elements(arith, flags):
+    """Shifted and tilted thin multipoles and dipole edges on the GPU
+    against the oracle (itself pinned to the reference's transformation
+    wrapper for Multipole and DipoleEdge)."""
+    from lattice_cases import shifted_thin_elements
+    recs, arrs, L = _setup(shifted_thin_elements(), small_beam(400, seed=17, scale=6.0))
+    got, ref = _run_both(recs, arrs, L, arith=arith, num_turns=3, track_flags=flags)
+    for f in ("state", "at_turn", "at_element"):
+        assert np.array_equal(got[f], ref[f]), f
+    compare(got, ref, 1e-14 if arith == "exact" else 1e-12)
+
+
 def test_batch_matches_per_seed_oracle():
     """Three error seeds of one ring in one persistent launch, particles of
     the seeds interleaved: each particle equals the oracle run of its seed."""

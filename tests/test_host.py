@@ -136,6 +136,34 @@ def test_aperture_shifts_validated():
         assert st == _abi.XTG_E_UNSUPPORTED and "misalignment" in _abi.last_error(lib)
 
 
+def test_thin_element_shifts_validated():
+    """Transverse shifts and tilts pass for thin multipoles and dipole edges
+    (oracle and library alike); a thick multipole or a quadrupole with one,
+    or a thin multipole with a longitudinal shift, is rejected."""
+    line = xt.Line(elements=[xt.Multipole(knl=[0.0, 0.1], shift_x=1e-3, rot_s_rad=0.2),
+                             xt.DipoleEdge(k=1e-3, e1=0.01, shift_y=1e-3),
+                             xt.Multipole(knl=[0.0, 0.1], length=1.0, isthick=True),
+                             xt.Quadrupole(length=1.0, k1=0.01)])
+    recs = line._element_records()
+    lib = _abi.load_library()
+    cfg = _abi.XtgConfig()
+    h = ctypes.c_void_p()
+    assert pyoracle.validate(recs)[0] == _abi.XTG_OK
+    st = lib.xtg_lattice_create(recs.ctypes.data_as(ctypes.c_void_p), 4, ctypes.byref(cfg),
+                                ctypes.byref(h))
+    assert st != _abi.XTG_E_UNSUPPORTED       # without a GPU: validated, then no device
+    if st == _abi.XTG_OK:
+        lib.xtg_lattice_destroy(h)
+    for i, field in ((2, "shift_x"), (3, "rot_s_rad"), (0, "shift_s"), (1, "rot_y_rad")):
+        bad = recs.copy()
+        bad[i][field] = 1e-3
+        st, msg = pyoracle.validate(bad)
+        assert st == _abi.XTG_E_UNSUPPORTED and "misalignment" in msg
+        st = lib.xtg_lattice_create(bad.ctypes.data_as(ctypes.c_void_p), 4, ctypes.byref(cfg),
+                                    ctypes.byref(h))
+        assert st == _abi.XTG_E_UNSUPPORTED and "misalignment" in _abi.last_error(lib)
+
+
 def test_null_arguments_return_errors():
     lib = _abi.load_library()
     assert lib.xtg_lattice_create(None, 0, None, None) == _abi.XTG_E_NULL

@@ -9,7 +9,8 @@ import pytest
 import pyoracle
 import xtrack_gb300 as xt
 from xtrack_gb300 import workloads
-from lattice_cases import element_zoo, fringe_zoo, shifted_apertures, sliced_line, small_beam
+from lattice_cases import (element_zoo, fringe_zoo, shifted_apertures, shifted_thin_elements,
+                           sliced_line, small_beam)
 
 pyoracle.ensure_built(with_ref=True)
 pytestmark = pytest.mark.skipif(not pyoracle.ref_available(),
@@ -104,6 +105,27 @@ def test_shifted_apertures(flags):
     _assert_identical(a, b)
     if flags == 0:
         assert 50 < np.sum(a["state"] == 0) < 350
+
+
+@pytest.mark.parametrize("flags", [0, 1 << 0, 1 << 4])
+def test_shifted_thin_elements(flags):
+    """Thin multipoles (one of zero strength, one with a curvature kick) and
+    dipole edges (linear, full, suppressed) with transverse shifts and
+    tilts, through the reference's own transformation wrapper for
+    Multipole and DipoleEdge; forward, backtracking (the full edge kills)
+    and with local apertures ignored; bit for bit."""
+    a, b = _both(shifted_thin_elements(), small_beam(400, seed=17, scale=6.0), num_turns=3,
+                 track_flags=flags)
+    _assert_identical(a, b)
+    if flags == 0:
+        assert 0 < np.sum(a["state"] <= 0) < 400
+    plain = shifted_thin_elements()
+    for e in plain.elements:
+        for f in ("shift_x", "shift_y", "rot_s_rad", "rot_s_rad_no_frame"):
+            if hasattr(e, f):
+                setattr(e, f, 0.0)
+    c, _ = _both(plain, small_beam(400, seed=17, scale=6.0), num_turns=3, track_flags=flags)
+    assert not np.array_equal(a["x"], c["x"])   # the transforms act
 
 
 @pytest.mark.parametrize("thin", [True, False])

@@ -13,7 +13,8 @@ import pyoracle
 import xtrack_gb300 as xt
 from xtrack_gb300 import serialization as ser
 from xtrack_gb300 import workloads
-from lattice_cases import element_zoo, fringe_zoo, shifted_apertures, sliced_line
+from lattice_cases import (element_zoo, fringe_zoo, shifted_apertures, shifted_thin_elements,
+                           sliced_line)
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LHC = os.path.join(HERE, "golden", "lhc", "hllhc14_thin_64p_10t.npz")
@@ -42,7 +43,7 @@ def _with_polygon():
 
 @pytest.mark.parametrize("factory", [workloads.toy_ring, element_zoo, lambda: sliced_line(True),
                                      _with_polygon, fringe_zoo, shifted_apertures,
-                                     lambda: sliced_line(False),
+                                     shifted_thin_elements, lambda: sliced_line(False),
                                      lambda: workloads.thick_ring(n_arcs=1, n_cells=2)])
 def test_dict_and_json_round_trip(factory, tmp_path):
     line = factory()

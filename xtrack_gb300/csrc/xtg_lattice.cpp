@@ -406,6 +406,18 @@ int32_t exact_pass_coefs(int64_t order, double inv_factorial, const double* knl,
 
 }  // namespace
 
+// Elements whose transverse shifts and s-tilts run through the straight
+// misalignment of zero length (track_local_particle_with_transformations.h:
+// 99-160, track_misalignments.h:38-130 at zero length, anchor, shift_s,
+// rot_x_rad and rot_y_rad): the apertures, a thin Multipole (no `h` field,
+// so not curved; `isthick` 0, so length 0) and DipoleEdge (no length).
+static bool thin_straight(const xtg_element& e) {
+    return e.cls == XTG_CLS_LIMIT_RECT || e.cls == XTG_CLS_LIMIT_ELLIPSE ||
+           e.cls == XTG_CLS_LIMIT_POLYGON || e.cls == XTG_CLS_LIMIT_RECT_ELLIPSE ||
+           e.cls == XTG_CLS_DIPOLE_EDGE ||
+           (e.cls == XTG_CLS_MULTIPOLE && e.isthick <= 0 && e.slice == XTG_SLICE_NONE);
+}
+
 // --------------------------------------------------------------------------
 int32_t validate_element(const xtg_element& e, int64_t idx, std::string* why) {
     auto fail = [&](const char* m) {
@@ -417,14 +429,16 @@ int32_t validate_element(const xtg_element& e, int64_t idx, std::string* why) {
     if (e.order < 0 || e.order >= XTG_MAX_KNL) return fail("multipole order out of range");
     if (e.order_rel < -1 || e.order_rel >= 20)
         return fail("relative multipole order out of range (0..19)");
-    bool const aperture = e.cls == XTG_CLS_LIMIT_RECT || e.cls == XTG_CLS_LIMIT_ELLIPSE ||
-                          e.cls == XTG_CLS_LIMIT_POLYGON || e.cls == XTG_CLS_LIMIT_RECT_ELLIPSE;
-    if (!aperture && (e.shift_x != 0 || e.shift_y != 0))
-        return fail("misalignments (shift/rotation) are not supported (transverse shifts: apertures only)");
-    if (!aperture && (e.rot_s_rad != 0 || e.rot_s_rad_no_frame != 0))
-        return fail("misalignments (shift/rotation) are not supported (transverse shifts and tilts: apertures only)");
+    bool const movable = thin_straight(e);
+    if (!movable && (e.shift_x != 0 || e.shift_y != 0))
+        return fail("misalignments (shift/rotation) are not supported (transverse shifts: apertures, "
+                    "thin Multipoles and DipoleEdges only)");
+    if (!movable && (e.rot_s_rad != 0 || e.rot_s_rad_no_frame != 0))
+        return fail("misalignments (shift/rotation) are not supported (transverse shifts and tilts: "
+                    "apertures, thin Multipoles and DipoleEdges only)");
     if (e.shift_s != 0 || e.rot_x_rad != 0 || e.rot_y_rad != 0)
-        return fail("misalignments (shift/rotation) are not supported (transverse shifts and tilts: apertures only)");
+        return fail("misalignments (shift/rotation) are not supported (transverse shifts and tilts: "
+                    "apertures, thin Multipoles and DipoleEdges only)");
     if (e.cls >= XTG_CLS_MULTIPOLE && e.cls <= XTG_CLS_OCTUPOLE) {
         int64_t model = e.model;
         if (e.cls == XTG_CLS_MULTIPOLE && e.isthick <= 0) model = -1;
@@ -1075,9 +1089,16 @@ int32_t pack_lattice(const xtg_element* els, int64_t n, const xtg_config& cfg,
             }
             break;
         }
-        if ((e.cls == XTG_CLS_LIMIT_RECT || e.cls == XTG_CLS_LIMIT_ELLIPSE ||
-             e.cls == XTG_CLS_LIMIT_POLYGON || e.cls == XTG_CLS_LIMIT_RECT_ELLIPSE) &&
+        if (thin_straight(e) &&
             (e.shift_x != 0.0 || e.shift_y != 0.0 || e.rot_s_rad != 0.0 || e.rot_s_rad_no_frame != 0.0)) {
+            // the kernel applies the block on these records only
+            int32_t const op = rb.head<RecHeader>()->op;
+            if (!(op == OP_KICK || op == OP_NOP || op == OP_DIPOLE_EDGE || op == OP_LIMIT_RECT ||
+                  op == OP_LIMIT_ELLIPSE || op == OP_LIMIT_POLYGON || op == OP_LIMIT_RECT_ELLIPSE)) {
+                *err = "element " + std::to_string(i) +
+                       ": misalignments (shift/rotation) are not supported on this record kind";
+                return (int32_t)XTG_E_UNSUPPORTED;
+            }
             // entry and exit of track_misalignment_entry/exit_straight with
             // zero anchor, shift_s, rot_x_rad and rot_y_rad
             double const mis_in_x = e.shift_x - 0.0, mis_in_y = e.shift_y - 0.0;

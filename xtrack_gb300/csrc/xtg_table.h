@@ -46,8 +46,8 @@ enum Op : int32_t {
 // RecHeader.flags
 enum : int32_t {
     F_GLOBAL_APER = 1,    // statically thick class: global aperture follows
-    F_SHIFTED = 2,        // aperture with a transverse shift or tilt: the record
-                          // ends with its ApertureShift block
+    F_SHIFTED = 2,        // aperture, thin Multipole or DipoleEdge with a transverse
+                          // shift or tilt: the record ends with its ApertureShift block
 };
 
 struct alignas(16) RecHeader {
@@ -75,15 +75,15 @@ struct alignas(16) LimitEllipseRec {
     int64_t reserved;
 };
 
-// Transverse shift and tilt of an aperture
-// (track_local_particle_with_transformations.h with shift_x, shift_y,
+// Transverse shift and tilt of an aperture, a thin Multipole or a
+// DipoleEdge (track_local_particle_with_transformations.h with shift_x, shift_y,
 // rot_s_rad, rot_s_rad_no_frame; track_misalignments.h:38-112,
 // track_xyshift.h, track_srotation.h). Entry: the XYShift adds in_x, in_y
 // (-(dx - 0); -(0 - dx) in backtracking tables), then the s-rotations by
 // rot_s_rad_no_frame and rot_s_rad, each when nonzero, as (sin, cos). Exit:
 // the s-rotations by -rot_s_rad and -rot_s_rad_no_frame, then the XYShift
 // adds out_x, out_y. The entry applies to every particle reaching the
-// aperture, the exit only to those that survive it (the CPU per-particle
+// element, the exit only to those that survive it (the CPU per-particle
 // blocks skip lost particles); both apply when local apertures are ignored.
 struct ApertureShift {
     double in_x, in_y, out_x, out_y;

@@ -361,10 +361,10 @@ __device__ __noinline__ void multi_element_monitor(const xtg_multi_element_monit
         }
     }
 }
-// Transverse shift of an aperture record (F_SHIFTED, ApertureShift in
-// xtg_table.h): the entry XYShift for the particle reaching the aperture,
-// the exit XYShift only if it survives; both also when local apertures are
-// ignored. The block is found again from the header at the exit, so that
+// Transverse shift and tilt of a record (F_SHIFTED, ApertureShift in
+// xtg_table.h: apertures, thin Multipoles, DipoleEdges): the entry
+// transform for the particle reaching the element, the exit transform only
+// if it survives; both also when local apertures are ignored. The block is found again from the header at the exit, so that
 // nothing stays live across the check.
 // limitpolygon.h:64-90: the crossing-number test with the inscribed-circle
 // shortcut of the CPU build; out of line (polygons are rare in a turn)
@@ -429,7 +429,9 @@ __device__ __forceinline__ bool apply_record(PState& p, const unsigned char* __r
     }
     case OP_KICK: {
         const KickRec& r = *reinterpret_cast<const KickRec*>(rec);
+        aperture_shift_in(p, rec, h);
         apply_kick<kExact>(p, kick_args(r), reinterpret_cast<const double*>(rec + sizeof(KickRec)));
+        aperture_shift_out(p, rec, h);
         break;
     }
     case OP_MAGNET: {
@@ -448,12 +450,14 @@ __device__ __forceinline__ bool apply_record(PState& p, const unsigned char* __r
         // 29-37) or the full model, which kills when backtracking; neither
         // touches ax, ay
         const DipoleEdgeRec& r = *reinterpret_cast<const DipoleEdgeRec*>(rec);
+        aperture_shift_in(p, rec, h);
         if (r.model == 0) {
             edge_linear_kick<kExact>(p, r.r21, r.r43);
         } else {
             p = fringe_edge(p, reinterpret_cast<const double*>(rec + sizeof(DipoleEdgeRec)) + r.fringe,
                             r.backtrack != 0);
         }
+        aperture_shift_out(p, rec, h);
         break;
     }
     case OP_CAVITY: {
@@ -524,6 +528,13 @@ __device__ __forceinline__ bool apply_record(PState& p, const unsigned char* __r
         break;
     case OP_MON_PROFILE:
         monitor_profile(*reinterpret_cast<const MonProfileRec*>(rec), p, pid);
+        break;
+    case OP_NOP:
+        // a shifted or tilted element with no effect of its own (a thin
+        // Multipole of zero strength, a suppressed DipoleEdge) still moves
+        // the particle by the entry and exit transforms
+        aperture_shift_in(p, rec, h);
+        aperture_shift_out(p, rec, h);
         break;
     default:
         break;

@@ -63,8 +63,8 @@ class BeamElement:
         rec["weight"] = 1.0
         rec["order_rel"] = -1
         self._fill(rec)
-        # transverse shift and tilt (apertures:
-        # track_local_particle_with_transformations.h)
+        # transverse shift and tilt (apertures, thin multipoles, dipole
+        # edges: track_local_particle_with_transformations.h)
         for f in ("shift_x", "shift_y", "rot_s_rad", "rot_s_rad_no_frame"):
             rec[f] = getattr(self, f, 0.0)
         return rec
@@ -197,9 +197,16 @@ class Multipole(_Magnet):
 
     def __init__(self, knl=None, ksl=None, order=None, hxl=0.0, length=0.0, isthick=False,
                  knl_rel=None, ksl_rel=None, main_order=0, main_is_skew=False,
-                 num_multipole_kicks=0, model="adaptive", integrator="adaptive"):
+                 num_multipole_kicks=0, model="adaptive", integrator="adaptive", shift_x=0.0,
+                 shift_y=0.0, rot_s_rad=0.0, rot_s_rad_no_frame=0.0):
         self._init_common(order, knl, ksl, knl_rel, ksl_rel, model, integrator,
                           num_multipole_kicks, default_order=0)
+        # transverse shift and tilt: thin multipoles only (a thick one is
+        # rejected when the tracker is built)
+        self.shift_x = float(shift_x)
+        self.shift_y = float(shift_y)
+        self.rot_s_rad = float(rot_s_rad)
+        self.rot_s_rad_no_frame = float(rot_s_rad_no_frame)
         self.hxl = float(hxl)
         self.length = float(length)
         self._isthick = bool(isthick)
@@ -584,7 +591,12 @@ class DipoleEdge(BeamElement):
     _SIDES = {"entry": 0, "exit": 1}
 
     def __init__(self, k=None, e1=None, e1_fd=None, hgap=None, fint=None, model=None,
-                 side=None, h=None):
+                 side=None, h=None, shift_x=0.0, shift_y=0.0, rot_s_rad=0.0,
+                 rot_s_rad_no_frame=0.0):
+        self.shift_x = float(shift_x)
+        self.shift_y = float(shift_y)
+        self.rot_s_rad = float(rot_s_rad)
+        self.rot_s_rad_no_frame = float(rot_s_rad_no_frame)
         if h is not None:
             if k is not None:
                 raise ValueError("give k or its older name h, not both")

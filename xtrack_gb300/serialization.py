@@ -39,7 +39,8 @@ _EDGE_KEYS = ("edge_entry_active", "edge_exit_active", "edge_entry_model", "edge
 _ACCEPT = {
     "Marker": (),
     "Drift": ("length", "model"),
-    "Multipole": ("length", "hxl", "isthick", "main_order", "main_is_skew") + _MAGNET_KEYS,
+    "Multipole": ("length", "hxl", "isthick", "main_order", "main_is_skew", "shift_x", "shift_y",
+                  "rot_s_rad", "rot_s_rad_no_frame") + _MAGNET_KEYS,
     "Bend": ("length", "angle", "k0", "k1", "k2") + _MAGNET_KEYS + _EDGE_KEYS,
     "Quadrupole": ("length", "k1", "k1s", "main_is_skew", "edge_entry_active",
                    "edge_exit_active") + _MAGNET_KEYS,
@@ -57,7 +58,8 @@ _ACCEPT = {
                          "shift_y", "rot_s_rad", "rot_s_rad_no_frame"),
     "LimitPolygon": ("x_vertices", "y_vertices", "shift_x", "shift_y", "rot_s_rad",
                      "rot_s_rad_no_frame"),
-    "DipoleEdge": ("k", "e1", "e1_fd", "hgap", "fint", "model", "side"),
+    "DipoleEdge": ("k", "e1", "e1_fd", "hgap", "fint", "model", "side", "shift_x", "shift_y",
+                   "rot_s_rad", "rot_s_rad_no_frame"),
 }
 
 
@@ -106,6 +108,9 @@ def element_from_dict(dct, name="?"):
     return klass(**kw)
 
 
+_TRANSFORM_KEYS = ("shift_x", "shift_y", "rot_s_rad", "rot_s_rad_no_frame")
+
+
 def element_to_dict(e):
     """xtrack-format dict of an element of this package."""
     cname = type(e).__name__
@@ -146,6 +151,7 @@ def element_to_dict(e):
             out["model"] = e.model
         if e._side != 0:
             out["side"] = e.side
+        out.update({f: getattr(e, f) for f in _TRANSFORM_KEYS if getattr(e, f) != 0.0})
         return out
     # magnets
     out.update(knl=e.knl.tolist(), ksl=e.ksl.tolist(), order=e.order,
@@ -154,6 +160,7 @@ def element_to_dict(e):
     if isinstance(e, el.Multipole):
         out.update(length=e.length, hxl=e.hxl, isthick=int(e.isthick),
                    main_order=e.main_order, main_is_skew=int(e.main_is_skew))
+        out.update({f: getattr(e, f) for f in _TRANSFORM_KEYS if getattr(e, f) != 0.0})
     elif isinstance(e, el.Bend):
         out.update(length=e.length, angle=e.angle, k1=e.k1, k2=e.k2)
         if e.k0 != "from_h":
