@@ -122,7 +122,12 @@ typedef struct xtg_element {
     double voltage, frequency, harmonic, lag, phase;   /* Cavity            */
     double a_squ, b_squ, a_b_squ;                      /* LimitEllipse      */
     double min_x, max_x, min_y, max_y;                 /* LimitRect         */
-    /* Misalignment fields (base_element.py:274-282); must all be zero. */
+    /* Misalignment fields (base_element.py:274-282). shift_x, shift_y,
+     * rot_s_rad and rot_s_rad_no_frame may be nonzero on the apertures, a
+     * thin Multipole (isthick 0) and DipoleEdge (the straight transform of
+     * zero length, track_misalignments.h:38-130); every other element, and
+     * shift_s, rot_x_rad, rot_y_rad everywhere, must be zero
+     * (XTG_E_UNSUPPORTED otherwise). */
     double shift_x, shift_y, shift_s;
     double rot_x_rad, rot_y_rad, rot_s_rad, rot_s_rad_no_frame;
     /* Host address of the class's extra description, read by
