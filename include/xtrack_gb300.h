@@ -401,6 +401,24 @@ int64_t xtg_launch_count(void);
 int32_t xtg_measure_fp64_peak(double* flops_per_s);
 
 /*
+ * Checks of the integer-pipe binary64 multiply that the exact push uses for
+ * its products (no reference counterpart: the reference multiplies on the
+ * FP64 unit). out[i] = a[i] * b[i], rounded to nearest even, for n pairs.
+ * xtg_f64_mul_host computes on the host (host arrays); xtg_f64_mul_device
+ * runs the device routine in a kernel on `stream` (device arrays). Both
+ * must equal the hardware multiply bit for bit.
+ */
+int32_t xtg_f64_mul_host(const double* a, const double* b, double* out, int64_t n);
+int32_t xtg_f64_mul_device(const double* a, const double* b, double* out, int64_t n,
+                           void* stream);
+
+/* Throughput probe of the same multiply: independent multiply+add chains
+ * over the whole GPU with the multiplies on the integer pipes and the adds
+ * on the FP64 unit. Returns the chains' FP64 operations (multiplies plus
+ * adds) per second. */
+int32_t xtg_measure_emul_rate(double* ops_per_s);
+
+/*
  * Diagnostic of the push's failure path (no reference counterpart: the
  * reference's kernel has no waits). Runs one shared-memory barrier wait of
  * the kind the push uses to stage its element table, on a barrier that

@@ -228,7 +228,7 @@ EXPORTED_SYMBOLS = (
     "xtg_get_tuning", "xtg_set_tuning", "xtg_device_status",
     "xtg_batch_create", "xtg_batch_destroy", "xtg_batch_get_tuning", "xtg_batch_set_tuning", "xtg_batch_device_status",
     "xtg_track_batch", "xtg_sync", "xtg_launch_count", "xtg_measure_fp64_peak",
-    "xtg_check_bounded_wait",
+    "xtg_check_bounded_wait", "xtg_f64_mul_host", "xtg_f64_mul_device", "xtg_measure_emul_rate",
     "xtg_mlp_gemm", "xtg_mlp_act_backward", "xtg_mlp_colsum", "xtg_mlp_loss", "xtg_mlp_adam",
     "xtg_mlp_to_bf16", "xtg_mlp_get_last_error",
 )
@@ -313,6 +313,12 @@ def load_library(path=None):
     lib.xtg_measure_fp64_peak.restype = c.c_int32
     lib.xtg_check_bounded_wait.argtypes = [c.c_int64]
     lib.xtg_check_bounded_wait.restype = c.c_int32
+    lib.xtg_f64_mul_host.argtypes = [c.c_void_p, c.c_void_p, c.c_void_p, c.c_int64]
+    lib.xtg_f64_mul_host.restype = c.c_int32
+    lib.xtg_f64_mul_device.argtypes = [c.c_void_p, c.c_void_p, c.c_void_p, c.c_int64, c.c_void_p]
+    lib.xtg_f64_mul_device.restype = c.c_int32
+    lib.xtg_measure_emul_rate.argtypes = [c.POINTER(c.c_double)]
+    lib.xtg_measure_emul_rate.restype = c.c_int32
     if lib.xtg_abi_version() != 3:
         raise RuntimeError("xtrack_gb300: ABI version mismatch")
     if path == LIB_PATH:

@@ -52,18 +52,25 @@ def _defines():
     """Build-time options of the push's register budget (see xtg_track.cu):
     XTG_FAST_MIN_BLOCKS (1 or 2) resident blocks of at most
     XTG_FAST_LB_THREADS (384, the default, or 256) threads each for the fast
-    push; XTG_EXACT_LB_THREADS (256, the default, or 384) for the exact one."""
+    push; XTG_EXACT_LB_THREADS (256, the default, 384 or 512) for the exact
+    one; XTG_EXACT_EMUL (1, the default: the exact push's products on the
+    integer pipes, or 0: on the FP64 unit)."""
     out = []
     v = os.environ.get("XTG_FAST_MIN_BLOCKS")
     if v:
         if v not in ("1", "2"):
             raise ValueError("XTG_FAST_MIN_BLOCKS must be 1 or 2")
         out.append(f"-DXTG_FAST_MIN_BLOCKS={v}")
+    v = os.environ.get("XTG_EXACT_EMUL")
+    if v:
+        if v not in ("0", "1"):
+            raise ValueError("XTG_EXACT_EMUL must be 0 or 1")
+        out.append(f"-DXTG_EXACT_EMUL={v}")
     for name in ("XTG_FAST_LB_THREADS", "XTG_EXACT_LB_THREADS"):
         v = os.environ.get(name)
         if v:
-            if v not in ("256", "384"):
-                raise ValueError(f"{name} must be 256 or 384")
+            if v not in ("256", "384", "512"):
+                raise ValueError(f"{name} must be 256, 384 or 512")
             out.append(f"-D{name}={v}")
     return out
 

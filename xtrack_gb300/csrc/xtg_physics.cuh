@@ -12,14 +12,50 @@
 #pragma once
 #include <stdint.h>
 
+#include "xtg_f64emu.cuh"
 #include "xtg_table.h"
 
 namespace xtg {
 
+#ifndef XTG_DEV
 #define XTG_DEV __device__ __forceinline__
+#endif
 // Element maps that the common lattices do not use per kick are kept out of
 // line so that they cost no registers in the hot loop.
+#ifndef XTG_COLD
 #define XTG_COLD __device__ __noinline__
+#endif
+
+// Products of the exact arithmetic run on the integer pipes (emul,
+// xtg_f64emu.cuh: bit-identical to the FP64 unit's) unless this is 0.
+#ifndef XTG_EXACT_EMUL
+#define XTG_EXACT_EMUL 1
+#endif
+
+// A product of the exact arithmetic: rounded as the FP64 multiply rounds it.
+// XSplit is an operand prepared once for several products (emu_split).
+#if XTG_EXACT_EMUL
+typedef F64Split XSplit;
+XTG_DEV XSplit xsplit(double v) { return emu_split(v); }
+XTG_DEV double xmul(double a, double b) { return emul(a, b); }
+XTG_DEV double xmul(const XSplit& a, const XSplit& b) { return emul_split(a, b); }
+XTG_DEV double xmul(double a, const XSplit& b) { return emul_split(emu_split(a), b); }
+#else
+struct XSplit {
+    double v;
+};
+XTG_DEV XSplit xsplit(double v) { return XSplit{v}; }
+XTG_DEV double xmul(double a, double b) { return a * b; }
+XTG_DEV double xmul(const XSplit& a, const XSplit& b) { return a.v * b.v; }
+XTG_DEV double xmul(double a, const XSplit& b) { return a * b.v; }
+#endif
+
+// +0.0 + v, as the reference forms a sum that starts from zero: v itself,
+// except that -0 becomes +0. Integer operations, off the FP64 pipe.
+XTG_DEV double plus_zero(double v) {
+    uint64_t const b = emu_bits(v);
+    return emu_double(b == 0x8000000000000000ull ? 0ull : b);
+}
 
 constexpr double kCLightD = 299792458.0;
 constexpr double kPiD = 3.1415926535897932384626433832795028841971693993751;
@@ -69,13 +105,15 @@ XTG_DEV void set_energy(PState& p, double delta, double rvv, double rpp, double 
 template <bool kExact>
 XTG_DEV void drift_expanded(PState& p, double length) {
     if (kExact) {
-        double const xp = p.px * p.rpp;
-        double const yp = p.py * p.rpp;
-        double const dzeta = 1 - p.rv0v * (1. + (xp * xp + yp * yp) * 0.5);
-        p.x = p.x + xp * length;
-        p.y = p.y + yp * length;
+        // 1 + (xp^2 + yp^2) * 0.5 as one fused step: the product with 0.5 is
+        // exact, so a single rounding of the sum is the reference's result
+        double const xp = xmul(p.px, p.rpp);
+        double const yp = xmul(p.py, p.rpp);
+        double const dzeta = 1 - xmul(p.rv0v, fma(xmul(xp, xp) + xmul(yp, yp), 0.5, 1.));
+        p.x = p.x + xmul(xp, length);
+        p.y = p.y + xmul(yp, length);
         p.s = p.s + length;
-        set_zeta(p, p.zeta + length * dzeta);
+        set_zeta(p, p.zeta + xmul(length, dzeta));
     } else {
         // the reference's grouping, contracted as its FMA build contracts
         // it: 1 + (xp^2 + yp^2)/2 is rounded before the product with 1/rvv
@@ -90,6 +128,23 @@ XTG_DEV void drift_expanded(PState& p, double length) {
         set_zeta(p, fma(length, dzeta, p.zeta));
         p.s = p.s + length;
     }
+}
+
+// Two consecutive expanded drifts of the same length in the exact
+// arithmetic (the adjacent half drifts of a uniform magnet body): nothing
+// between them changes px, py or the energy, so the slopes, the zeta slip
+// and the three increments are those of the first, and only the four sums
+// are formed twice, in order. Bit-identical to two drift_expanded<true>.
+XTG_DEV void drift_expanded_twice_exact(PState& p, double length) {
+    double const xp = xmul(p.px, p.rpp);
+    double const yp = xmul(p.py, p.rpp);
+    double const dzeta = 1 - xmul(p.rv0v, fma(xmul(xp, xp) + xmul(yp, yp), 0.5, 1.));
+    double const dx = xmul(xp, length), dy = xmul(yp, length), dz = xmul(length, dzeta);
+    p.x = (p.x + dx) + dx;
+    p.y = (p.y + dy) + dy;
+    p.s = (p.s + length) + length;
+    set_zeta(p, p.zeta + dz);
+    set_zeta(p, p.zeta + dz);
 }
 
 // track_drift.h:26-42
@@ -340,19 +395,20 @@ XTG_COLD PState magnet_drift_curved(PState p, double length, int drift_model, do
 // 182-260). `co` holds quintuples (A, B, knl, ksl, invf) from `top` down.
 // At chi = 1, chi*knl*factor*invf equals the precomputed A (and B).
 XTG_DEV void exact_pass_chi1(PState& p, const double* __restrict__ co, int top,
-                             double kick_weight, double x, double y) {
+                             double kick_weight, const XSplit& x, const XSplit& y) {
     double dpx_mul = co[0];
     double dpy_mul = co[1];
     for (int i = top; i > 0; i--) {
         co += 5;
-        double const zre = dpx_mul * x - dpy_mul * y;
-        double const zim = dpx_mul * y + dpy_mul * x;
+        XSplit const a = xsplit(dpx_mul), b = xsplit(dpy_mul);
+        double const zre = xmul(a, x) - xmul(b, y);
+        double const zim = xmul(a, y) + xmul(b, x);
         dpx_mul = co[0] + zre;
         dpy_mul = co[1] + zim;
     }
     dpx_mul = -dpx_mul;
-    p.px = p.px + kick_weight * dpx_mul;
-    p.py = p.py + kick_weight * dpy_mul;
+    p.px = p.px + xmul(kick_weight, dpx_mul);
+    p.py = p.py + xmul(kick_weight, dpy_mul);
 }
 
 XTG_DEV void exact_pass(PState& p, const double* __restrict__ co, int top, double factor,
@@ -422,16 +478,19 @@ XTG_DEV void apply_kick(PState& p, const KickArgs& a, const double* __restrict__
     double const x = p.x, y = p.y;
     if (kExact) {
         double const kw = a.kw;
+        XSplit const sx = xsplit(x), sy = xsplit(y);
 #pragma unroll 1
         for (int q = 0; q < 3; q++) {
             int const top = a.pass[q].top;
             if (top >= 0) {
-                if (p.chi_one) exact_pass_chi1(p, coefs + a.pass[q].coef, top, kw, x, y);
+                if (p.chi_one) exact_pass_chi1(p, coefs + a.pass[q].coef, top, kw, sx, sy);
                 else exact_pass(p, coefs + a.pass[q].coef, top, a.pass[q].factor, kw, x, y);
             }
         }
         int const curv = a.curv;
         if (curv) {
+            // track_magnet_kick.h:97-142: dpx, dpy and dzeta start from 0;
+            // the first term of each is 0 + v (plus_zero), later ones sum
             double dpx = 0.0, dpy = 0.0, dzeta = 0.0;
             double const chi = p.chi;
             double C0, C1;
@@ -444,13 +503,18 @@ XTG_DEV void apply_kick(PState& p, const KickArgs& a, const double* __restrict__
             }
             if (curv & 1) {
                 double const hl = a.hl;
-                dpx = dpx + hl * p.opd;
-                dzeta = dzeta + -p.rv0v * hl * x;
+                dpx = plus_zero(xmul(hl, p.opd));
+                dzeta = plus_zero(xmul(xmul(-p.rv0v, hl), sx));
             }
-            if (curv & 2) dpx = dpx + C0 * x;
+            if (curv & 2) {
+                double const t = xmul(C0, sx);
+                dpx = (curv & 1) ? dpx + t : plus_zero(t);
+            }
             if (curv & 4) {
-                dpx = dpx + C1 * (-x * x + 0.5 * y * y);
-                dpy = dpy + C1 * x * y;
+                XSplit const nx = xsplit(-x);
+                double const t = xmul(C1, xmul(nx, sx) + xmul(xmul(0.5, y), sy));
+                dpx = (curv & 3) ? dpx + t : plus_zero(t);
+                dpy = plus_zero(xmul(xmul(C1, sx), sy));
             }
             p.px = p.px + dpx;
             p.py = p.py + dpy;
@@ -760,8 +824,8 @@ XTG_DEV void edge_linear_kick(PState& p, double r21, double r43) {
     double const c21 = p.chi_one ? r21 : p.chi * r21;
     double const c43 = p.chi_one ? r43 : p.chi * r43;
     if (kExact) {
-        p.px = p.px + c21 * x;
-        p.py = p.py + c43 * y;
+        p.px = p.px + xmul(c21, x);
+        p.py = p.py + xmul(c43, y);
     } else {
         p.px = fma(c21, x, p.px);
         p.py = fma(c43, y, p.py);
@@ -806,7 +870,16 @@ XTG_DEV void magnet_body(PState& p, const MagnetRec& r, const double* __restrict
     }
     int const n = r.n_kicks;
     if (r.integrator == INT_UNIFORM) {
-        if (kExact || (dm != 0 && dm != 1)) {
+        if (kExact && dm == 0 && r.d_edge != 0.0 && n > 0) {
+            // the two half drifts between kicks share their work
+            drift_expanded<true>(p, r.d_edge);
+            for (int i = 0; i < n - 1; i++) {
+                magnet_kick<true>(p, r, coefs, 0);
+                drift_expanded_twice_exact(p, r.d_edge);
+            }
+            magnet_kick<true>(p, r, coefs, 0);
+            drift_expanded<true>(p, r.d_edge);
+        } else if (kExact || (dm != 0 && dm != 1)) {
             for (int i = 0; i < n; i++) {
                 magnet_drift<kExact>(p, r.d_edge, dm, k0d, k1d, hd);
                 magnet_kick<kExact>(p, r, coefs, 0);

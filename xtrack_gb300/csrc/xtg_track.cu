@@ -894,6 +894,28 @@ __global__ void wait_check_kernel(int32_t* err, long long limit) {
 // ---------------------------------------------------------------------------
 // FP64 peak probe: independent DFMA chains; each thread writes one value.
 // ---------------------------------------------------------------------------
+// out[i] = a[i] * b[i] by the integer-pipe multiply (xtg_f64emu.cuh)
+__global__ void f64_mul_kernel(const double* __restrict__ a, const double* __restrict__ b,
+                               double* __restrict__ out, int64_t n) {
+    int64_t const i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = emul(a[i], b[i]);
+}
+
+// independent chains of (integer-pipe multiply, FP64 add) pairs
+__global__ void emul_probe_kernel(double* out, int iters, double m0, double m1, double d0) {
+    double v[8];
+    for (int c = 0; c < 8; c++) v[c] = 1.0 + 1e-3 * (threadIdx.x + c);
+    for (int it = 0; it < iters; it++) {
+        double const m = (it & 1) ? m1 : m0;
+        double const d = (it & 1) ? -d0 : d0;
+#pragma unroll
+        for (int c = 0; c < 8; c++) v[c] = __dadd_rn(emul(v[c], m), d);
+    }
+    double s = 0;
+    for (int c = 0; c < 8; c++) s += v[c];
+    out[(int64_t)blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
 __global__ void dfma_probe_kernel(double* out, int iters, double a, double b) {
     double r[8];
 #pragma unroll
@@ -1719,6 +1741,56 @@ int32_t xtg_measure_fp64_peak(double* flops_per_s) {
     if (err != cudaSuccess) return set_error(XTG_E_CUDA, "probe failed: %s", cudaGetErrorString(err));
     double const flops = 2.0 * 8.0 * (double)iters * (double)grid * block;
     *flops_per_s = flops / (best * 1e-3);
+    return XTG_OK;
+}
+
+int32_t xtg_f64_mul_host(const double* a, const double* b, double* out, int64_t n) {
+    if (n < 0) return set_error(XTG_E_VALUE, "xtg_f64_mul_host: negative n");
+    if (n > 0 && (!a || !b || !out)) return set_error(XTG_E_NULL, "xtg_f64_mul_host: NULL array");
+    for (int64_t i = 0; i < n; i++) out[i] = emul(a[i], b[i]);
+    return XTG_OK;
+}
+
+int32_t xtg_f64_mul_device(const double* a, const double* b, double* out, int64_t n, void* stream) {
+    if (n < 0) return set_error(XTG_E_VALUE, "xtg_f64_mul_device: negative n");
+    if (n == 0) return XTG_OK;
+    if (!a || !b || !out) return set_error(XTG_E_NULL, "xtg_f64_mul_device: NULL array");
+    int const block = 256;
+    int64_t const grid = (n + block - 1) / block;
+    if (grid > 0x7fffffffLL) return set_error(XTG_E_VALUE, "xtg_f64_mul_device: n too large");
+    f64_mul_kernel<<<(unsigned)grid, block, 0, (cudaStream_t)stream>>>(a, b, out, n);
+    g_launch_count++;
+    XTG_CUDA_CHECK(cudaGetLastError());
+    return XTG_OK;
+}
+
+int32_t xtg_measure_emul_rate(double* ops_per_s) {
+    if (!ops_per_s) return set_error(XTG_E_NULL, "xtg_measure_emul_rate: NULL output");
+    int dev = 0, sms = 0;
+    XTG_CUDA_CHECK(cudaGetDevice(&dev));
+    XTG_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    int const block = 128, grid = sms * 4, iters = 2048;
+    double* out = nullptr;
+    XTG_CUDA_CHECK(cudaMalloc(&out, (size_t)grid * block * sizeof(double)));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 1e30f;
+    for (int rep = 0; rep < 4; rep++) {
+        cudaEventRecord(e0);
+        emul_probe_kernel<<<grid, block>>>(out, iters, 1.0000001, 0.9999999, 1e-3);
+        cudaEventRecord(e1);
+        cudaEventSynchronize(e1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0 && ms < best) best = ms;
+    }
+    cudaError_t err = cudaGetLastError();
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    if (err != cudaSuccess) return set_error(XTG_E_CUDA, "probe failed: %s", cudaGetErrorString(err));
+    *ops_per_s = 2.0 * 8.0 * (double)iters * (double)grid * block / (best * 1e-3);
     return XTG_OK;
 }
 
