@@ -302,8 +302,15 @@ int32_t xtg_track(const xtg_lattice* lattice, const xtg_particles* particles,
  * use_graph are not used), compact_every and block_size are. Capacities
  * above XTG_NOALLOC_MAX_PARTICLES are rejected with XTG_E_CAPACITY; so is
  * backtracking until an xtg_track call has built the lattice's reversed
- * table. The first call on a device does the set-up (looks up the array's
- * address and clears its error word): make it before any stream capture.
+ * table. Every call looks up the array's address (no allocation); the
+ * first call on a device, and the first after the context is re-created
+ * (cudaDeviceReset), also clears its error word: make that call before any
+ * stream capture. The array is device memory of the library's module: with
+ * CUDA's lazy module loading it is reserved when the module is first loaded
+ * on a device (the first call into the push there), so make that call
+ * before a framework's allocator takes the device's free memory.
+ * xtg_device_status on any lattice of the device reports (and clears) the
+ * device-side error word of these calls along with the lattice's own.
  * All calls on a device share the one array: calls that overlap in time
  * (on different streams or host threads) race and must not be issued.
  */
@@ -362,7 +369,10 @@ int32_t xtg_set_tuning(xtg_lattice* lattice, const xtg_tuning* tuning);
 /* Device-side status of the calls on this lattice (or batch) since the last
  * status read: XTG_OK, XTG_E_TIMEOUT when a bounded wait inside a kernel gave
  * up, XTG_E_VALUE when a particle named a lattice outside the batch (that
- * particle is not tracked). Synchronizes the device and clears the status. */
+ * particle is not tracked). Synchronizes the device and clears the status.
+ * xtg_device_status also reads and clears the error word of the
+ * allocation-free calls (xtg_track_noalloc) on the current device; the
+ * lattice's own status is returned first when both are set. */
 int32_t xtg_device_status(const xtg_lattice* lattice);
 
 /*

@@ -69,7 +69,10 @@ def ensure_built(with_ref=True):
         need = need or not os.path.exists(REF_LIBS["default"])
     if need:
         targets = ["all", "ref"] if with_ref else ["all"]
-        subprocess.run(["make", "-C", HERE] + targets, check=True, capture_output=True)
+        # the xtrack sources: XTG_REFERENCE_SRC, else "reference" beside the repository
+        ref = os.environ.get("XTG_REFERENCE_SRC") or os.path.join(os.path.dirname(os.path.dirname(HERE)),
+                                                                  "reference")
+        subprocess.run(["make", "-C", HERE] + targets + [f"REF={ref}"], check=True, capture_output=True)
 
 
 def ref_available():

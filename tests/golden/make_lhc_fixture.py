@@ -9,8 +9,9 @@ element records (the lattice cannot be rebuilt from a generator without
 the reference's data file), 64 particles around the file's particle, and
 their state after 10 turns of the reference-compiled code (oracle/_ref).
 
-Run from the repository root, in a checkout with the reference at
-/root/reference:  python tests/golden/make_lhc_fixture.py
+Run from the repository root with the xtrack source tree named by
+XTG_REFERENCE_SRC (default: a directory "reference" beside the
+repository):  python tests/golden/make_lhc_fixture.py
 """
 import json
 import os
@@ -26,7 +27,8 @@ import pyoracle  # noqa: E402
 import xtrack_gb300 as xt  # noqa: E402
 from xtrack_gb300 import serialization  # noqa: E402
 
-SRC = "/root/reference/test_data/hllhc_14/line_and_particle.json"
+REF = os.environ.get("XTG_REFERENCE_SRC") or os.path.join(os.path.dirname(ROOT), "reference")
+SRC = os.path.join(REF, "test_data", "hllhc_14", "line_and_particle.json")
 OUT = os.path.join(HERE, "lhc", "hllhc14_thin_64p_10t.npz")
 KEEP_CLASSES = {"Drift", "Multipole", "Cavity"}
 KEEP = ("x", "px", "y", "py", "zeta", "delta", "ptau", "rpp", "rvv", "s", "state",

@@ -20,8 +20,9 @@ records, the particles and their state after the turns of the
 reference-compiled code (oracle/_ref), so state, at_turn and at_element
 (aperture losses) are pinned with the coordinates.
 
-Run from the repository root, in a checkout with the reference at
-/root/reference:  python tests/golden/make_real_lattice_fixtures.py
+Run from the repository root with the xtrack source tree named by
+XTG_REFERENCE_SRC (default: a directory "reference" beside the
+repository):  python tests/golden/make_real_lattice_fixtures.py
 """
 import json
 import os
@@ -37,7 +38,8 @@ import pyoracle  # noqa: E402
 import xtrack_gb300 as xt  # noqa: E402
 from xtrack_gb300 import serialization  # noqa: E402
 
-DATA = "/root/reference/test_data"
+REF = os.environ.get("XTG_REFERENCE_SRC") or os.path.join(os.path.dirname(ROOT), "reference")
+DATA = os.path.join(REF, "test_data")
 KEEP = ("x", "px", "y", "py", "zeta", "delta", "ptau", "rpp", "rvv", "s", "state",
         "at_turn", "at_element", "particle_id")
 APERTURES = ("LimitRect", "LimitEllipse", "LimitPolygon", "LimitRectEllipse")

@@ -1,7 +1,8 @@
 """xtg_track_noalloc: the allocation-free variant of xtg_track (scratch in a
 static device array) against xtg_track on the same inputs, two calls in a
-row, and its capacity limit. Named to be collected last; it also passes on
-its own."""
+row, with a turn-by-turn monitor, its capacity limit and its rejection of
+backtracking before the reversed table exists. Named to be collected last;
+it also passes on its own."""
 import ctypes
 
 import numpy as np
@@ -66,6 +67,8 @@ def test_noalloc_equals_track_on_two_calls_in_a_row(arith):
                     a, b = a.view(torch.int64), b.view(torch.int64)
                 assert torch.equal(a, b), f
         assert lost > 100
+        # the device-side status of both paths reads clean
+        _abi.check(lib.xtg_device_status(h_na), lib)
         # and the calls allocated nothing on the device
         torch.cuda.synchronize()
         free0 = torch.cuda.mem_get_info()[0]
@@ -103,3 +106,61 @@ def test_noalloc_rejects_capacity_above_limit():
             assert torch.equal(t[k], before[k])
     finally:
         lib.xtg_lattice_destroy(h)
+
+
+def test_noalloc_rejects_backtracking_before_the_reversed_table_exists():
+    lib = _abi.load_library()
+    line = workloads.toy_ring()
+    recs = line._element_records()
+    h = _lattice(lib, recs, "exact")
+    try:
+        arrs = pyoracle.host_arrays(xt.Particles(device="cpu", **small_beam(64)).to_numpy())
+        t, ps = _device_arrays(arrs)
+        st = lib.xtg_track_noalloc(h, ctypes.byref(ps), 1, 0, len(recs), 0, 0, 0, len(recs),
+                                   line.get_length(), None, 1 << _abi.FLAG_BACKTRACK, None)
+        assert st == _abi.XTG_E_VALUE
+        assert "backtracking table" in _abi.last_error(lib)
+    finally:
+        lib.xtg_lattice_destroy(h)
+
+
+@pytest.mark.parametrize("arith", ["exact", "fast"])
+def test_noalloc_with_monitor_equals_track(arith):
+    import torch
+    from xtg_testutil import make_monitor
+    lib = _abi.load_library()
+    line = workloads.toy_ring()
+    recs = line._element_records()
+    L = line.get_length()
+    n = len(recs)
+    arrs = pyoracle.host_arrays(xt.Particles(device="cpu", **small_beam(300, p0c=450e9, seed=5,
+                                                                          scale=6.0)).to_numpy())
+    h_ref = _lattice(lib, recs, arith)
+    h_na = _lattice(lib, recs, arith)
+    try:
+        out = []
+        for h, fn in ((h_ref, lib.xtg_track), (h_na, lib.xtg_track_noalloc)):
+            mon = make_monitor(0, 6, (0, 300))
+            t, ps = _device_arrays(arrs)
+            md = {k: torch.from_numpy(v).cuda() for k, v in mon["data"].items()}
+            mst = _abi.XtgMonitor()
+            for k in ("start_at_turn", "stop_at_turn", "part_id_start", "part_id_end",
+                      "ebe_mode", "n_repetitions", "repetition_period", "n_records"):
+                setattr(mst, k, int(mon[k]))
+            mst.data = _abi.particles_struct_from_ptrs(mon["n_records"], 0., 0., 0.,
+                                                       {k: v.data_ptr() for k, v in md.items()})
+            _abi.check(fn(h, ctypes.byref(ps), 6, 0, n, 1, 1, 1, n, L, ctypes.byref(mst), 0, None),
+                       lib)
+            _abi.check(lib.xtg_sync(None), lib)
+            out.append(({k: v.cpu().numpy() for k, v in t.items()},
+                        {k: v.cpu().numpy() for k, v in md.items()}))
+        (pa, ma), (pb, mb) = out
+        for f in pa:
+            assert np.array_equal(pa[f].view(np.int64), pb[f].view(np.int64)), f
+        for f in ma:
+            assert np.array_equal(ma[f].view(np.int64), mb[f].view(np.int64)), f
+        assert np.count_nonzero(ma["at_turn"]) > 0
+        _abi.check(lib.xtg_device_status(h_na), lib)
+    finally:
+        lib.xtg_lattice_destroy(h_ref)
+        lib.xtg_lattice_destroy(h_na)

@@ -1349,25 +1349,50 @@ constexpr int64_t kNoAllocLatCountOff = kNoAllocCountersOff + 16;
 constexpr int64_t kNoAllocLatBaseOff = kNoAllocLatCountOff + 16;
 constexpr int64_t kNoAllocBytes = kNoAllocLatBaseOff + 16;
 static_assert(kNoAllocItemsOff % 16 == 0 && kNoAllocLatBaseOff % 8 == 0, "scratch alignment");
+// items_kernel cuts the list into blocks of at least kMinBlock particles:
+// the item buffer always has room, so its overflow word is never set here
+static_assert(kNoAllocItems >= (XTG_NOALLOC_MAX_PARTICLES + kMinBlock - 1) / kMinBlock + 1,
+              "work items of the static scratch");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 static std::mutex g_noalloc_mu;
 static unsigned char* g_noalloc_addr[64] = {nullptr};
 
-// Per-device set-up on the first call: the array's address, and the error
-// word cleared (the rest is rewritten by every round before it is read).
+// Set-up, with the device current: the array's address is looked up on
+// every call (no allocation; it changes only when the context is created
+// anew, e.g. after cudaDeviceReset), and whenever it is new the error word
+// is cleared (the rest is rewritten by every round before it is read).
 static int32_t noalloc_scratch(int dev, unsigned char** out) {
     if (dev < 0 || dev >= 64) return set_error(XTG_E_VALUE, "xtg_track_noalloc: device %d out of range", dev);
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_addr[dev]) {
-        void* p = nullptr;
-        XTG_CUDA_CHECK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    void* p = nullptr;
+    XTG_CUDA_CHECK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    if (g_noalloc_addr[dev] != (unsigned char*)p) {
         XTG_CUDA_CHECK(cudaMemset((unsigned char*)p + kNoAllocCountersOff, 0, 16));
         g_noalloc_addr[dev] = (unsigned char*)p;
     }
     *out = g_noalloc_addr[dev];
     return XTG_OK;
+}
+
+// The device error word of the allocation-free calls on the current device
+// (0 when the path was never used there); read and cleared.
+static int32_t read_noalloc_status() {
+    int dev = 0;
+    XTG_CUDA_CHECK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return XTG_OK;
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) return XTG_OK;
+    int32_t* word = reinterpret_cast<int32_t*>(g_noalloc_addr[dev] + kNoAllocCountersOff) + 2;
+    int32_t h = 0;
+    XTG_CUDA_CHECK(cudaDeviceSynchronize());
+    XTG_CUDA_CHECK(cudaMemcpy(&h, word, sizeof(h), cudaMemcpyDeviceToHost));
+    if (h == 0) return XTG_OK;
+    XTG_CUDA_CHECK(cudaMemset(word, 0, sizeof(int32_t)));
+    if (h == XTG_DEV_ERR_TIMEOUT) return set_error(XTG_E_TIMEOUT, "a bounded device wait timed out (xtg_track_noalloc)");
+    if (h == XTG_DEV_ERR_ITEMS) return set_error(XTG_E_VALUE, "the work-item buffer is too small (xtg_track_noalloc)");
+    return set_error(XTG_E_VALUE, "device error %d in xtg_track_noalloc", (int)h);
 }
 
 template <bool kExact>
@@ -1527,7 +1552,9 @@ int32_t xtg_set_tuning(xtg_lattice* L, const xtg_tuning* t) {
 
 int32_t xtg_device_status(const xtg_lattice* L) {
     if (!L) return set_error(XTG_E_NULL, "xtg_device_status: NULL lattice");
-    return read_device_status(&L->ctx);
+    int32_t const st = read_device_status(&L->ctx);
+    int32_t const st_noalloc = read_noalloc_status();
+    return st != XTG_OK ? st : st_noalloc;
 }
 
 int32_t xtg_sync(void* stream) {
