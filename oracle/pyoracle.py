@@ -225,6 +225,22 @@ def set_multi_element_monitor(mapping, data, start_at_turn, stop_at_turn, part_i
     lib.xto_set_multi_element_monitor(ctypes.byref(m))
 
 
+def edge_distance(records, arrs, **track_kw):
+    """Tracks a copy of ``arrs`` through the oracle and returns, per
+    particle_id (0 .. n-1), the smallest distance in metres to the edge of
+    any aperture the particle reached (+inf: it reached none)."""
+    lib = _load(ORACLE_LIB, "oracle")
+    lib.xto_set_edge_distance.argtypes = [ctypes.c_void_p, ctypes.c_int64]
+    n = len(arrs["x"])
+    out = np.full(n, np.inf)
+    lib.xto_set_edge_distance(out.ctypes.data, n)
+    try:
+        track(records, {k: v.copy() for k, v in arrs.items()}, which="oracle", **track_kw)
+    finally:
+        lib.xto_set_edge_distance(None, 0)
+    return out
+
+
 def validate(records):
     ensure_built(with_ref=False)
     lib = _load(ORACLE_LIB, "oracle")

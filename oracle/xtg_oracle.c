@@ -1369,9 +1369,58 @@ static void xto_srotation(xto_part* p, double sin_z, double cos_z) {
     p->py = -sin_z * px + cos_z * py;
 }
 
+/* Per particle (indexed by particle_id), the smallest distance in metres
+ * from the particle to the edge of any aperture it reached, inside or out
+ * (set by xto_set_edge_distance; no counterpart in the reference: it lists
+ * the particles whose survival a last-ulp difference could flip). The
+ * distance to a rectangle is that to its nearest side line, to an ellipse
+ * |sqrt(x^2/a^2 + y^2/b^2) - 1| * min(a, b), to a polygon that to its
+ * nearest segment. */
+static double* xto_edge = NULL;
+static int64_t xto_edge_n = 0;
+
+static void xto_record_edge(const xtg_element* e, const xto_part* p) {
+    int64_t const id = p->particle_id;
+    if (!xto_edge || id < 0 || id >= xto_edge_n) return;
+    double const x = p->x, y = p->y;
+    double d = INFINITY;
+    if (e->cls == XTG_CLS_LIMIT_RECT || e->cls == XTG_CLS_LIMIT_RECT_ELLIPSE) {
+        double const lo_x = e->cls == XTG_CLS_LIMIT_RECT ? e->min_x : -e->max_x;
+        double const lo_y = e->cls == XTG_CLS_LIMIT_RECT ? e->min_y : -e->max_y;
+        d = fmin(fmin(fabs(x - lo_x), fabs(e->max_x - x)), fmin(fabs(y - lo_y), fabs(e->max_y - y)));
+    }
+    if (e->cls == XTG_CLS_LIMIT_ELLIPSE || e->cls == XTG_CLS_LIMIT_RECT_ELLIPSE) {
+        double const a = sqrt(e->a_squ), b = sqrt(e->b_squ);
+        double const r = sqrt(x * x / e->a_squ + y * y / e->b_squ);
+        d = fmin(d, fabs(r - 1.0) * fmin(a, b));
+    }
+    if (e->cls == XTG_CLS_LIMIT_POLYGON) {
+        const xtg_polygon* pg = (const xtg_polygon*)(uintptr_t)e->aux;
+        for (int64_t ii = 0; ii < pg->n_vertices; ii++) {
+            int64_t const jj = (ii + 1) % pg->n_vertices;
+            double const x0 = pg->x_vertices[ii], y0 = pg->y_vertices[ii];
+            double const dx = pg->x_vertices[jj] - x0, dy = pg->y_vertices[jj] - y0;
+            double const l2 = dx * dx + dy * dy;
+            double t = l2 > 0.0 ? ((x - x0) * dx + (y - y0) * dy) / l2 : 0.0;
+            if (t < 0.0) t = 0.0;
+            else if (t > 1.0) t = 1.0;
+            d = fmin(d, hypot(x - (x0 + t * dx), y - (y0 + t * dy)));
+        }
+    }
+    if (d != d) d = 0.0;   /* a NaN coordinate is as close to the edge as can be */
+    if (d < xto_edge[id]) xto_edge[id] = d;
+}
+
+int32_t xto_set_edge_distance(double* out, int64_t n) {
+    xto_edge = out;
+    xto_edge_n = out ? n : 0;
+    return XTG_OK;
+}
+
 /* The aperture check of one LimitEllipse / LimitPolygon / LimitRect on the
  * particle's current x, y (limitellipse.h, limitpolygon.h, limitrect.h). */
 static void xto_aperture(const xtg_element* e, xto_part* p) {
+    if (xto_edge && !flag_set(p, XTG_FLAG_IGNORE_LOCAL_APERTURE)) xto_record_edge(e, p);
     switch (e->cls) {
     case XTG_CLS_LIMIT_RECT_ELLIPSE: {
         /* limitrectellipse.h:14-44 */

@@ -52,6 +52,11 @@ int32_t xto_abi_sizes(int64_t* out);
  * clears it); host buffers. */
 int32_t xto_set_multi_element_monitor(const xtg_multi_element_monitor* m);
 
+/* Smallest distance to an aperture edge per particle_id (n entries, which
+ * the caller fills with +inf) recorded by the following xto_track calls at
+ * every aperture a particle reaches; NULL stops the recording. */
+int32_t xto_set_edge_distance(double* out, int64_t n);
+
 /* Threads the OpenMP runtime would use (1 when built without OpenMP). */
 int32_t xto_max_threads(void);
 

@@ -35,7 +35,8 @@ import pyoracle
 import xtrack_gb300 as xt
 from xtrack_gb300 import _abi, workloads
 from lattice_cases import element_zoo, shifted_apertures, sliced_line, small_beam
-from xtg_testutil import compare, compare_within_spread, fma_spread, gpu_track, make_monitor
+from xtg_testutil import (compare, compare_within_spread, fma_spread, gpu_track, make_monitor,
+                          near_edge_mask)
 
 pytestmark = pytest.mark.gpu
 
@@ -70,7 +71,8 @@ def test_toy_ring_one_turn_exact():
 def test_thick_ring_one_turn_exact():
     recs, arrs, L = _setup(workloads.thick_ring(), small_beam(512, seed=12))
     got, ref = _run_both(recs, arrs, L, num_turns=1)
-    compare(got, ref, 1e-14)
+    near = near_edge_mask(recs, arrs, line_length=L, num_turns=1)
+    compare(got, ref, 1e-14, near_edge=near, label="thick ring, exact, 1 turn:")
     assert np.all(got["at_turn"] == 1)
     for f in BEFORE_CAVITY:
         assert np.array_equal(got[f], ref[f]), f
@@ -79,7 +81,8 @@ def test_thick_ring_one_turn_exact():
 def test_thick_ring_one_turn_fast():
     recs, arrs, L = _setup(workloads.thick_ring(), small_beam(512, seed=13))
     got, ref = _run_both(recs, arrs, L, arith="fast", num_turns=1)
-    compare(got, ref, 1e-12)
+    near = near_edge_mask(recs, arrs, line_length=L, num_turns=1)
+    compare(got, ref, 1e-12, near_edge=near, label="thick ring, fast, 1 turn:")
 
 
 def _regular_mask(recs, arrs, L, num_turns, tol=1e-10):

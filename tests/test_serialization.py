@@ -188,20 +188,23 @@ def test_real_lattice_fixture_gpu(name, arith):
     rvv moves by an ulp, and the drifts of the following turns carry that
     to ~8e-12 relative in zeta. Fast mode: within 3x the reference's FMA
     spread."""
-    from xtg_testutil import compare, compare_within_spread, fma_spread, gpu_track
+    from xtg_testutil import (compare, compare_within_spread, fma_spread, gpu_track,
+                              near_edge_mask)
     recs, arrs, out, meta = _fixture(REAL[name][0])
     kw = dict(line_length=meta["line_length"], num_turns=meta["num_turns"], q0=meta["q0"],
               mass0=meta["mass0"])
     got, _ = gpu_track(recs, {k: v.copy() for k, v in arrs.items()}, arith=arith, **kw)
-    for f in ("state", "at_turn", "at_element"):
-        assert np.array_equal(got[f], out[f]), f
+    near = near_edge_mask(recs, arrs, **kw)
     if arith == "exact":
-        compare(got, out, 1e-10)
+        compare(got, out, 1e-10, near_edge=near, label=f"{name}, exact, {meta['num_turns']} turns:")
         kw1 = dict(kw, num_turns=1)
         one = {k: v.copy() for k, v in arrs.items()}
         pyoracle.track(recs, one, **kw1)
         g1, _ = gpu_track(recs, {k: v.copy() for k, v in arrs.items()}, arith=arith, **kw1)
         compare(g1, one, 1e-14)
     else:
+        # integer fields against the reference, near-edge particles exempt
+        # only where they differ
+        compare(got, out, np.inf, near_edge=near, label=f"{name}, fast, {meta['num_turns']} turns:")
         spread, ok = fma_spread(recs, arrs, **kw)
         compare_within_spread(got, out, spread, ok)

@@ -154,18 +154,72 @@ def rel_err(a, b, field):
     return float(np.max(np.abs(a[~same] - b[~same])) / scale)
 
 
-def compare(got, ref, coord_tol, fields=COORDS, mask=None):
+# Per-particle relative error: |got - ref| / max(|ref|, PP_FLOOR * scale),
+# scale = max |ref| of the field over the compared particles. Values below
+# a thousandth of the field's scale are measured against that floor, so
+# that a coordinate that happens to pass near zero does not report an
+# unbounded relative error.
+PP_FLOOR = 1e-3
+
+
+def per_particle_rel_err(a, b):
+    """Largest per-particle relative error (see PP_FLOOR) of finite pairs."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    fin = np.isfinite(a) & np.isfinite(b) & (np.abs(b) < 1e29)
+    if not fin.any():
+        return 0.0
+    a, b = a[fin], b[fin]
+    scale = np.max(np.abs(b))
+    if scale == 0:
+        return float(np.max(np.abs(a - b)))
+    return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), PP_FLOOR * scale)))
+
+
+def near_edge_mask(records, arrs, tol=1e-9, **track_kw):
+    """Particles (by particle_id, as a mask over the arrays' order) that come
+    within ``tol`` metres of an aperture edge in the oracle's run of the
+    same call: the particles whose state, at_turn and at_element a last-ulp
+    difference of the coordinates could change."""
+    d = pyoracle.edge_distance(records, arrs, **track_kw)
+    pid = np.asarray(arrs["particle_id"], dtype=np.int64)
+    return d[pid] <= tol
+
+
+def compare(got, ref, coord_tol, fields=COORDS, mask=None, near_edge=None, label=""):
     """Asserts integer fields bit-exact and coordinates within coord_tol
-    (scale-relative). Returns {field: (rel_err, n_bitexact)}."""
+    (scale-relative). With ``near_edge`` (a mask from near_edge_mask), the
+    particles whose integer fields differ must all be near-edge ones; they
+    are listed and left out of the coordinate comparison. Prints, per
+    field, the scale-relative and the per-particle relative error.
+    Returns {field: (rel_err, n_bitexact, per_particle_rel_err)}."""
     report = {}
-    sel = slice(None) if mask is None else mask
+    n = len(ref["x"])
+    sel = np.ones(n, dtype=bool) if mask is None else np.asarray(mask, dtype=bool).copy()
+    differ = np.zeros(n, dtype=bool)
     for f in INTS:
         if f in ref:
-            assert np.array_equal(got[f][sel], ref[f][sel]), f"{f} differs"
+            differ |= np.asarray(got[f]) != np.asarray(ref[f])
+    differ &= sel
+    if near_edge is not None:
+        listed = np.nonzero(differ)[0]
+        outside = listed[~near_edge[listed]]
+        assert len(outside) == 0, (f"integer fields differ for particles {outside[:10]} that stay "
+                                   f"farther than the near-edge tolerance from every aperture")
+        print(f"{label} near-edge particles: {int(near_edge[sel].sum())} within tolerance, "
+              f"integer mismatches among them: {listed.tolist()}")
+        sel &= ~differ
+    else:
+        for f in INTS:
+            if f in ref:
+                assert np.array_equal(got[f][sel], ref[f][sel]), f"{f} differs"
     for f in fields:
         e = rel_err(got[f][sel], ref[f][sel], f)
-        report[f] = (e, int(np.sum(got[f][sel] == ref[f][sel])))
+        pp = per_particle_rel_err(got[f][sel], ref[f][sel])
+        report[f] = (e, int(np.sum(got[f][sel] == ref[f][sel])), pp)
         assert e <= coord_tol, f"{f}: relative error {e:.3e} > {coord_tol:.1e}"
+    print(f"{label} scale-relative / per-particle relative error: " +
+          ", ".join(f"{f} {v[0]:.1e}/{v[2]:.1e}" for f, v in report.items()))
     return report
 
 
