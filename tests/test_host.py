@@ -8,6 +8,7 @@ the beam exactly once (gloo, two ranks)."""
 import ctypes
 import os
 import re
+import sys
 
 import numpy as np
 import pytest
@@ -17,6 +18,8 @@ import pyoracle
 import xtrack_gb300 as xt
 from xtrack_gb300 import _abi
 from xtrack_gb300.particles import PROTON_MASS_EV
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 HEADER = os.path.join(ROOT, "include", "xtrack_gb300.h")
@@ -304,20 +307,83 @@ def _shard_worker(rank, world, port, n, out):
     dist.destroy_process_group()
 
 
-def test_particle_sharding_gloo_two_ranks():
-    import multiprocessing as mp
+def _free_port():
     import socket
     s = socket.socket()
     s.bind(("127.0.0.1", 0))
     port = s.getsockname()[1]
     s.close()
+    return port
+
+
+def _run_ranks(target, world, *args):
+    import multiprocessing as mp
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
-    procs = [ctx.Process(target=_shard_worker, args=(r, 2, port, 1_000_001, q)) for r in range(2)]
+    port = _free_port()
+    procs = [ctx.Process(target=target, args=(r, world, port) + args + (q,)) for r in range(world)]
     for p in procs:
         p.start()
-    ranges = q.get(timeout=120)
+    res = q.get(timeout=300)
     for p in procs:
         p.join(timeout=120)
         assert p.exitcode == 0
+    return res
+
+
+def test_particle_sharding_gloo_two_ranks():
+    ranges = _run_ranks(_shard_worker, 2, 1_000_001)
     assert ranges[0][0] == 0 and ranges[0][1] == ranges[1][0] and ranges[1][1] == 1_000_001
+
+
+def _oracle_track(line, shard, num_turns=1):
+    # the per-shard push of this CPU test: the oracle on the shard's arrays
+    import pyoracle
+    from xtrack_gb300.parallel import TRACKED_FIELDS
+    arrs = pyoracle.host_arrays(shard.to_numpy())
+    pyoracle.track(line._element_records(), arrs, num_turns=num_turns,
+                   line_length=line.get_length())
+    for f in TRACKED_FIELDS:
+        setattr(shard, f, torch.from_numpy(arrs[f]))
+
+
+def _sharded_track_worker(rank, world, port, n, turns, out):
+    import sys
+    import torch.distributed as dist
+    sys.path[:0] = [os.path.join(ROOT, "oracle"), os.path.join(ROOT, "tests")]
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    from lattice_cases import small_beam
+    from xtrack_gb300 import workloads
+    from xtrack_gb300.parallel import track_sharded
+    line = workloads.toy_ring()
+    p = xt.Particles(device="cpu", **small_beam(n, p0c=450e9, seed=41, scale=7.0))
+    # ids out of slot order: sharding goes by particle_id, not by slot
+    perm = np.random.default_rng(3).permutation(n)
+    p.particle_id = torch.from_numpy(perm)
+    track_sharded(line, p, device="cpu", track=_oracle_track, num_turns=turns)
+    if rank == 0:
+        out.put(p.to_numpy())
+    dist.destroy_process_group()
+
+
+def test_sharded_track_gloo_two_ranks_equals_one_run():
+    """One beam split by particle_id over two gloo ranks, each tracking its
+    shard (through the oracle in this CPU test) and gathering the results:
+    bit-identical to one unsharded run, losses included."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    from lattice_cases import small_beam
+    from xtrack_gb300 import workloads
+    n, turns = 301, 12
+    got = _run_ranks(_sharded_track_worker, 2, n, turns)
+    line = workloads.toy_ring()
+    p = xt.Particles(device="cpu", **small_beam(n, p0c=450e9, seed=41, scale=7.0))
+    p.particle_id = torch.from_numpy(np.random.default_rng(3).permutation(n))
+    ref = pyoracle.host_arrays(p.to_numpy())
+    pyoracle.track(line._element_records(), ref, num_turns=turns, line_length=line.get_length())
+    assert 10 < int(np.sum(ref["state"] <= 0)) < n - 10
+    for f in ("x", "px", "y", "py", "zeta", "delta", "ptau", "rpp", "rvv", "s", "state",
+              "at_turn", "at_element", "particle_id"):
+        assert np.array_equal(np.asarray(got[f]).view(np.int64), np.asarray(ref[f]).view(np.int64)), f
