@@ -756,7 +756,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--arith", default="fast", choices=["exact", "fast"])
+    ap.add_argument("--arith", default="exact", choices=["exact", "fast"])
     ap.add_argument("--no-alt", action="store_true",
                     help="skip the timing of the other arithmetic mode")
     ap.add_argument("--particles", type=int, default=1_000_000)

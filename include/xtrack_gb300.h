@@ -347,7 +347,7 @@ int32_t xtg_set_multi_element_monitor(xtg_lattice* lattice,
 
 /* Launch tuning of the push. Results do not depend on it. */
 /* Defaults of a new lattice: block_size 128, compact_every 0, chunk_bytes
-   32768, use_graph 0. */
+   32768 (fast arithmetic) or 16384 (exact), use_graph 0. */
 typedef struct xtg_tuning {
     int32_t block_size;      /* threads per block: 32, 64, 128 or 256        */
     int32_t compact_every;   /* turns between lost-particle compactions;

@@ -52,7 +52,7 @@ def _defines():
     """Build-time options of the push's register budget (see xtg_track.cu):
     XTG_FAST_MIN_BLOCKS (1 or 2) resident blocks of at most
     XTG_FAST_LB_THREADS (384, the default, or 256) threads each for the fast
-    push; XTG_EXACT_LB_THREADS (256, the default, 384 or 512) for the exact
+    push; XTG_EXACT_LB_THREADS (512, the default, 384 or 256) for the exact
     one; XTG_EXACT_EMUL (1, the default: the exact push's products on the
     integer pipes, or 0: on the FP64 unit)."""
     out = []

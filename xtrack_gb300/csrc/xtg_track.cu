@@ -85,9 +85,12 @@ static int32_t set_error(int32_t code, const char* fmt, ...) {
 #ifndef XTG_FAST_LB_THREADS
 #define XTG_FAST_LB_THREADS 384
 #endif
-// the same for the exact push: 256 (228 registers) or 384 (168)
+// the same for the exact push: 512 (128 registers: four 128-thread blocks,
+// 16 warps per SM; the integer-pipe multiplies are latency chains that need
+// the warps: 394k particle-turns/s on the thick ring against 382k at 384
+// and 328k at 256), 384 (168) or 256 (192)
 #ifndef XTG_EXACT_LB_THREADS
-#define XTG_EXACT_LB_THREADS 256
+#define XTG_EXACT_LB_THREADS 512
 #endif
 
 // largest staging chunk: two chunks plus the static shared memory of the
@@ -1494,6 +1497,8 @@ int32_t xtg_lattice_create(const xtg_element* elements, int64_t n_elements, cons
     L->ctx.lattices.emplace_back(elements, elements + n_elements);
     own_monitors(&L->ctx);
     L->ctx.config = *config;
+    // the exact push runs four blocks per SM: 2 x 16 KB chunks each fit
+    if (config->arith == XTG_ARITH_EXACT) L->ctx.tune.chunk_bytes = 16384;
     XTG_CUDA_CHECK(cudaGetDevice(&L->ctx.device));
     int32_t st = build_tables(&L->ctx, false, &L->ctx.fwd);
     if (st != XTG_OK) return st;
