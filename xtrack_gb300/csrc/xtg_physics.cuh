@@ -859,7 +859,30 @@ XTG_DEV void magnet_edge(PState& p, int kind, bool is_exit, double r21, double r
     if (kind == EDGE_LINEAR) edge_linear_kick<kExact>(p, r21, r43);
 }
 
-// track_magnet.h:25-285 (body) after the host-side resolution.
+// One drift step of a magnet body: `reps` (1 or 2) consecutive drifts of
+// the same length. Consecutive expanded drifts in the exact arithmetic
+// share their work (drift_expanded_twice_exact); other models run twice.
+template <bool kExact>
+XTG_DEV void body_drift(PState& p, double len, int reps, int dm, double k0d, double k1d, double hd) {
+    if (kExact && dm == 0 && len != 0.0) {
+        if (reps == 2) drift_expanded_twice_exact(p, len);
+        else drift_expanded<true>(p, len);
+        return;
+    }
+    for (int q = 0; q < reps; q++) magnet_drift<kExact>(p, len, dm, k0d, k1d, hd);
+}
+
+// track_magnet.h:25-285 (body) after the host-side resolution. Every
+// integrator is a sequence drift, kick, drift, ..., kick, drift; the body
+// walks it in one loop with a single kick and a single drift step in the
+// code (a few KB each once the products run on the integer pipes), so that
+// the push's instruction footprint stays within the instruction caches.
+//   uniform:   d_edge | 2 x d_edge (fast, straight models: d_fast_inside,
+//              the two halves composed) | ... | d_edge, kick weight 0;
+//   TEAPOT:    d_edge | d_inside | ... | d_edge, kick weight 0;
+//   Yoshida-4: slices of 7 kicks with weights 0 1 2 3 2 1 0 and drifts
+//              d0 d1 d2 d3 d3 d2 d1 d0; the d0 ending a slice and the d0
+//              starting the next are consecutive (one step of 2 x d0).
 template <bool kExact>
 XTG_DEV void magnet_body(PState& p, const MagnetRec& r, const double* __restrict__ coefs) {
     int const dm = r.drift_model;
@@ -869,58 +892,45 @@ XTG_DEV void magnet_body(PState& p, const MagnetRec& r, const double* __restrict
         return;
     }
     int const n = r.n_kicks;
-    if (r.integrator == INT_UNIFORM) {
-        if (kExact && dm == 0 && r.d_edge != 0.0 && n > 0) {
-            // the two half drifts between kicks share their work
-            drift_expanded<true>(p, r.d_edge);
-            for (int i = 0; i < n - 1; i++) {
-                magnet_kick<true>(p, r, coefs, 0);
-                drift_expanded_twice_exact(p, r.d_edge);
-            }
-            magnet_kick<true>(p, r, coefs, 0);
-            drift_expanded<true>(p, r.d_edge);
-        } else if (kExact || (dm != 0 && dm != 1)) {
-            for (int i = 0; i < n; i++) {
-                magnet_drift<kExact>(p, r.d_edge, dm, k0d, k1d, hd);
-                magnet_kick<kExact>(p, r, coefs, 0);
-                magnet_drift<kExact>(p, r.d_edge, dm, k0d, k1d, hd);
-            }
+    int const integ = r.integrator;
+    if (n <= 0) {
+        // no kick: the uniform and Yoshida loops run zero times; the TEAPOT
+        // sequence keeps its edge drifts and its one kick
+        if (integ == INT_TEAPOT) {
+            magnet_drift<kExact>(p, r.d_edge, dm, k0d, k1d, hd);
+            magnet_kick<kExact>(p, r, coefs, 0);
+            magnet_drift<kExact>(p, r.d_edge, dm, k0d, k1d, hd);
+        }
+        return;
+    }
+    if (integ != INT_UNIFORM && integ != INT_TEAPOT && integ != INT_YOSHIDA4) return;
+    bool const fast_merged = !kExact && (dm == 0 || dm == 1);
+    int const nk = (integ == INT_YOSHIDA4) ? 7 * n : n;
+#pragma unroll 1
+    for (int j = 0; j <= nk; j++) {
+        // the drift step before kick j (after the last kick when j == nk)
+        double len;
+        int reps = 1;
+        int kw = 0;
+        if (integ == INT_YOSHIDA4) {
+            int const m = j % 7;
+            int const di = (m == 0) ? 0 : (m <= 3 ? m : 7 - m);
+            len = r.d_yoshida[di];
+            if (m == 0 && j > 0 && j < nk) reps = 2;
+            kw = (m <= 3) ? m : 6 - m;
+        } else if (j == 0 || j == nk) {
+            len = r.d_edge;
+        } else if (integ == INT_TEAPOT) {
+            len = r.d_inside;
+        } else if (fast_merged) {
+            len = r.d_fast_inside;
         } else {
-            // adjacent half drifts of straight drift maps compose exactly
-            magnet_drift<false>(p, r.d_edge, dm, 0, 0, 0);
-            for (int i = 0; i < n - 1; i++) {
-                magnet_kick<false>(p, r, coefs, 0);
-                magnet_drift<false>(p, r.d_fast_inside, dm, 0, 0, 0);
-            }
-            magnet_kick<false>(p, r, coefs, 0);
-            magnet_drift<false>(p, r.d_edge, dm, 0, 0, 0);
+            len = r.d_edge;
+            reps = 2;
         }
-    } else if (r.integrator == INT_TEAPOT) {
-        magnet_drift<kExact>(p, r.d_edge, dm, k0d, k1d, hd);
-        for (int i = 0; i < n - 1; i++) {
-            magnet_kick<kExact>(p, r, coefs, 0);
-            magnet_drift<kExact>(p, r.d_inside, dm, k0d, k1d, hd);
-        }
-        magnet_kick<kExact>(p, r, coefs, 0);
-        magnet_drift<kExact>(p, r.d_edge, dm, k0d, k1d, hd);
-    } else if (r.integrator == INT_YOSHIDA4) {
-        for (int s = 0; s < n; s++) {
-            magnet_drift<kExact>(p, r.d_yoshida[0], dm, k0d, k1d, hd);
-            magnet_kick<kExact>(p, r, coefs, 0);
-            magnet_drift<kExact>(p, r.d_yoshida[1], dm, k0d, k1d, hd);
-            magnet_kick<kExact>(p, r, coefs, 1);
-            magnet_drift<kExact>(p, r.d_yoshida[2], dm, k0d, k1d, hd);
-            magnet_kick<kExact>(p, r, coefs, 2);
-            magnet_drift<kExact>(p, r.d_yoshida[3], dm, k0d, k1d, hd);
-            magnet_kick<kExact>(p, r, coefs, 3);
-            magnet_drift<kExact>(p, r.d_yoshida[3], dm, k0d, k1d, hd);
-            magnet_kick<kExact>(p, r, coefs, 2);
-            magnet_drift<kExact>(p, r.d_yoshida[2], dm, k0d, k1d, hd);
-            magnet_kick<kExact>(p, r, coefs, 1);
-            magnet_drift<kExact>(p, r.d_yoshida[1], dm, k0d, k1d, hd);
-            magnet_kick<kExact>(p, r, coefs, 0);
-            magnet_drift<kExact>(p, r.d_yoshida[0], dm, k0d, k1d, hd);
-        }
+        body_drift<kExact>(p, len, reps, dm, k0d, k1d, hd);
+        if (j == nk) break;
+        magnet_kick<kExact>(p, r, coefs, kw);
     }
 }
 
