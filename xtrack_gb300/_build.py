@@ -53,19 +53,19 @@ def _defines():
     XTG_FAST_MIN_BLOCKS (1 or 2) resident blocks of at most
     XTG_FAST_LB_THREADS (384, the default, or 256) threads each for the fast
     push; XTG_EXACT_LB_THREADS (512, the default, 384 or 256) for the exact
-    one; XTG_EXACT_EMUL (1, the default: the exact push's products on the
-    integer pipes, or 0: on the FP64 unit)."""
+    one; XTG_EMUL (1, the default: the push's stand-alone products on the
+    integer pipes, or 0: on the FP64 unit; the results are the same)."""
     out = []
     v = os.environ.get("XTG_FAST_MIN_BLOCKS")
     if v:
         if v not in ("1", "2"):
             raise ValueError("XTG_FAST_MIN_BLOCKS must be 1 or 2")
         out.append(f"-DXTG_FAST_MIN_BLOCKS={v}")
-    v = os.environ.get("XTG_EXACT_EMUL")
+    v = os.environ.get("XTG_EMUL")
     if v:
         if v not in ("0", "1"):
-            raise ValueError("XTG_EXACT_EMUL must be 0 or 1")
-        out.append(f"-DXTG_EXACT_EMUL={v}")
+            raise ValueError("XTG_EMUL must be 0 or 1")
+        out.append(f"-DXTG_EMUL={v}")
     for name in ("XTG_FAST_LB_THREADS", "XTG_EXACT_LB_THREADS"):
         v = os.environ.get(name)
         if v:

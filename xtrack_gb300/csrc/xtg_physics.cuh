@@ -26,15 +26,17 @@ namespace xtg {
 #define XTG_COLD __device__ __noinline__
 #endif
 
-// Products of the exact arithmetic run on the integer pipes (emul,
-// xtg_f64emu.cuh: bit-identical to the FP64 unit's) unless this is 0.
-#ifndef XTG_EXACT_EMUL
-#define XTG_EXACT_EMUL 1
+// Products that are not fused into an addition (every product of the
+// exact arithmetic; the stand-alone ones of the fast arithmetic) run on the
+// integer pipes (emul, xtg_f64emu.cuh: bit-identical to the FP64 unit's)
+// unless this is 0. Either way the results are the same bits.
+#ifndef XTG_EMUL
+#define XTG_EMUL 1
 #endif
 
-// A product of the exact arithmetic: rounded as the FP64 multiply rounds it.
+// A stand-alone product: rounded as the FP64 multiply rounds it.
 // XSplit is an operand prepared once for several products (emu_split).
-#if XTG_EXACT_EMUL
+#if XTG_EMUL
 typedef F64Split XSplit;
 XTG_DEV XSplit xsplit(double v) { return emu_split(v); }
 XTG_DEV double xmul(double a, double b) { return emul(a, b); }
@@ -119,9 +121,9 @@ XTG_DEV void drift_expanded(PState& p, double length) {
         // it: 1 + (xp^2 + yp^2)/2 is rounded before the product with 1/rvv
         // (regrouping it changes zeta by ~1e-12 m per turn on a 6000-drift
         // ring, far outside the reference's own FMA/no-FMA spread)
-        double const xp = p.px * p.rpp;
-        double const yp = p.py * p.rpp;
-        double const t = fma(xp, xp, yp * yp);
+        double const xp = xmul(p.px, p.rpp);
+        double const yp = xmul(p.py, p.rpp);
+        double const t = fma(xp, xp, xmul(yp, yp));
         double const dzeta = fma(-p.rv0v, fma(t, 0.5, 1.0), 1.0);
         p.x = fma(xp, length, p.x);
         p.y = fma(yp, length, p.y);
@@ -160,10 +162,10 @@ XTG_DEV void drift_exact(PState& p, double length) {
         set_zeta(p, p.zeta + dzeta * length);
         p.s = p.s + length;
     } else {
-        double const pz2 = fma(-py, py, fma(-px, px, opd * opd));
+        double const pz2 = fma(-py, py, fma(-px, px, xmul(opd, opd)));
         double const one_over_pz = 1. / sqrt(pz2);
-        double const dzeta = fma(-p.rv0v * opd, one_over_pz, 1.0);
-        double const fl = one_over_pz * length;
+        double const dzeta = fma(-xmul(p.rv0v, opd), one_over_pz, 1.0);
+        double const fl = xmul(one_over_pz, length);
         p.x = fma(px, fl, p.x);
         p.y = fma(py, fl, p.y);
         set_zeta(p, fma(dzeta, length, p.zeta));
@@ -540,7 +542,7 @@ XTG_DEV void apply_kick(PState& p, const KickArgs& a, const double* __restrict__
         }
         // every term is accumulated straight into px / py, in the
         // reference's order (multipoles, then curvature terms)
-        double const cs = p.chi_one ? a.fscale : p.chi * a.fscale;
+        double const cs = p.chi_one ? a.fscale : xmul(p.chi, a.fscale);
         p.px = fma(-cs, pr, p.px);
         p.py = fma(cs, pi, p.py);
         int const curv = a.curv;
@@ -549,13 +551,13 @@ XTG_DEV void apply_kick(PState& p, const KickArgs& a, const double* __restrict__
             if (curv & 1) {
                 double const hl = a.hl;
                 p.px = fma(hl, p.opd, p.px);
-                set_zeta(p, fma(-p.rv0v * hl, x, p.zeta));
+                set_zeta(p, fma(xmul(-p.rv0v, hl), x, p.zeta));
             }
-            if (curv & 2) p.px = fma(p.chi_one ? a.C0 : chi * a.C0, x, p.px);
+            if (curv & 2) p.px = fma(p.chi_one ? a.C0 : xmul(chi, a.C0), x, p.px);
             if (curv & 4) {
-                double const c1 = p.chi_one ? a.C1 : chi * a.C1;
-                p.px = fma(c1, fma(-x, x, 0.5 * y * y), p.px);
-                p.py = fma(c1 * x, y, p.py);
+                double const c1 = p.chi_one ? a.C1 : xmul(chi, a.C1);
+                p.px = fma(c1, fma(-x, x, xmul(xmul(0.5, y), y)), p.px);
+                p.py = fma(xmul(c1, x), y, p.py);
             }
         }
     }
@@ -821,8 +823,8 @@ XTG_COLD PState fringe_edge(PState p, const double* __restrict__ fr, bool backtr
 template <bool kExact>
 XTG_DEV void edge_linear_kick(PState& p, double r21, double r43) {
     double const x = p.x, y = p.y;
-    double const c21 = p.chi_one ? r21 : p.chi * r21;
-    double const c43 = p.chi_one ? r43 : p.chi * r43;
+    double const c21 = p.chi_one ? r21 : xmul(p.chi, r21);
+    double const c43 = p.chi_one ? r43 : xmul(p.chi, r43);
     if (kExact) {
         p.px = p.px + xmul(c21, x);
         p.py = p.py + xmul(c43, y);

@@ -473,7 +473,7 @@ __device__ __forceinline__ bool apply_record(PState& p, const unsigned char* __r
         aperture_shift_in(p, rec, h);
         if (!flag_on(a.track_flags, XTG_FLAG_IGNORE_LOCAL_APERTURE)) {
             const LimitEllipseRec& r = *reinterpret_cast<const LimitEllipseRec*>(rec);
-            double const temp = p.x * p.x * r.b_squ + p.y * p.y * r.a_squ;
+            double const temp = xmul(xmul(p.x, p.x), r.b_squ) + xmul(xmul(p.y, p.y), r.a_squ);
             int64_t const kt = ord_key(temp);
             if (!(kt >= lower_key(0.0) && kt <= r.key_a_b_squ)) p.state = 0;
         }
@@ -486,7 +486,7 @@ __device__ __forceinline__ bool apply_record(PState& p, const unsigned char* __r
         aperture_shift_in(p, rec, h);
         if (!flag_on(a.track_flags, XTG_FLAG_IGNORE_LOCAL_APERTURE)) {
             const LimitRectEllipseRec& r = *reinterpret_cast<const LimitRectEllipseRec*>(rec);
-            double const temp = p.x * p.x * r.b_squ + p.y * p.y * r.a_squ;
+            double const temp = xmul(xmul(p.x, p.x), r.b_squ) + xmul(xmul(p.y, p.y), r.a_squ);
             int64_t const kx = ord_key(p.x), ky = ord_key(p.y), kt = ord_key(temp);
             bool const alive = (kx <= r.key_max_x) && (kx >= r.key_min_x) && (ky <= r.key_max_y) &&
                                (ky >= r.key_min_y) && (kt >= lower_key(0.0)) && (kt <= r.key_a_b_squ);
