@@ -97,6 +97,13 @@ static int32_t set_error(int32_t code, const char* fmt, ...) {
 // push kernel stay within the 227 KB a block may use
 static constexpr int32_t kMaxChunkBytes = 113 * 1024;
 
+// Every record is read as at least kRecordHead bytes at once (the whole of
+// the small records: drifts, apertures, linear dipole edges), so the device
+// table and each shared-memory staging area end with kRecordSlack unused
+// bytes that such a read of the last record may touch.
+static constexpr int32_t kRecordHead = 48;
+static constexpr int32_t kRecordSlack = 32;
+
 // smallest block size of the push; the work-item buffers hold one item per
 // kMinBlock particles plus one per lattice
 static constexpr int32_t kMinBlock = 32;
@@ -419,13 +426,34 @@ __device__ __forceinline__ void aperture_shift_out(PState& p, const unsigned cha
         p = aperture_transform_out(p, reinterpret_cast<const ApertureShift*>(rec + h.nbytes - sizeof(ApertureShift)));
 }
 
+// The first kRecordHead bytes of a record, read with three 16-byte loads
+// issued together: the header and, for the small records, every field, so
+// that their maps wait on one load latency instead of a header load
+// followed by field loads.
+union RecHead {
+    uint4 w[3];
+    RecHeader h;
+    DriftRec drift;
+    LimitRectRec rect;
+    LimitEllipseRec ellipse;
+    DipoleEdgeRec dedge;
+};
+static_assert(sizeof(RecHead) == kRecordHead, "record head");
+
+__device__ __forceinline__ void load_head(RecHead& u, const unsigned char* rec) {
+    const uint4* q = reinterpret_cast<const uint4*>(rec);
+    u.w[0] = q[0];
+    u.w[1] = q[1];
+    u.w[2] = q[2];
+}
+
 template <bool kExact>
-__device__ __forceinline__ bool apply_record(PState& p, const unsigned char* __restrict__ rec,
+__device__ __forceinline__ bool apply_record(PState& p, const unsigned char* __restrict__ rec, const RecHead& u,
                                              const TrackArgs& a, const RfCtx& rf, int64_t i, int64_t pid) {
-    const RecHeader& h = *reinterpret_cast<const RecHeader*>(rec);
+    const RecHeader& h = u.h;
     switch (h.op) {
     case OP_DRIFT: {
-        const DriftRec& r = *reinterpret_cast<const DriftRec*>(rec);
+        const DriftRec& r = u.drift;
         if (r.exact) drift_exact<kExact>(p, r.length);
         else drift_expanded<kExact>(p, r.length);
         break;
@@ -452,7 +480,7 @@ __device__ __forceinline__ bool apply_record(PState& p, const unsigned char* __r
         // dipoleedge.h:14-71: the linear kick (track_dipole_edge_linear.h:
         // 29-37) or the full model, which kills when backtracking; neither
         // touches ax, ay
-        const DipoleEdgeRec& r = *reinterpret_cast<const DipoleEdgeRec*>(rec);
+        const DipoleEdgeRec& r = u.dedge;
         aperture_shift_in(p, rec, h);
         if (r.model == 0) {
             edge_linear_kick<kExact>(p, r.r21, r.r43);
@@ -472,7 +500,7 @@ __device__ __forceinline__ bool apply_record(PState& p, const unsigned char* __r
         // limitellipse.h:12-38
         aperture_shift_in(p, rec, h);
         if (!flag_on(a.track_flags, XTG_FLAG_IGNORE_LOCAL_APERTURE)) {
-            const LimitEllipseRec& r = *reinterpret_cast<const LimitEllipseRec*>(rec);
+            const LimitEllipseRec& r = u.ellipse;
             double const temp = xmul(xmul(p.x, p.x), r.b_squ) + xmul(xmul(p.y, p.y), r.a_squ);
             int64_t const kt = ord_key(temp);
             if (!(kt >= lower_key(0.0) && kt <= r.key_a_b_squ)) p.state = 0;
@@ -501,7 +529,7 @@ __device__ __forceinline__ bool apply_record(PState& p, const unsigned char* __r
         if (!flag_on(a.track_flags, XTG_FLAG_IGNORE_LOCAL_APERTURE)) {
             // the FP64 compares of the reference as integer compares of
             // ordered keys (ord_key, xtg_table.h): same outcome, NaN lost
-            const LimitRectRec& r = *reinterpret_cast<const LimitRectRec*>(rec);
+            const LimitRectRec& r = u.rect;
             int64_t const kx = ord_key(p.x), ky = ord_key(p.y);
             bool const alive = (kx >= r.key_min_x) && (kx <= r.key_max_x) && (ky >= r.key_min_y) &&
                                (ky <= r.key_max_y);
@@ -554,7 +582,9 @@ __device__ __forceinline__ void walk(PState& p, bool& active, const unsigned cha
     while (active && rec < rec_end) {
         if (a.flag_monitor == 2) monitor(a, p, i, pid);
         if (a.E.data) multi_element_monitor(a.E, p, pid);
-        bool const thick = apply_record<kExact>(p, rec, a, rf, i, pid);
+        RecHead u;
+        load_head(u, rec);
+        bool const thick = apply_record<kExact>(p, rec, u, a, rf, i, pid);
         if (thick && !ignore_global) {
             // local_particle_custom_api.h:259-287
             // |x|, |y| <= limit as ordered-key compares (ord_key)
@@ -568,7 +598,7 @@ __device__ __forceinline__ void walk(PState& p, bool& active, const unsigned cha
             break;
         }
         p.at_element += incr;
-        rec += reinterpret_cast<const RecHeader*>(rec)->nbytes;
+        rec += u.h.nbytes;
     }
 }
 
@@ -1052,8 +1082,9 @@ static int32_t build_tables(ExecCtx* C, bool backtrack, DevTables* T) {
     T->n_rec = n;
     T->h_rec_off = rec_off;
     T->max_record = max_rec;
-    size_t const nb = bytes.empty() ? 16 : bytes.size();
+    size_t const nb = (bytes.empty() ? 16 : bytes.size()) + kRecordSlack;
     XTG_CUDA_CHECK(cudaMalloc(&T->d_bytes, nb));
+    XTG_CUDA_CHECK(cudaMemset(T->d_bytes, 0, nb));
     if (!bytes.empty()) XTG_CUDA_CHECK(cudaMemcpy(T->d_bytes, bytes.data(), bytes.size(), cudaMemcpyHostToDevice));
     XTG_CUDA_CHECK(cudaMalloc(&T->d_lat_base, lat_base.size() * sizeof(int64_t)));
     XTG_CUDA_CHECK(cudaMemcpy(T->d_lat_base, lat_base.data(), lat_base.size() * sizeof(int64_t),
@@ -1178,11 +1209,12 @@ static int32_t run_rounds(ExecCtx* C, TrackArgs a, const int32_t* lat, int64_t c
     int32_t const block = C->tune.block_size;
     int32_t smem = 0;
     if (a.chunk_bytes > 0) {
-        smem = 2 * a.chunk_bytes;
+        // two staging buffers, then the slack of the record-head reads
+        smem = 2 * a.chunk_bytes + kRecordSlack;
         int32_t st = configure_kernel<kExact>(smem);
         if (st != XTG_OK) return st;
     }
-    a.smem_bytes = smem;
+    a.smem_bytes = smem > 0 ? 2 * a.chunk_bytes : 0;
     int grid = 0;
     int32_t st = persistent_grid<kExact>(block, smem, &grid);
     if (st != XTG_OK) return st;
