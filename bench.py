@@ -181,6 +181,10 @@ def run_gpu(args):
     peak = ctypes.c_double()
     _abi.check(lib.xtg_measure_fp64_peak(ctypes.byref(peak)))
     fp64_peak = peak.value
+    # multiply+add chains with the products on the integer pipes
+    er = ctypes.c_double()
+    _abi.check(lib.xtg_measure_emul_rate(ctypes.byref(er)))
+    emul_rate = er.value
 
     stream = torch.cuda.current_stream(dev)
     monitor = None
@@ -280,7 +284,11 @@ def run_gpu(args):
            "roofline": {"bound": "fp64", "achieved": achieved / 1e12, "peak": fp64_peak / 1e12,
                         "unit": "TFLOP/s", "frac": achieved / fp64_peak,
                         "peak_source": "in-run DFMA probe (FP64 pipe, FMA = 2)",
-                        "flops_per_particle_turn": flops_pt, "traffic": _traffic()},
+                        "flops_per_particle_turn": flops_pt, "traffic": _traffic(args.arith),
+                        "note": "the push runs its stand-alone FP64 products on the integer "
+                                "pipes (bit-identical), next to the FP64 pipe; the peak is the "
+                                "FP64 pipe's alone",
+                        "emul_probe_ops_per_s": emul_rate},
            "clocks": clk.summary()}
     if not args.no_alt:
         # the other arithmetic mode on the same beam, same step count
@@ -738,13 +746,13 @@ def run_turn_latency(args):
                               "alive": alive, "arith": args.arith}), flush=True)
 
 
-def _traffic():
-    """DRAM bytes per launch of the track kernel from the committed ncu
-    summary, when present."""
+def _traffic(arith):
+    """DRAM bytes per launch of the track kernel in arithmetic `arith` from
+    the committed ncu summary, when present."""
     p = os.path.join(ROOT, "profiles", "track_kernel_traffic.json")
     if os.path.exists(p):
         try:
-            return json.load(open(p)).get("dram_bytes_per_launch")
+            return json.load(open(p)).get(arith, {}).get("dram_bytes_per_launch")
         except Exception:
             return None
     return None
