@@ -499,10 +499,15 @@ def run_batch_scan(args):
     scan = sc.build_scan(lines, counts, r_max=args.da_rmax, device=dev)
     t_setup = time.perf_counter() - t0
     bt = xt.BatchTracker(lines, device=dev, arith=args.arith)
-    probe = sc.make_particles(scan, device=dev)
+    # the autotuner times its candidates on an evenly thinned copy of the
+    # scan (every k-th particle, all seeds kept) when the scan is large
+    k = max(1, int(np.ceil(scan.n / args.batch_tune_max)))
+    sub = np.zeros(scan.n, dtype=bool)
+    sub[::k] = True
+    probe = sc.make_particles(scan, select=sub, device=dev)
     t0 = time.perf_counter()
     tuning, rep = tu.autotune(bt, probe, turns, probe_turns=2, repeats=1,
-                              lattice_index=scan.lattice_index)
+                              lattice_index=scan.lattice_index[sub])
     t_tune = time.perf_counter() - t0
     del probe
 
@@ -535,11 +540,13 @@ def run_batch_scan(args):
            "config": {"workload": f"{n_seeds} seeds of the thick ring (6993 elements), "
                                   f"{args.batch_min}-{args.batch_max} particles per seed on a "
                                   f"polar grid 0-{args.da_rmax:g} sigma x 11 angles x 2 deltas",
-                      "turns": turns, "particles": int(scan.n), "arith": args.arith},
+                      "turns": turns, "particles": int(scan.n), "arith": args.arith,
+                      "seed_particles_min": int(counts.min()), "seed_particles_max": int(counts.max())},
            "batched_s": t_batch, "per_seed_s": t_seq, "speedup_vs_per_seed": t_seq / t_batch,
            "per_seed_particle_turns_per_s": pt / t_seq, "particle_turns": pt,
            "results_identical": same, "tuning": tuning, "autotune_s": t_tune,
-           "autotune_candidates": len(rep.get("timings", [])), "setup_s": t_setup}
+           "autotune_candidates": len(rep.get("timings", [])), "autotune_particles": int(sub.sum()),
+           "setup_s": t_setup}
     print(json.dumps(out))
     if not same:
         raise SystemExit("batched and per-seed results differ")
@@ -787,6 +794,8 @@ def main():
     ap.add_argument("--batch-min", dest="batch_min", type=int, default=1000)
     ap.add_argument("--batch-max", dest="batch_max", type=int, default=20000)
     ap.add_argument("--batch-turns", dest="batch_turns", type=int, default=20)
+    ap.add_argument("--batch-tune-max", dest="batch_tune_max", type=int, default=500000,
+                    help="largest particle count the batch autotuner times candidates on")
     ap.add_argument("--da-turns", dest="da_turns", type=int, default=100)
     ap.add_argument("--da-train-particles", dest="da_train_particles", type=int, default=16000)
     ap.add_argument("--da-lo", dest="da_lo", type=float, default=0.02)
