@@ -413,6 +413,19 @@ def run_da_screen(args):
         p, _ = net.predict(features(s_test))
         return p
 
+    if args.da_dump:
+        # the scans' inputs and plain outcomes, for studying screening
+        # strategies on the host (tracking is deterministic per particle)
+        pt, lt_pred = net.predict(features(s_test))
+        np.savez_compressed(args.da_dump, r=s_test.r, theta=s_test.theta,
+                            delta_index=s_test.delta_index, lattice_index=s_test.lattice_index,
+                            ray=ray, state=st_p, at_turn=at_p, p_survive=pt, logturn_pred=lt_pred,
+                            x_test=features(s_test), seed_features_test=s_test.seed_features,
+                            x_train=features(s_train), surv_train=surv, logturn_train=lt,
+                            lattice_index_train=s_train.lattice_index, r_train=s_train.r,
+                            ray_train=s_train.ray_index(), seed_features_train=s_train.seed_features,
+                            turns=turns, t_plain=t_plain)
+
     # (1) the network's band alone, one pass
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
@@ -550,6 +563,71 @@ def run_batch_scan(args):
     print(json.dumps(out))
     if not same:
         raise SystemExit("batched and per-seed results differ")
+
+
+def run_monitor_hbm(args):
+    """The turn-by-turn monitor's HBM regime: --particles protons (default
+    3.2e7, the monitor-stress configuration's beam) through a one-drift
+    line for --monitor-turns turns in one tracking call, with a
+    ParticlesMonitor recording x, px, y, py, zeta, delta of every particle
+    every turn in the reference's record layout (n_turns*(id - id0) +
+    turn). Per call the push reads and writes the particle arrays once and
+    writes 48 B per particle-turn of records: value = bytes moved / CUDA-event
+    time of the call, against the measured HBM copy bandwidth."""
+    import torch
+    import xtrack_gb300 as xt
+    from xtrack_gb300.monitors import ParticlesMonitor
+
+    rank, world, local = _dist()
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    n = args.particles if args.particles != 1_000_000 else 32_000_000
+    turns = args.monitor_turns
+    line = xt.Line(elements=[xt.Drift(length=1.0)])
+    rng = np.random.default_rng(5)
+    p = xt.Particles(device=dev, p0c=7e12, x=rng.normal(0, 1e-3, n), px=rng.normal(0, 1e-5, n),
+                     y=rng.normal(0, 1e-3, n), py=rng.normal(0, 1e-5, n))
+    line.build_tracker(device=dev, arith=args.arith)
+    fields = ("x", "px", "y", "py", "zeta", "delta")
+    times = []
+    for rep in range(args.warmup + args.steps):
+        mon = ParticlesMonitor(start_at_turn=rep * turns, stop_at_turn=(rep + 1) * turns,
+                               num_particles=n, fields=fields, device=dev, auto_to_numpy=False)
+        torch.cuda.synchronize(dev)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        line.track(p, num_turns=turns, turn_by_turn_monitor=mon)
+        e1.record()
+        torch.cuda.synchronize(dev)
+        if rep >= args.warmup:
+            times.append(e0.elapsed_time(e1) * 1e-3)
+        del mon
+    t = min(times)
+    mon_bytes = n * turns * 48
+    io_bytes = n * 152
+    peak = _measured_hbm_gbs()
+    gbs = (mon_bytes + io_bytes) / t / 1e9
+    out = {"metric": "turn-by-turn monitor write bandwidth (GB/s)", "value": gbs, "unit": "GB/s",
+           "higher_is_better": True, "n_gpus": 1, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": f"{n:.3g} protons, one-drift line, {turns} turns per call, "
+                                  "monitor of every particle (6 coordinates per turn)",
+                      "arith": args.arith, "particles": n, "turns_per_call": turns},
+           "seconds_per_call": t, "monitor_bytes_per_call": mon_bytes,
+           "particle_io_bytes_per_call": io_bytes,
+           "hbm_peak_gbs": peak, "frac": (gbs / peak) if peak else None,
+           "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy, read+write)" if peak else None}
+    print(json.dumps(out))
+
+
+def _measured_hbm_gbs():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        return float(json.load(open(p))["hbm_gbs"])
+    except Exception:
+        return None
 
 
 def run_toy_ring(args):
@@ -780,11 +858,13 @@ def main():
     ap.add_argument("--compact-every", dest="compact_every", type=int, default=None)
     ap.add_argument("--chunk-bytes", dest="chunk_bytes", type=int, default=None)
     ap.add_argument("--use-graph", dest="use_graph", type=int, default=None)
+    ap.add_argument("--monitor-turns", dest="monitor_turns", type=int, default=8,
+                    help="turns per call of the monitor_hbm workload")
     ap.add_argument("--monitor-first", dest="monitor_first", type=int, default=0,
                     help="record 6 coordinates per turn of the first N particles")
     ap.add_argument("--workload", default="thick_ring",
                     choices=["thick_ring", "da_screen", "turn_latency", "batch_scan", "toy_ring",
-                             "real_lattice"])
+                             "real_lattice", "monitor_hbm"])
     ap.add_argument("--lattice", default="sps", choices=sorted(REAL_LATTICES),
                     help="real_lattice workload: which fixture's line")
     ap.add_argument("--toy-particles", dest="toy_particles", type=int, default=10000)
@@ -817,6 +897,8 @@ def main():
                     help="physics: coordinates, tunes, orbit extremes and the ray's linear "
                          "aperture; all: plus the 32 multipole-error statistics")
     ap.add_argument("--da-weight-decay", dest="da_weight_decay", type=float, default=0.0)
+    ap.add_argument("--da-dump", dest="da_dump", default=None,
+                    help="write the DA scans' inputs and plain outcomes to this .npz")
     args = ap.parse_args()
     if args.workload == "da_screen":
         run_da_screen(args)
@@ -824,6 +906,8 @@ def main():
         run_turn_latency(args)
     elif args.workload == "batch_scan":
         run_batch_scan(args)
+    elif args.workload == "monitor_hbm":
+        run_monitor_hbm(args)
     elif args.workload == "toy_ring":
         run_toy_ring(args)
     elif args.workload == "real_lattice":
