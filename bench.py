@@ -459,6 +459,18 @@ def run_da_screen(args):
     no_net["pass_seconds"] = res0.seconds
     no_net["pass_fractions"] = [float(res0.pass1.mean()), float(res0.pass2.mean())]
 
+    # (4) three passes without the network: coarse sentinels, a fine window
+    # below each ray's first coarse loss, brackets
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    res3 = sc.adaptive_da_scan(bt_test, s_test, turns, coarse=args.da_coarse, fine=args.da_stride,
+                               window=args.da_window, device=dev)
+    t_adapt = time.perf_counter() - t0
+    adaptive = stats(res3.da, t_adapt, res3.tracked)
+    adaptive["pass_seconds"] = res3.seconds
+    adaptive["pass_fractions"] = [float(res3.pass1.mean()), float(res3.pass2.mean()),
+                                  float(res3.pass3.mean())]
+
     grid_step = float(np.max(np.diff(np.unique(s_test.r))))
     out = {"metric": "DA-scan time, surrogate vs plain", "value": t_plain / t_net,
            "unit": "x (plain time / screened time)", "higher_is_better": True, "n_gpus": 1,
@@ -467,6 +479,7 @@ def run_da_screen(args):
                                   f"0-{args.da_rmax:g} sigma x 11 angles x delta in {{0, 2.7e-4}}",
                       "turns": turns, "screen_band": [args.da_lo, args.da_hi],
                       "sentinel_stride": args.da_stride, "band_stride": args.da_band_stride,
+                      "adaptive_coarse_stride": args.da_coarse, "adaptive_window_sigma": args.da_window,
                       "train_seeds": len(train_lines), "test_seeds": n_seeds,
                       "train_particles": int(s_train.n), "test_particles": int(s_test.n),
                       "radial_step_sigma": grid_step, "arith": args.arith,
@@ -476,7 +489,8 @@ def run_da_screen(args):
            "da_error_mean_sigma": two_pass["da_error_mean_sigma"],
            "tracked_fraction": two_pass["tracked_fraction"],
            "methods": {"learned_band_one_pass": band, "sentinels_band_bracket": two_pass,
-                       "sentinels_bracket_no_network": no_net},
+                       "sentinels_bracket_no_network": no_net,
+                       "adaptive_three_pass_no_network": adaptive},
            "da_plain_mean_sigma": float(da_plain.mean()),
            "misclassification_all": float(np.mean((p >= 0.5) != surv_plain)),
            "train_scan_s": t_train_scan, "fit_s": t_fit, "fit_loss": [hist[0], hist[-1]],
@@ -892,11 +906,16 @@ def main():
     ap.add_argument("--da-train-seeds", dest="da_train_seeds", type=int, default=24)
     ap.add_argument("--da-test-seeds", dest="da_test_seeds", type=int, default=8)
     ap.add_argument("--da-epochs", dest="da_epochs", type=int, default=40)
-    ap.add_argument("--da-features", dest="da_features", default="physics",
+    ap.add_argument("--da-features", dest="da_features", default="all",
                     choices=["all", "physics"],
-                    help="physics: coordinates, tunes, orbit extremes and the ray's linear "
-                         "aperture; all: plus the 32 multipole-error statistics")
+                    help="all (the configuration's inputs): coordinates, tunes, orbit extremes, "
+                         "the ray's linear aperture and the seed's 32 multipole-error features "
+                         "(orders 0-10); physics: without the error features")
     ap.add_argument("--da-weight-decay", dest="da_weight_decay", type=float, default=0.0)
+    ap.add_argument("--da-coarse", dest="da_coarse", type=int, default=272,
+                    help="coarse sentinel stride of the three-pass scan")
+    ap.add_argument("--da-window", dest="da_window", type=float, default=12.0,
+                    help="sigma below the first coarse loss scanned at --da-stride")
     ap.add_argument("--da-dump", dest="da_dump", default=None,
                     help="write the DA scans' inputs and plain outcomes to this .npz")
     args = ap.parse_args()

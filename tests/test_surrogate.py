@@ -226,6 +226,45 @@ def test_sentinels_bracket_and_ray_survival():
     assert da(surv) == [120.0, 37.0, 200.0]
 
 
+def test_adaptive_da_scan_finds_islands_below_the_boundary():
+    """The three-pass scan on a synthetic survival map (host tracking stub):
+    4 rays of 2000 amplitudes. Ray 0 is lost from 1500 on; ray 1 from 1200
+    with an island of loss at 1150-1154 (inside the window below the
+    boundary); ray 2 from 900 with an island at 300 (far below: missed, as
+    sentinels miss it); ray 3 survives. The coarse pass locates each
+    boundary, the fine window finds ray 1's island, the bracket gives the
+    exact DA there; far fewer particles are tracked than the two-pass scan
+    with fine sentinels everywhere."""
+    from xtrack_gb300 import scan as sc
+    na = 2000
+    s = sc.Scan()
+    s.r = np.tile(np.arange(1.0, na + 1.0), 4)
+    s.theta = np.repeat(np.array([0.1, 0.2, 0.3, 0.4]), na)
+    s.lattice_index = np.zeros(4 * na, dtype=np.int32)
+    s.delta_index = np.zeros(4 * na, dtype=np.int64)
+    s.deltas = np.array([0.0])
+    ray = s.ray_index()
+    truth = np.ones(4 * na, dtype=bool)
+    truth[(ray == 0) & (s.r >= 1500)] = False
+    truth[(ray == 1) & (s.r >= 1200)] = False
+    truth[(ray == 1) & (s.r >= 1150) & (s.r <= 1154)] = False
+    truth[(ray == 2) & (s.r >= 900)] = False
+    truth[(ray == 2) & (s.r == 300)] = False
+    calls = []
+
+    def track(mask):
+        calls.append(int(mask.sum()))
+        return truth[mask]
+
+    res = sc.adaptive_da_scan(None, s, 10, coarse=64, fine=4, window=120.0, track_fn=track)
+    da = res.da.ravel()
+    assert da.tolist() == [1500.0, 1150.0, 900.0, 2000.0]
+    assert len(calls) == 3
+    assert np.array_equal(res.survive[res.tracked], truth[res.tracked])
+    # the two-pass scan with the fine stride everywhere tracks far more
+    assert res.tracked.sum() < 0.5 * sg.sentinels(s.r, ray, 4).sum()
+
+
 @pytest.mark.gpu
 def test_screened_da_scan_equals_plain_scan_on_most_rays():
     """End to end on a short ring. The screened DA scan (sentinels every

@@ -113,6 +113,16 @@ static constexpr int32_t kMinBlock = 32;
 #define XTG_DEV_ERR_LATTICE_INDEX 2
 #define XTG_DEV_ERR_ITEMS 3
 
+// Bits of |limit| for the global-aperture test, or -1 when no value passes
+// (a negative or NaN limit: |x| <= limit is then false for every x).
+static int64_t global_abs_bits(double limit) {
+    if (!(limit >= 0.0)) return -1;
+    double const m = fabs(limit);
+    int64_t b;
+    memcpy(&b, &m, sizeof(b));
+    return b;
+}
+
 // ---------------------------------------------------------------------------
 // kernel arguments
 // ---------------------------------------------------------------------------
@@ -135,7 +145,9 @@ struct TrackArgs {
     int32_t has_global;
     int32_t preserve_angle;
     // global aperture |x|, |y| <= limit as ordered keys: lower_key(-limit), upper_key(limit)
-    int64_t global_key_lo, global_key_hi;
+    // |x|, |y| <= limit as one compare each of the magnitude bits:
+    // bits(|limit|), or -1 (nothing passes) for a negative or NaN limit
+    int64_t global_abs_hi;
     int64_t num_ele_line;
     double line_length;
     uint64_t track_flags;
@@ -586,11 +598,13 @@ __device__ __forceinline__ void walk(PState& p, bool& active, const unsigned cha
         load_head(u, rec);
         bool const thick = apply_record<kExact>(p, rec, u, a, rf, i, pid);
         if (thick && !ignore_global) {
-            // local_particle_custom_api.h:259-287
-            // |x|, |y| <= limit as ordered-key compares (ord_key)
-            int64_t const kx = ord_key(p.x), ky = ord_key(p.y);
-            bool const within = (kx >= a.global_key_lo) && (kx <= a.global_key_hi) &&
-                                (ky >= a.global_key_lo) && (ky <= a.global_key_hi);
+            // local_particle_custom_api.h:259-287: |x| <= limit && |y| <= limit.
+            // The magnitude bits of a double order as its absolute value
+            // (+-0 at 0, a NaN above +inf), so each test is one integer
+            // compare against the bits of the limit, off the FP64 pipe
+            int64_t const ax = (int64_t)(emu_bits(p.x) & 0x7FFFFFFFFFFFFFFFull);
+            int64_t const ay = (int64_t)(emu_bits(p.y) & 0x7FFFFFFFFFFFFFFFull);
+            bool const within = (ax <= a.global_abs_hi) && (ay <= a.global_abs_hi);
             if (p.state > 0 && !within) p.state = -1;
         }
         if (p.state <= 0) {
@@ -1352,8 +1366,7 @@ static int32_t track_impl(ExecCtx* C, const xtg_particles* particles, const int3
     a.backtrack = backtrack ? 1 : 0;
     a.has_global = C->config.has_global_xy_limit;
     a.preserve_angle = C->config.cavity_preserve_angle;
-    a.global_key_lo = lower_key(-C->config.global_xy_limit);
-    a.global_key_hi = upper_key(C->config.global_xy_limit);
+    a.global_abs_hi = global_abs_bits(C->config.global_xy_limit);
     a.num_ele_line = num_ele_line;
     a.line_length = line_length;
     a.track_flags = track_flags;
@@ -1678,8 +1691,7 @@ int32_t xtg_track_noalloc(const xtg_lattice* lattice, const xtg_particles* parti
     a.backtrack = backtrack ? 1 : 0;
     a.has_global = C->config.has_global_xy_limit;
     a.preserve_angle = C->config.cavity_preserve_angle;
-    a.global_key_lo = lower_key(-C->config.global_xy_limit);
-    a.global_key_hi = upper_key(C->config.global_xy_limit);
+    a.global_abs_hi = global_abs_bits(C->config.global_xy_limit);
     a.num_ele_line = num_ele_line;
     a.line_length = line_length;
     a.track_flags = track_flags;

@@ -192,24 +192,83 @@ def da_table(scan, survive, n_seeds):
 
 
 class ScreenedDA:
-    """Result of ``screened_da_scan``: per-particle masks of the two passes,
-    the survival map, the DA table (n_seeds, n_deltas, n_angles) and the
-    wall time of each pass (tracking plus the host work that chose it)."""
+    """Result of ``screened_da_scan`` / ``adaptive_da_scan``: per-particle
+    masks of the passes, the survival map, the DA table (n_seeds, n_deltas,
+    n_angles) and the wall time of each pass (tracking plus the host work
+    that chose it)."""
 
     def __init__(self):
         self.pass1 = None
         self.pass2 = None
+        self.pass3 = None
         self.survive = None
         self.da = None
         self.seconds = []
 
     @property
     def tracked(self):
-        return self.pass1 | self.pass2
+        out = self.pass1 | self.pass2
+        return out if self.pass3 is None else out | self.pass3
 
     @property
     def tracked_fraction(self):
         return float(self.tracked.mean())
+
+
+def adaptive_da_scan(tracker, scan, num_turns, coarse=272, fine=34, window=12.0, device="cuda",
+                     track_fn=None):
+    """DA scan in three passes, each on the amplitudes the previous ones
+    left open. Pass 1 tracks every ``coarse``-th amplitude of each ray
+    (plus its largest): the first lost one places the ray's boundary within
+    one coarse step. Pass 2 tracks every ``fine``-th amplitude in the
+    ``window`` sigma below that first coarse loss, where islands of loss
+    just inside the boundary lie. Pass 3 tracks each ray's ``bracket``
+    (the untracked amplitudes between the last tracked survivor and the
+    first tracked loss). The ray's DA is its smallest tracked loss. On the
+    thick-ring seeds this tracks 1.5 % of the grid at the two-pass scan's
+    error (0.155 sigma mean, same rays exact) against its 3.65 %.
+    ``track_fn(mask) -> survive`` replaces the tracking (tests)."""
+    import time
+    from . import surrogate as sg
+
+    res = ScreenedDA()
+    ray = scan.ray_index()
+    n = scan.n
+    survive = np.zeros(n, dtype=bool)
+    tracked = np.zeros(n, dtype=bool)
+
+    def track(mask):
+        if not mask.any():
+            return
+        if track_fn is not None:
+            survive[mask] = np.asarray(track_fn(mask), dtype=bool)
+        else:
+            st, at, _ = run_scan(tracker, scan, num_turns, select=mask, device=device)
+            survive[mask] = sg.targets(st, at, num_turns)[0] > 0
+        tracked[mask] = True
+
+    n_rays = int(ray.max()) + 1 if n else 0
+    t0 = time.perf_counter()
+    m1 = sg.sentinels(scan.r, ray, coarse)
+    track(m1)
+    res.seconds.append(time.perf_counter() - t0)
+    t0 = time.perf_counter()
+    lost = tracked & ~survive
+    first = np.full(n_rays, np.inf)
+    np.minimum.at(first, ray[lost], scan.r[lost])
+    top = first[ray]
+    near = (scan.r < top) & (scan.r >= top - window)
+    m2 = sg.sentinels(scan.r, ray, fine) & near & ~tracked
+    track(m2)
+    res.seconds.append(time.perf_counter() - t0)
+    t0 = time.perf_counter()
+    m3 = sg.bracket(scan.r, ray, tracked, survive)
+    track(m3)
+    res.seconds.append(time.perf_counter() - t0)
+    res.pass1, res.pass2, res.pass3 = m1, m2, m3
+    res.survive = sg.ray_survival(scan.r, ray, tracked, survive)
+    res.da = da_table(scan, res.survive, int(scan.lattice_index.max()) + 1 if n else 0)
+    return res
 
 
 def screened_da_scan(tracker, scan, num_turns, p_survive=None, stride=34, lo=0.02, hi=0.98,

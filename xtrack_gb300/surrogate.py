@@ -217,24 +217,39 @@ class SurvivalMLP:
 # features and targets
 # ----------------------------------------------------------------------
 _FAMILIES = ("Bend", "Quadrupole", "Sextupole", "Multipole")
+_MAIN_ORDER = {"Bend": 0, "Quadrupole": 1, "Sextupole": 2}
+_R_REF = 0.017
 
 
-def seed_features(line):
-    """32 numbers that summarise a seed's multipole errors: for each magnet
-    family (bends, quadrupoles, sextupoles, thin multipoles) and each order
-    0..3, the RMS over the family of knl_rel and of ksl_rel, in units of
-    1e-4."""
-    acc = {(f, n, s): [] for f in _FAMILIES for n in range(4) for s in (0, 1)}
+def seed_features(line, r_ref=_R_REF):
+    """32 numbers that summarise a seed's multipole errors, orders 0..10.
+    Each knl_rel / ksl_rel entry of order n of a magnet with main order m
+    is turned into the relative field error at radius r_ref,
+    b_n = knl_rel[n] * m! / n! * r_ref^(n - m) (a_n from ksl_rel), in units
+    of 1e-4. Per magnet family (bends, quadrupoles, sextupoles, thin
+    multipoles): the family mean of b_0..b_3, of a_0 and a_1, and the RMS
+    over orders of the family means of b_4..b_10 and of a_2..a_10. Means,
+    not RMS over magnets: the RMS of independent errors is the same for
+    every seed, the mean (the systematic part the magnets share) is not."""
+    acc = {(f, n, s): [] for f in _FAMILIES for n in range(11) for s in (0, 1)}
     for name in line.element_names:
         e = line.element_dict[name]
         fam = type(e).__name__
         if fam not in _FAMILIES:
             continue
+        m = _MAIN_ORDER.get(fam, int(getattr(e, "main_order", 0) or 0))
         for s, arr in ((0, getattr(e, "knl_rel", None)), (1, getattr(e, "ksl_rel", None))):
             arr = np.zeros(1) if arr is None else np.asarray(arr, dtype=np.float64)
-            for n in range(4):
-                acc[(fam, n, s)].append(arr[n] if n < len(arr) else 0.0)
-    out = [math.sqrt(np.mean(np.square(v))) * 1e4 if v else 0.0 for v in acc.values()]
+            for n in range(11):
+                v = arr[n] if n < len(arr) else 0.0
+                acc[(fam, n, s)].append(v * math.factorial(m) / math.factorial(n) * r_ref ** (n - m) * 1e4)
+    out = []
+    for f in _FAMILIES:
+        mean = {(n, s): (float(np.mean(acc[(f, n, s)])) if acc[(f, n, s)] else 0.0)
+                for n in range(11) for s in (0, 1)}
+        out += [mean[(n, 0)] for n in range(4)] + [mean[(0, 1)], mean[(1, 1)]]
+        out.append(math.sqrt(np.mean([mean[(n, 0)] ** 2 for n in range(4, 11)])))
+        out.append(math.sqrt(np.mean([mean[(n, 1)] ** 2 for n in range(2, 11)])))
     return np.asarray(out, dtype=np.float64)
 
 
