@@ -113,14 +113,14 @@ static constexpr int32_t kMinBlock = 32;
 #define XTG_DEV_ERR_LATTICE_INDEX 2
 #define XTG_DEV_ERR_ITEMS 3
 
-// Bits of |limit| for the global-aperture test, or -1 when no value passes
-// (a negative or NaN limit: |x| <= limit is then false for every x).
-static int64_t global_abs_bits(double limit) {
-    if (!(limit >= 0.0)) return -1;
-    double const m = fabs(limit);
-    int64_t b;
-    memcpy(&b, &m, sizeof(b));
-    return b;
+// The bit pattern of |limit| shifted left by one (the sign bit dropped) for
+// the global-aperture test; a negative or NaN limit, for which |x| <= limit
+// holds for no x, is flagged by global_none instead.
+static uint64_t global_abs2(double limit) {
+    if (!(limit >= 0.0)) return 0;
+    uint64_t b;
+    memcpy(&b, &limit, sizeof(b));
+    return b << 1;
 }
 
 // ---------------------------------------------------------------------------
@@ -145,9 +145,11 @@ struct TrackArgs {
     int32_t has_global;
     int32_t preserve_angle;
     // global aperture |x|, |y| <= limit as ordered keys: lower_key(-limit), upper_key(limit)
-    // |x|, |y| <= limit as one compare each of the magnitude bits:
-    // bits(|limit|), or -1 (nothing passes) for a negative or NaN limit
-    int64_t global_abs_hi;
+    // |x|, |y| <= limit as one unsigned compare each of the bit patterns
+    // shifted left by one (global_abs2); global_none: nothing passes
+    uint64_t global_abs2;
+    int32_t global_none;
+    int32_t reserved_global;
     int64_t num_ele_line;
     double line_length;
     uint64_t track_flags;
@@ -599,12 +601,13 @@ __device__ __forceinline__ void walk(PState& p, bool& active, const unsigned cha
         bool const thick = apply_record<kExact>(p, rec, u, a, rf, i, pid);
         if (thick && !ignore_global) {
             // local_particle_custom_api.h:259-287: |x| <= limit && |y| <= limit.
-            // The magnitude bits of a double order as its absolute value
-            // (+-0 at 0, a NaN above +inf), so each test is one integer
-            // compare against the bits of the limit, off the FP64 pipe
-            int64_t const ax = (int64_t)(emu_bits(p.x) & 0x7FFFFFFFFFFFFFFFull);
-            int64_t const ay = (int64_t)(emu_bits(p.y) & 0x7FFFFFFFFFFFFFFFull);
-            bool const within = (ax <= a.global_abs_hi) && (ay <= a.global_abs_hi);
+            // A double's bit pattern shifted left by one drops the sign and
+            // orders as its absolute value (+-0 at 0, a NaN above +inf), so
+            // each test is one unsigned integer compare, off the FP64 pipe.
+            // (Masking the sign bit instead lets the compiler turn the mask
+            // into an FP64 absolute value, which keeps a NaN's sign.)
+            uint64_t const ax = emu_bits(p.x) << 1, ay = emu_bits(p.y) << 1;
+            bool const within = !a.global_none && (ax <= a.global_abs2) && (ay <= a.global_abs2);
             if (p.state > 0 && !within) p.state = -1;
         }
         if (p.state <= 0) {
@@ -1366,7 +1369,8 @@ static int32_t track_impl(ExecCtx* C, const xtg_particles* particles, const int3
     a.backtrack = backtrack ? 1 : 0;
     a.has_global = C->config.has_global_xy_limit;
     a.preserve_angle = C->config.cavity_preserve_angle;
-    a.global_abs_hi = global_abs_bits(C->config.global_xy_limit);
+    a.global_abs2 = global_abs2(C->config.global_xy_limit);
+    a.global_none = !(C->config.global_xy_limit >= 0.0);
     a.num_ele_line = num_ele_line;
     a.line_length = line_length;
     a.track_flags = track_flags;
@@ -1691,7 +1695,8 @@ int32_t xtg_track_noalloc(const xtg_lattice* lattice, const xtg_particles* parti
     a.backtrack = backtrack ? 1 : 0;
     a.has_global = C->config.has_global_xy_limit;
     a.preserve_angle = C->config.cavity_preserve_angle;
-    a.global_abs_hi = global_abs_bits(C->config.global_xy_limit);
+    a.global_abs2 = global_abs2(C->config.global_xy_limit);
+    a.global_none = !(C->config.global_xy_limit >= 0.0);
     a.num_ele_line = num_ele_line;
     a.line_length = line_length;
     a.track_flags = track_flags;
