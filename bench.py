@@ -333,13 +333,20 @@ def run_da_screen(args):
     amplitudes up to --da-rmax sigma) with all seeds in one persistent
     launch. A survival MLP is trained with the library's kernels on the
     training seeds' outcomes (features: coordinates, the seed's tunes,
-    closed-orbit extremes and the ray's linear aperture). The test seeds are
-    then scanned plainly (every particle tracked) and screened three ways:
-    the network's uncertain band alone (one pass); sentinels every
+    closed-orbit extremes, the ray's linear aperture and, by default, the
+    seed's 32 multipole-error features). The test seeds are then scanned
+    plainly (every particle tracked) and screened six ways: (1) the
+    network's uncertain band alone (one pass); (2) sentinels every
     --da-stride amplitudes plus that band, then each ray's bracket (two
-    passes); the same two passes without the network. value = plain time /
-    time of the two-pass scan with the network. The DA error per ray (sigma)
-    judges each screened result against the plain one."""
+    passes); (3) the same two passes without the network; (4) three passes
+    without the network (coarse sentinels every --da-coarse amplitudes, a
+    fine window below the first coarse loss, brackets); (5) two passes with
+    the fine window placed by the network around its predicted boundary;
+    (6) the same two passes without the network (coarse sentinels, brackets
+    of one coarse step). value = plain time / time of (2). The DA error per
+    ray (sigma) judges each screened result against the plain one; the
+    network's own DA per ray (its predicted boundary) is reported beside
+    them."""
     import torch
     from xtrack_gb300 import scan as sc
     from xtrack_gb300 import surrogate as sg
@@ -471,6 +478,34 @@ def run_da_screen(args):
     adaptive["pass_fractions"] = [float(res3.pass1.mean()), float(res3.pass2.mean()),
                                   float(res3.pass3.mean())]
 
+    # (5) two passes with the fine window placed by the network: coarse
+    # sentinels + fine sentinels around the predicted boundary, brackets
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    p = predict()
+    res5 = sc.guided_da_scan(bt_test, s_test, turns, p, coarse=args.da_coarse, fine=args.da_stride,
+                             below=args.da_guide_below, above=args.da_guide_above, device=dev)
+    t_guided = time.perf_counter() - t0
+    guided = stats(res5.da, t_guided, res5.tracked)
+    guided["pass_seconds"] = res5.seconds
+    guided["pass_fractions"] = [float(res5.pass1.mean()), float(res5.pass2.mean())]
+
+    # (6) the same two passes without the network: coarse sentinels, then
+    # brackets of one coarse step
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    res6 = sc.guided_da_scan(bt_test, s_test, turns, np.ones(s_test.n), coarse=args.da_coarse,
+                             fine=args.da_stride, below=0.0, above=-1.0, device=dev)
+    t_blind = time.perf_counter() - t0
+    blind = stats(res6.da, t_blind, res6.tracked)
+    blind["pass_seconds"] = res6.seconds
+    blind["pass_fractions"] = [float(res6.pass1.mean()), float(res6.pass2.mean())]
+
+    # the network's own DA per ray (its predicted boundary) against plain tracking
+    pred = sc.predicted_boundary(p, s_test)
+    da_net = sc.da_table(s_test, s_test.r < pred, n_seeds)
+    net_err = np.abs(da_net - da_plain)
+
     grid_step = float(np.max(np.diff(np.unique(s_test.r))))
     out = {"metric": "DA-scan time, surrogate vs plain", "value": t_plain / t_net,
            "unit": "x (plain time / screened time)", "higher_is_better": True, "n_gpus": 1,
@@ -480,6 +515,7 @@ def run_da_screen(args):
                       "turns": turns, "screen_band": [args.da_lo, args.da_hi],
                       "sentinel_stride": args.da_stride, "band_stride": args.da_band_stride,
                       "adaptive_coarse_stride": args.da_coarse, "adaptive_window_sigma": args.da_window,
+                      "guided_window_sigma": [args.da_guide_below, args.da_guide_above],
                       "train_seeds": len(train_lines), "test_seeds": n_seeds,
                       "train_particles": int(s_train.n), "test_particles": int(s_test.n),
                       "radial_step_sigma": grid_step, "arith": args.arith,
@@ -490,7 +526,12 @@ def run_da_screen(args):
            "tracked_fraction": two_pass["tracked_fraction"],
            "methods": {"learned_band_one_pass": band, "sentinels_band_bracket": two_pass,
                        "sentinels_bracket_no_network": no_net,
-                       "adaptive_three_pass_no_network": adaptive},
+                       "adaptive_three_pass_no_network": adaptive,
+                       "guided_two_pass": guided, "coarse_bracket_two_pass_no_network": blind},
+           "network_da_error_mean_sigma": float(net_err.mean()),
+           "network_da_error_median_sigma": float(np.median(net_err)),
+           "network_da_within_window": float(np.mean((da_net - da_plain <= args.da_guide_below)
+                                                     & (da_plain - da_net <= args.da_guide_above))),
            "da_plain_mean_sigma": float(da_plain.mean()),
            "misclassification_all": float(np.mean((p >= 0.5) != surv_plain)),
            "train_scan_s": t_train_scan, "fit_s": t_fit, "fit_loss": [hist[0], hist[-1]],
@@ -633,6 +674,118 @@ def run_monitor_hbm(args):
            "particle_io_bytes_per_call": io_bytes,
            "hbm_peak_gbs": peak, "frac": (gbs / peak) if peak else None,
            "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy, read+write)" if peak else None}
+    print(json.dumps(out))
+
+
+def run_mlp(args):
+    """The surrogate's tensor-core contraction (tcgen05, TMA-staged BF16
+    operands, FP32 accumulation in tensor memory): the forward product of
+    one hidden layer, X[M, 256] W[256, 256]^T + b -> GELU, at M =
+    --mlp-rows (2^20) rows, storing the BF16 activation only (the inference layer) and the
+    FP32 pre-activation as well (the training layer); then one training
+    step (forward, loss, backward, Adam) of the DA network at batch 4096
+    and inference over 2^20 samples. Each timing is the best of --steps
+    CUDA-event runs after --warmup. The layer moves 2*M*256*(2 + out) bytes
+    against 2*M*256*256 FLOPs, so at this width the product is bound by
+    HBM: the line reports both fractions against the measured peaks."""
+    import ctypes
+
+    import torch
+    from xtrack_gb300 import _abi
+    from xtrack_gb300 import surrogate as sg
+
+    rank, world, local = _dist()
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    lib = _abi.load_library()
+    M, K, N = args.mlp_rows, 256, 256
+    g = torch.Generator(device="cpu").manual_seed(3)
+    X = torch.randn(M, K, generator=g).to(torch.bfloat16).to(dev)
+    W = (torch.randn(N, K, generator=g) / 16).to(torch.bfloat16).to(dev)
+    b = torch.randn(N, generator=g).to(dev)
+    Z = torch.empty(M, N, device=dev)
+    Y = torch.empty(M, N, dtype=torch.bfloat16, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    st = ctypes.c_void_p(stream.cuda_stream)
+
+    def best(fn):
+        for _ in range(args.warmup):
+            fn()
+        ts = []
+        for _ in range(args.steps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize(dev)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            ts.append(e0.elapsed_time(e1) * 1e-3)
+        return min(ts)
+
+    def layer(store_z):
+        _abi.check_mlp(lib.xtg_mlp_gemm(sg._ptr(X), K, 1, sg._ptr(W), K, 1, M, N, K, sg._ptr(b),
+                                        _abi.MLP_ACT_GELU, sg._ptr(Z) if store_z else None, N,
+                                        sg._ptr(Y), N, None, 0, 0, st), lib)
+
+    flops = 2.0 * M * N * K
+    t_y = best(lambda: layer(False))
+    t_zy = best(lambda: layer(True))
+    bytes_y = M * K * 2 + N * K * 2 + M * N * 2
+    bytes_zy = bytes_y + M * N * 4
+    ref = torch.nn.functional.gelu(X[:4096].float() @ W.float().t() + b)
+    layer(False)
+    torch.cuda.synchronize(dev)
+    err = float((Y[:4096].float() - ref).abs().max() / ref.abs().max())
+
+    net = sg.SurvivalMLP(n_in=sg.N_DA_FEATURES + sg.N_SEED_FEATURES, seed=0, device=dev)
+    rng = np.random.default_rng(1)
+    Xs = rng.normal(size=(1 << 20, net.n_in)).astype(np.float32)
+    net.set_normalisation(Xs)
+    X16 = net.prepare_input(Xs)
+    xb = X16[:4096].contiguous()
+    sv = torch.from_numpy((rng.random(4096) < 0.5).astype(np.float32)).to(dev)
+    lt = torch.from_numpy(rng.random(4096).astype(np.float32)).to(dev)
+
+    def train_step():
+        out = net.forward(xb, keep=True)
+        _, dout, dout16 = net.loss_and_grad(out, sv, lt)
+        net.backward(dout, dout16)
+        net.adam_step(lr=1e-4)
+
+    t_step = best(train_step)
+    t_inf = best(lambda: net.forward(X16))
+    _abi.check_mlp(lib.xtg_mlp_device_status(), lib)
+    dims = net.dims
+    flops_sample = 2.0 * sum(a * b_ for a, b_ in zip(dims[:-1], dims[1:]))
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    tf_peak = peaks.get("bf16_tflops")
+    hbm = peaks.get("hbm_gbs")
+    tf = flops / t_y / 1e12
+    gbs_y = bytes_y / t_y / 1e9
+    gbs_zy = bytes_zy / t_zy / 1e9
+    out = {"metric": "surrogate contraction throughput (tcgen05, bf16 x bf16 -> f32)",
+           "value": tf, "unit": "TFLOP/s", "higher_is_better": True, "n_gpus": 1,
+           "dtype": "bf16", "data": "synthetic",
+           "config": {"workload": f"hidden layer X[{M}, {K}] W[{N}, {K}]^T + b, GELU, bf16 store; "
+                                  f"DA network {dims} training step at batch 4096 and inference "
+                                  f"over {1 << 20} samples"},
+           "layer_seconds": {"bf16_store": t_y, "f32_and_bf16_store": t_zy},
+           "layer_gbs": {"bf16_store": gbs_y, "f32_and_bf16_store": gbs_zy},
+           "roofline": {"bound": "hbm", "achieved": gbs_y, "peak": hbm, "unit": "GB/s",
+                        "frac": (gbs_y / hbm) if hbm else None,
+                        "tensor_frac": (tf / tf_peak) if tf_peak else None,
+                        "peak_source": "MEASURED_PEAKS.json (hbm_gbs, bf16_tflops)"},
+           "rel_error_vs_torch_fp32": err,
+           "train_step_ms": t_step * 1e3,
+           "inference_samples_per_s": (1 << 20) / t_inf,
+           "inference_tflops": flops_sample * (1 << 20) / t_inf / 1e12}
     print(json.dumps(out))
 
 
@@ -878,7 +1031,7 @@ def main():
                     help="record 6 coordinates per turn of the first N particles")
     ap.add_argument("--workload", default="thick_ring",
                     choices=["thick_ring", "da_screen", "turn_latency", "batch_scan", "toy_ring",
-                             "real_lattice", "monitor_hbm"])
+                             "real_lattice", "monitor_hbm", "mlp"])
     ap.add_argument("--lattice", default="sps", choices=sorted(REAL_LATTICES),
                     help="real_lattice workload: which fixture's line")
     ap.add_argument("--toy-particles", dest="toy_particles", type=int, default=10000)
@@ -916,6 +1069,12 @@ def main():
                     help="coarse sentinel stride of the three-pass scan")
     ap.add_argument("--da-window", dest="da_window", type=float, default=12.0,
                     help="sigma below the first coarse loss scanned at --da-stride")
+    ap.add_argument("--mlp-rows", dest="mlp_rows", type=int, default=1 << 20,
+                    help="rows of the mlp workload's layer product")
+    ap.add_argument("--da-guide-below", dest="da_guide_below", type=float, default=6.0,
+                    help="sigma below the network's predicted boundary scanned at --da-stride")
+    ap.add_argument("--da-guide-above", dest="da_guide_above", type=float, default=2.0,
+                    help="sigma above the network's predicted boundary scanned at --da-stride")
     ap.add_argument("--da-dump", dest="da_dump", default=None,
                     help="write the DA scans' inputs and plain outcomes to this .npz")
     args = ap.parse_args()
@@ -925,6 +1084,8 @@ def main():
         run_turn_latency(args)
     elif args.workload == "batch_scan":
         run_batch_scan(args)
+    elif args.workload == "mlp":
+        run_mlp(args)
     elif args.workload == "monitor_hbm":
         run_monitor_hbm(args)
     elif args.workload == "toy_ring":

@@ -452,7 +452,10 @@ int32_t xtg_check_bounded_wait(int64_t limit_cycles);
 
 /* Tensor-core contraction R[m, n] = sum_k A(m, k) B(n, k), with A(m, k) at
  * A[m*a_sm + k*a_sk] and B(n, k) at B[n*b_sn + k*b_sk] (bf16, any strides),
- * FP32 accumulation. Epilogue: z = R + bias[n] (bias may be NULL);
+ * FP32 accumulation in tensor memory (tcgen05). Operands with a unit stride
+ * along k or along their rows, a 16-byte aligned base and a pitch that is a
+ * multiple of 8 elements are staged by TMA; others by the threads (same
+ * results). Epilogue: z = R + bias[n] (bias may be NULL);
  * Z[m*z_ld + n] = z (fp32, optional); Y[m*y_ld + n] = act(z) (bf16,
  * optional); C[m*c_ld + n] = z, or += z with c_accumulate (fp32, optional). */
 int32_t xtg_mlp_gemm(const void* A, int64_t a_sm, int64_t a_sk, const void* B,
@@ -469,13 +472,15 @@ int32_t xtg_mlp_act_backward(const float* dY, const float* Z, int64_t n, int32_t
 int32_t xtg_mlp_colsum(const float* X, int64_t M, int32_t N, int64_t ld, float* out,
                        int32_t accumulate, void* stream);
 
-/* Loss of the two network outputs per sample (out[m*2+0]: logit of
- * P(survive), out[m*2+1]: normalised log loss turn): binary cross-entropy
+/* Loss of the two network outputs per sample (out[m*ld+0]: logit of
+ * P(survive), out[m*ld+1]: normalised log loss turn; ld >= 2, the other
+ * columns of a padded output layer are not read): binary cross-entropy
  * plus w_turn * squared error on the loss turn of lost samples. Writes
- * dLoss/dout / M (fp32 and bf16) and the per-sample loss. */
-int32_t xtg_mlp_loss(const float* out, const float* survive, const float* logturn,
-                     int64_t M, float w_turn, float* dout, void* dout16, float* loss,
-                     void* stream);
+ * dLoss/dout / M (fp32 and bf16) into columns 0 and 1 of dout / dout16
+ * (row pitch ld) and the per-sample loss. */
+int32_t xtg_mlp_loss(const float* out, int64_t ld, const float* survive,
+                     const float* logturn, int64_t M, float w_turn, float* dout,
+                     void* dout16, float* loss, void* stream);
 
 /* One Adam step (bias-corrected, decoupled weight decay) on fp32 master
  * weights w; refreshes the bf16 copy w16 when not NULL. step >= 1. */
@@ -485,6 +490,11 @@ int32_t xtg_mlp_adam(float* w, void* w16, const float* grad, float* m1, float* m
 
 /* y = bf16(x) over n elements. */
 int32_t xtg_mlp_to_bf16(const float* x, int64_t n, void* y, void* stream);
+
+/* Waits for the device, then reads and clears the xtg_mlp kernels' device
+ * error word: XTG_E_TIMEOUT when a bounded wait inside one of them gave up
+ * (that kernel's outputs were not written), else XTG_OK. */
+int32_t xtg_mlp_device_status(void);
 
 /* Message of the last failed xtg_mlp_* call of this thread. */
 int32_t xtg_mlp_get_last_error(char* buf, int64_t n);

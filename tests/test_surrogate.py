@@ -45,38 +45,68 @@ def _bf(x):
     return x.to(torch.bfloat16)
 
 
-@pytest.mark.gpu
-@pytest.mark.parametrize("M,N,K", [(37, 70, 38), (256, 256, 256), (1000, 2, 256), (64, 256, 1)])
-@pytest.mark.parametrize("transpose", [False, True])
-def test_gemm_matches_torch(M, N, K, transpose):
+def _gemm(A, a_sm, a_sk, B, b_sn, b_sk, M, N, K, bias):
     import torch
     from xtrack_gb300 import _abi
     lib = _abi.load_library()
-    g = torch.Generator().manual_seed(M * 7 + N)
-    A = _bf(torch.randn(M, K, generator=g)).cuda()
-    B = _bf(torch.randn(N, K, generator=g)).cuda()
-    bias = torch.randn(N, generator=g).cuda()
-    if transpose:
-        At = A.t().contiguous()      # (k, m) storage
-        Bt = B.t().contiguous()
-        a = (At, 1, M)
-        b = (Bt, 1, N)
-    else:
-        a = (A, K, 1)
-        b = (B, K, 1)
     Z = torch.empty(M, N, device="cuda")
     Y = torch.empty(M, N, dtype=torch.bfloat16, device="cuda")
     C = torch.ones(M, N, device="cuda")
-    st = _abi.check_mlp(lib.xtg_mlp_gemm(
-        sg._ptr(a[0]), a[1], a[2], sg._ptr(b[0]), b[1], b[2], M, N, K, sg._ptr(bias),
-        _abi.MLP_ACT_GELU, sg._ptr(Z), N, sg._ptr(Y), N, sg._ptr(C), N, 1, None))
+    _abi.check_mlp(lib.xtg_mlp_gemm(
+        sg._ptr(A), a_sm, a_sk, sg._ptr(B), b_sn, b_sk, M, N, K, sg._ptr(bias),
+        _abi.MLP_ACT_GELU, sg._ptr(Z), N, sg._ptr(Y), N, sg._ptr(C), N, 1, None), lib)
     torch.cuda.synchronize()
+    _abi.check_mlp(lib.xtg_mlp_device_status(), lib)
+    return Z, Y, C
+
+
+def _stored(X, transpose, extra):
+    """X (rows, k) stored k-contiguous (transpose False) or row-contiguous,
+    with `extra` unused elements after each line; returns (tensor, s_row, s_k)."""
+    import torch
+    rows, k = X.shape
+    if not transpose:
+        buf = torch.zeros(rows, k + extra, dtype=X.dtype, device=X.device)
+        buf[:, :k] = X
+        return buf, k + extra, 1
+    buf = torch.zeros(k, rows + extra, dtype=X.dtype, device=X.device)
+    buf[:, :rows] = X.t()
+    return buf, 1, rows + extra
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("M,N,K", [(37, 70, 38), (256, 256, 256), (1000, 2, 256), (64, 256, 1),
+                                   (264, 136, 200), (128, 520, 64), (256, 40, 4096),
+                                   (4096, 256, 256)])
+@pytest.mark.parametrize("transpose", [False, True])
+def test_gemm_matches_torch(M, N, K, transpose):
+    """The tcgen05 contraction against a torch fp32 product of the same
+    bf16 operands, for operands stored k-contiguous (the forward product)
+    and row-contiguous (the backward products' transposed operands), with
+    ragged M, N and K, several N tiles and a long K. Each case runs twice:
+    with line pitches that are multiples of 8 elements (TMA staging where
+    the sizes allow it) and with pitches one element longer (staged by the
+    threads); the two must agree bit for bit."""
+    import torch
+    g = torch.Generator().manual_seed(M * 7 + N + K)
+    A = _bf(torch.randn(M, K, generator=g)).cuda()
+    B = _bf(torch.randn(N, K, generator=g)).cuda()
+    bias = torch.randn(N, generator=g).cuda()
     ref = A.float() @ B.float().t() + bias
     tol = 1e-4 * math.sqrt(K) * float(ref.abs().max())
-    assert float((Z - ref).abs().max()) <= tol
-    assert float((C - (ref + 1)).abs().max()) <= tol
     gelu = torch.nn.functional.gelu(ref)
-    assert float((Y.float() - gelu).abs().max()) <= 1e-2 * float(gelu.abs().max()) + tol
+    outs = []
+    for extra in (0, 1):
+        pad = 0 if extra == 0 else 1
+        a, a_sm, a_sk = _stored(A, transpose, pad)
+        b, b_sn, b_sk = _stored(B, transpose, pad)
+        Z, Y, C = _gemm(a, a_sm, a_sk, b, b_sn, b_sk, M, N, K, bias)
+        assert float((Z - ref).abs().max()) <= tol
+        assert float((C - (ref + 1)).abs().max()) <= tol
+        assert float((Y.float() - gelu).abs().max()) <= 1e-2 * float(gelu.abs().max()) + tol
+        outs.append((Z, Y, C))
+    for x0, x1 in zip(*outs):
+        assert torch.equal(x0, x1)
 
 
 @pytest.mark.gpu
@@ -263,6 +293,56 @@ def test_adaptive_da_scan_finds_islands_below_the_boundary():
     assert np.array_equal(res.survive[res.tracked], truth[res.tracked])
     # the two-pass scan with the fine stride everywhere tracks far more
     assert res.tracked.sum() < 0.5 * sg.sentinels(s.r, ray, 4).sum()
+
+
+def test_guided_da_scan_places_the_window_by_the_network():
+    """The network-guided two-pass scan on the synthetic survival map of
+    the three-pass test (host tracking stub). The network's boundary is
+    right on rays 0 and 1, 300 amplitudes too high on ray 2 and absent on
+    ray 3 (survives). Pass 1 (coarse sentinels + fine window at the
+    predicted boundary) and pass 2 (brackets) give the three-pass scan's
+    DA on every ray in one pass fewer; without the network the same two
+    passes (coarse sentinels, then brackets of one coarse step) track
+    more particles (here 1.3x: one of the three rays with a boundary was
+    mispredicted and its bracket spans a coarse step)."""
+    from xtrack_gb300 import scan as sc
+    na = 2000
+    s = sc.Scan()
+    s.r = np.tile(np.arange(1.0, na + 1.0), 4)
+    s.theta = np.repeat(np.array([0.1, 0.2, 0.3, 0.4]), na)
+    s.lattice_index = np.zeros(4 * na, dtype=np.int32)
+    s.delta_index = np.zeros(4 * na, dtype=np.int64)
+    s.deltas = np.array([0.0])
+    ray = s.ray_index()
+    truth = np.ones(4 * na, dtype=bool)
+    truth[(ray == 0) & (s.r >= 1500)] = False
+    truth[(ray == 1) & (s.r >= 1200)] = False
+    truth[(ray == 1) & (s.r >= 1150) & (s.r <= 1154)] = False
+    truth[(ray == 2) & (s.r >= 900)] = False
+    truth[(ray == 2) & (s.r == 300)] = False
+    boundary = np.array([1500.0, 1160.0, 1200.0, np.inf])[ray]
+    p = np.where(s.r < boundary, 0.9, 0.1)
+    pred = sc.predicted_boundary(p, s)
+    assert pred.reshape(4, na)[:, 0].tolist() == [1500.0, 1160.0, 1200.0, 2000.0]
+    calls = []
+
+    def track(mask):
+        calls.append(int(mask.sum()))
+        return truth[mask]
+
+    res = sc.guided_da_scan(None, s, 10, p, coarse=128, fine=4, below=120.0, above=40.0,
+                            track_fn=track)
+    assert res.da.ravel().tolist() == [1500.0, 1150.0, 900.0, 2000.0]
+    assert len(calls) == 2
+    assert np.array_equal(res.survive[res.tracked], truth[res.tracked])
+    adaptive = sc.adaptive_da_scan(None, s, 10, coarse=128, fine=4, window=120.0,
+                                   track_fn=lambda m: truth[m])
+    assert np.array_equal(res.da, adaptive.da)
+    # the same two passes without the network: coarse sentinels, brackets
+    blind = np.zeros(4 * na) + 1.0
+    res0 = sc.guided_da_scan(None, s, 10, blind, coarse=128, fine=4, below=0.0, above=-1.0,
+                             track_fn=lambda m: truth[m])
+    assert res.tracked.sum() < 0.8 * res0.tracked.sum()
 
 
 @pytest.mark.gpu

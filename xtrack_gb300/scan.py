@@ -271,6 +271,71 @@ def adaptive_da_scan(tracker, scan, num_turns, coarse=272, fine=34, window=12.0,
     return res
 
 
+def predicted_boundary(p_survive, scan, threshold=0.5):
+    """Per particle: its ray's smallest amplitude at which the network's
+    P(survive) falls below ``threshold`` (the network's DA of the ray), or
+    the ray's largest amplitude when it never does."""
+    p = np.asarray(p_survive)
+    ray = scan.ray_index()
+    n_rays = int(ray.max()) + 1 if scan.n else 0
+    top = np.full(n_rays, -np.inf)
+    np.maximum.at(top, ray, scan.r)
+    pred = top.copy()
+    lost = p < threshold
+    np.minimum.at(pred, ray[lost], scan.r[lost])
+    return pred[ray]
+
+
+def guided_da_scan(tracker, scan, num_turns, p_survive, coarse=272, fine=34, below=6.0, above=2.0,
+                   device="cuda", track_fn=None):
+    """DA scan in two passes with the window of fine sentinels placed by the
+    network. Pass 1 tracks every ``coarse``-th amplitude of each ray (plus
+    its largest) and every ``fine``-th amplitude from ``below`` sigma under
+    to ``above`` sigma over the ray's predicted boundary
+    (``predicted_boundary``). Pass 2 tracks each ray's ``bracket``: the
+    untracked amplitudes between the last tracked survivor and the first
+    tracked loss. Where the network placed the window right, the bracket
+    spans one fine step; where it did not, the first loss is a coarse
+    sentinel and the bracket spans one coarse step, so the result is the
+    same as the three-pass ``adaptive_da_scan`` (coarse pass, window below
+    the first coarse loss, brackets) up to islands of loss the windows
+    differ on, in one pass fewer. ``track_fn(mask) -> survive`` replaces
+    the tracking (tests)."""
+    import time
+    from . import surrogate as sg
+
+    res = ScreenedDA()
+    ray = scan.ray_index()
+    n = scan.n
+    survive = np.zeros(n, dtype=bool)
+    tracked = np.zeros(n, dtype=bool)
+
+    def track(mask):
+        if not mask.any():
+            return
+        if track_fn is not None:
+            survive[mask] = np.asarray(track_fn(mask), dtype=bool)
+        else:
+            st, at, _ = run_scan(tracker, scan, num_turns, select=mask, device=device)
+            survive[mask] = sg.targets(st, at, num_turns)[0] > 0
+        tracked[mask] = True
+
+    t0 = time.perf_counter()
+    pred = predicted_boundary(p_survive, scan)
+    near = (scan.r >= pred - below) & (scan.r <= pred + above)
+    m1 = sg.sentinels(scan.r, ray, coarse) | (sg.sentinels(scan.r, ray, fine) & near)
+    track(m1)
+    res.seconds.append(time.perf_counter() - t0)
+    t0 = time.perf_counter()
+    m2 = sg.bracket(scan.r, ray, tracked, survive)
+    track(m2)
+    res.seconds.append(time.perf_counter() - t0)
+    res.pass1, res.pass2 = m1, m2
+    res.survive = sg.ray_survival(scan.r, ray, tracked, survive)
+    res.da = da_table(scan, res.survive, int(scan.lattice_index.max()) + 1 if n else 0)
+    return res
+
+
 def screened_da_scan(tracker, scan, num_turns, p_survive=None, stride=34, lo=0.02, hi=0.98,
                      band_stride=1, refine=True, device="cuda"):
     """DA scan that tracks a subset of the grid. Pass 1 tracks the

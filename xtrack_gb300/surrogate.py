@@ -40,9 +40,22 @@ def _ptr(t):
     return ctypes.c_void_p(t.data_ptr()) if t is not None else None
 
 
+def _pad8(n):
+    return (int(n) + 7) // 8 * 8
+
+
+N_OUT = 2
+
+
 class SurvivalMLP:
     """MLP n_in -> width (x depth, GELU) -> 2 outputs, BF16 weights and
-    activations, FP32 accumulation, Adam on FP32 master weights."""
+    activations, FP32 accumulation, Adam on FP32 master weights.
+
+    The input and output widths are padded to multiples of 8 (``dims``), so
+    that every operand row is a multiple of 16 bytes and the contractions
+    stage it by TMA; the padded input columns are zero, the padded output
+    rows of the last weight matrix are zero and receive zero gradients, so
+    the padding changes no result."""
 
     def __init__(self, n_in=N_COORD_FEATURES + N_SEED_FEATURES, width=256, depth=4, seed=0,
                  device="cuda", w_turn=0.5):
@@ -50,14 +63,18 @@ class SurvivalMLP:
         if self.device.type != "cuda":
             raise RuntimeError("SurvivalMLP runs on a CUDA device only")
         self._lib = _abi.load_library()
-        self.dims = [n_in] + [width] * depth + [2]
+        self.n_in = int(n_in)
+        self.dims = [_pad8(n_in)] + [width] * depth + [_pad8(N_OUT)]
         self.w_turn = float(w_turn)
         g = torch.Generator().manual_seed(seed)
         self.W, self.b = [], []
-        for k_in, k_out in zip(self.dims[:-1], self.dims[1:]):
-            std = math.sqrt(2.0 / k_in)
-            self.W.append((torch.randn(k_out, k_in, generator=g, dtype=torch.float64) * std)
-                          .float().to(self.device))
+        real = [self.n_in] + [width] * depth + [N_OUT]
+        for l, (k_in, k_out) in enumerate(zip(self.dims[:-1], self.dims[1:])):
+            std = math.sqrt(2.0 / real[l])
+            w = torch.zeros(k_out, k_in, dtype=torch.float64)
+            w[:real[l + 1], :real[l]] = torch.randn(real[l + 1], real[l], generator=g,
+                                                    dtype=torch.float64) * std
+            self.W.append(w.float().to(self.device))
             self.b.append(torch.zeros(k_out, dtype=torch.float32, device=self.device))
         self.W16 = [w.to(torch.bfloat16) for w in self.W]
         self.mW = [torch.zeros_like(w) for w in self.W]
@@ -67,8 +84,8 @@ class SurvivalMLP:
         self.gW = [torch.zeros_like(w) for w in self.W]
         self.gb = [torch.zeros_like(b) for b in self.b]
         self.step_count = 0
-        self.x_mean = torch.zeros(n_in, dtype=torch.float32, device=self.device)
-        self.x_std = torch.ones(n_in, dtype=torch.float32, device=self.device)
+        self.x_mean = torch.zeros(self.dims[0], dtype=torch.float32, device=self.device)
+        self.x_std = torch.ones(self.dims[0], dtype=torch.float32, device=self.device)
         self._acts = None
 
     # ------------------------------------------------------------------
@@ -79,14 +96,23 @@ class SurvivalMLP:
     def _stream(self):
         return ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
 
-    def set_normalisation(self, X):
+    def _padded(self, X):
         X = torch.as_tensor(X, dtype=torch.float32, device=self.device)
+        if X.shape[1] not in (self.n_in, self.dims[0]):
+            raise ValueError(f"expected {self.n_in} features, got {X.shape[1]}")
+        if X.shape[1] < self.dims[0]:
+            X = torch.nn.functional.pad(X, (0, self.dims[0] - X.shape[1]))
+        return X
+
+    def set_normalisation(self, X):
+        X = self._padded(X)
         self.x_mean = X.mean(0)
         self.x_std = X.std(0).clamp_min(1e-12)
 
     def prepare_input(self, X):
-        """Normalised BF16 copy of the features (fp32 [B, n_in])."""
-        X = torch.as_tensor(X, dtype=torch.float32, device=self.device)
+        """Normalised BF16 copy of the features (fp32 [B, n_in]), padded
+        with zero columns to ``dims[0]``."""
+        X = self._padded(X)
         Xn = ((X - self.x_mean) / self.x_std).contiguous()
         X16 = torch.empty(Xn.shape, dtype=torch.bfloat16, device=self.device)
         _abi.check_mlp(self._lib.xtg_mlp_to_bf16(_ptr(Xn), Xn.numel(), _ptr(X16), self._stream()),
@@ -94,8 +120,11 @@ class SurvivalMLP:
         return X16
 
     def forward(self, X16, keep=False):
-        """Outputs fp32 [B, 2] for BF16 input [B, n_in]; keeps the
-        activations for ``backward`` when ``keep``."""
+        """Outputs fp32 [B, dims[-1]] for BF16 input [B, dims[0]]: column 0
+        is the logit of P(survive), column 1 the normalised log loss turn,
+        the others are padding (zero). Keeps the activations for
+        ``backward`` when ``keep``; otherwise the hidden layers store only
+        their BF16 activations."""
         B = X16.shape[0]
         st = self._stream()
         acts = [(None, X16)]
@@ -104,7 +133,7 @@ class SurvivalMLP:
         for l in range(self.n_layers):
             k_in, k_out = self.dims[l], self.dims[l + 1]
             last = l == self.n_layers - 1
-            Z = torch.empty(B, k_out, dtype=torch.float32, device=self.device)
+            Z = torch.empty(B, k_out, dtype=torch.float32, device=self.device) if (keep or last) else None
             Y = None if last else torch.empty(B, k_out, dtype=torch.bfloat16, device=self.device)
             _abi.check_mlp(self._lib.xtg_mlp_gemm(
                 _ptr(y), k_in, 1, _ptr(self.W16[l]), k_in, 1, B, k_out, k_in, _ptr(self.b[l]),
@@ -119,10 +148,11 @@ class SurvivalMLP:
     def loss_and_grad(self, out, survive, logturn):
         B = out.shape[0]
         st = self._stream()
-        dout = torch.empty(B, 2, dtype=torch.float32, device=self.device)
-        dout16 = torch.empty(B, 2, dtype=torch.bfloat16, device=self.device)
+        ld = out.shape[1]
+        dout = torch.zeros(B, ld, dtype=torch.float32, device=self.device)
+        dout16 = torch.zeros(B, ld, dtype=torch.bfloat16, device=self.device)
         loss = torch.empty(B, dtype=torch.float32, device=self.device)
-        _abi.check_mlp(self._lib.xtg_mlp_loss(_ptr(out), _ptr(survive), _ptr(logturn), B,
+        _abi.check_mlp(self._lib.xtg_mlp_loss(_ptr(out), ld, _ptr(survive), _ptr(logturn), B,
                                               self.w_turn, _ptr(dout), _ptr(dout16), _ptr(loss),
                                               st), self._lib)
         return loss, dout, dout16
@@ -210,6 +240,7 @@ class SurvivalMLP:
             out = self.forward(X16[i0:i0 + batch].contiguous())
             ps.append(torch.sigmoid(out[:, 0]).cpu().numpy())
             ts.append(out[:, 1].cpu().numpy())
+        _abi.check_mlp(self._lib.xtg_mlp_device_status(), self._lib)
         return np.concatenate(ps), np.concatenate(ts)
 
 
