@@ -448,7 +448,7 @@ int32_t xtg_check_bounded_wait(int64_t limit_cycles);
  * are asynchronous on `stream`.
  */
 #define XTG_MLP_ACT_NONE 0
-#define XTG_MLP_ACT_GELU 1
+#define XTG_MLP_ACT_GELU 1   /* tanh form: z/2 (1 + tanh(sqrt(2/pi)(z + 0.044715 z^3))) */
 
 /* Tensor-core contraction R[m, n] = sum_k A(m, k) B(n, k), with A(m, k) at
  * A[m*a_sm + k*a_sk] and B(n, k) at B[n*b_sn + k*b_sk] (bf16, any strides),

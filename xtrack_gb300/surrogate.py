@@ -1,9 +1,9 @@
 """Learned screening of dynamic-aperture scans.
 
-A multilayer perceptron (default: 4 hidden layers of width 256, GELU)
-predicts, from a particle's normalised initial coordinates and its seed's
-multipole-error summary, the probability that it survives the turn budget
-and, if lost, its normalised log loss turn. It is trained on the
+A multilayer perceptron (default: 4 hidden layers of width 256, GELU in
+its tanh form) predicts, from a particle's normalised initial coordinates
+and its seed's multipole-error summary, the probability that it survives
+the turn budget and, if lost, its normalised log loss turn. It is trained on the
 ``state`` / ``at_turn`` maps that batched tracking produces, entirely with
 the library's own kernels: BF16 tensor-core contractions with FP32
 accumulation for forward and backward passes, a fixed-order bias-gradient
@@ -48,8 +48,9 @@ N_OUT = 2
 
 
 class SurvivalMLP:
-    """MLP n_in -> width (x depth, GELU) -> 2 outputs, BF16 weights and
-    activations, FP32 accumulation, Adam on FP32 master weights.
+    """MLP n_in -> width (x depth, tanh-form GELU) -> 2 outputs, BF16
+    weights and activations, FP32 accumulation, Adam on FP32 master
+    weights.
 
     The input and output widths are padded to multiples of 8 (``dims``), so
     that every operand row is a multiple of 16 bytes and the contractions
