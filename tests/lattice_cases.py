@@ -207,3 +207,35 @@ def shifted_thin_elements():
            xt.Multipole(knl=[0.0, 0.05, -0.3, 2.0], ksl=[0.0, 0.0, 0.1], shift_y=2e-3,
                         rot_s_rad=0.7, rot_s_rad_no_frame=-0.3)]
     return xt.Line(elements=els)
+
+
+def drift_aperture_pairs():
+    """Drifts followed by apertures (the pattern of MAD-X thin lattices),
+    runs of markers after drifts, apertures and kicks, an aperture after a
+    kick, a shifted aperture after a drift, a drift followed by a drift,
+    and a drift-aperture pair and a marker at the end of the line. The
+    apertures cut into a wide beam."""
+    els = [xt.Marker(),
+           xt.Drift(length=0.5),
+           xt.LimitRect(min_x=-0.02, max_x=0.018, min_y=-0.012, max_y=0.014),
+           xt.Marker(), xt.Marker(),
+           xt.Drift(length=0.3),
+           xt.LimitEllipse(a=0.022, b=0.015),
+           xt.Multipole(knl=[0.0, 0.04, 0.3]),
+           xt.Marker(),
+           xt.Drift(length=0.4),
+           xt.Marker(),
+           xt.LimitRect(min_x=-0.021, max_x=0.021, min_y=-0.016, max_y=0.016),
+           xt.Drift(length=0.2),
+           xt.LimitRect(min_x=-0.017, max_x=0.019, min_y=-0.013, max_y=0.013, shift_x=1e-3),
+           xt.Marker(), xt.Marker(), xt.Marker(),
+           xt.Drift(length=0.6),
+           xt.LimitEllipse(a=0.019, b=0.013),
+           xt.Drift(length=0.1),
+           xt.Drift(length=0.2),
+           xt.LimitRect(min_x=-0.018, max_x=0.017, min_y=-0.0125, max_y=0.012),
+           xt.Multipole(knl=[0.0, -0.04]),
+           xt.Drift(length=0.35),
+           xt.LimitEllipse(a=0.0185, b=0.0122),
+           xt.Marker()]
+    return xt.Line(elements=els)

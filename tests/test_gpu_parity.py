@@ -382,6 +382,58 @@ def test_shifted_thin_elements(arith, flags):
     compare(got, ref, 1e-14 if arith == "exact" else 1e-12)
 
 
+@pytest.mark.parametrize("arith", ["exact", "fast"])
+@pytest.mark.parametrize("flags", [0, 1 << 0, 1 << 4])
+def test_drift_aperture_pairs_and_markers(arith, flags):
+    """Drift-aperture pairs and marker runs against the oracle: forward,
+    backtracking and with local apertures ignored; then with staging chunks
+    that split the pairs (80 bytes: every pair split; 128: some), element
+    ranges that end between a drift and its aperture or inside a marker
+    run, and an element-by-element monitor. Integer fields bit for bit
+    everywhere."""
+    from lattice_cases import drift_aperture_pairs
+    line = drift_aperture_pairs()
+    recs, arrs, L = _setup(line, small_beam(600, seed=23, scale=9.0))
+    tol = 1e-14 if arith == "exact" else 1e-12
+    got, ref = _run_both(recs, arrs, L, arith=arith, num_turns=3, track_flags=flags)
+    for f in ("state", "at_turn", "at_element"):
+        assert np.array_equal(got[f], ref[f]), f
+    compare(got, ref, tol)
+    if flags == 0:
+        assert np.sum(ref["state"] <= 0) > 50      # the apertures do cut
+        lost_el = set(ref["at_element"][ref["state"] == 0].tolist())
+        assert {2, 6, 18} <= lost_el               # losses at apertures after drifts
+    if flags != 0:
+        return
+    n = len(recs)
+    for chunk in (80, 128):
+        g2, _ = gpu_track(recs, {k: v.copy() for k, v in arrs.items()}, arith=arith,
+                          line_length=L, num_turns=3, chunk_bytes=chunk)
+        for f in ("state", "at_turn", "at_element"):
+            assert np.array_equal(g2[f], ref[f]), (chunk, f)
+        compare(g2, ref, tol)
+    for start, count in ((0, 2), (0, 4), (1, 5), (5, 10), (17, n - 17), (2, n - 2)):
+        got, ref = _run_both(recs, arrs, L, arith=arith, num_turns=1, ele_start=start,
+                             num_ele_track=count, flag_end_turn_actions=0)
+        for f in ("state", "at_turn", "at_element"):
+            assert np.array_equal(got[f], ref[f]), (start, count, f)
+        compare(got, ref, tol)
+    mref = make_monitor(0, n + 1, (0, 600), ebe_mode=1)
+    mon = make_monitor(0, n + 1, (0, 600), ebe_mode=1)
+    ref = {k: v.copy() for k, v in arrs.items()}
+    pyoracle.track(recs, ref, line_length=L, num_turns=1, monitor=mref, flag_monitor=2)
+    got, mgot = gpu_track(recs, {k: v.copy() for k, v in arrs.items()}, arith=arith, line_length=L,
+                          num_turns=1, monitor=mon, flag_monitor=2)
+    for f in ("state", "at_turn", "at_element"):
+        assert np.array_equal(got[f], ref[f]), f
+    for f, v in mref["data"].items():
+        if f in ("state", "at_turn", "at_element", "particle_id"):
+            assert np.array_equal(mgot[f], v), f
+        else:
+            scale = np.max(np.abs(v)) or 1.0
+            assert np.max(np.abs(mgot[f] - v)) / scale <= tol, f
+
+
 def test_batch_matches_per_seed_oracle():
     """Three error seeds of one ring in one persistent launch, particles of
     the seeds interleaved: each particle equals the oracle run of its seed."""
