@@ -244,7 +244,10 @@ def test_line_dict_roundtrip():
 
 
 def test_turn_split(monkeypatch):
-    """tracker.py:1270-1336: first partial turn, middle turns, last turn."""
+    """tracker.py:1270-1336: first partial turn, middle turns, last turn.
+    A first turn that is a whole turn with the middle turns' end-of-turn
+    actions joins them in one call (the same arguments but the turn count,
+    so the same result)."""
     calls = []
 
     class FakeTracker(xt.Tracker):
@@ -276,13 +279,14 @@ def test_turn_split(monkeypatch):
     monkeypatch.setattr(torch.cuda, "current_stream", lambda d: type("S", (), {"cuda_stream": 0})())
     monkeypatch.setattr(torch.cuda, "device", lambda d: __import__("contextlib").nullcontext())
     cases = [
-        (dict(num_turns=3), [(1, 0, 10, True), (2, 0, 10, True)]),
+        (dict(num_turns=3), [(3, 0, 10, True)]),
+        (dict(num_turns=1), [(1, 0, 10, True)]),
         (dict(ele_start=4, num_turns=2), [(1, 4, 6, True), (1, 0, 10, True)]),
         (dict(ele_start=3, ele_stop=7), [(1, 3, 4, False)]),
         (dict(ele_start=7, ele_stop=3), [(1, 7, 3, True), (1, 0, 3, False)]),
         (dict(ele_start=2, ele_stop=5, num_turns=3), [(1, 2, 8, True), (1, 0, 10, True),
                                                       (1, 0, 5, False)]),
-        (dict(num_elements=25), [(1, 0, 10, True), (1, 0, 10, True), (1, 0, 5, False)]),
+        (dict(num_elements=25), [(2, 0, 10, True), (1, 0, 5, False)]),
         (dict(ele_start=5, num_elements=3), [(1, 5, 3, False)]),
     ]
     for kw, expected in cases:
@@ -290,6 +294,14 @@ def test_turn_split(monkeypatch):
         tr._track(P(), **kw)
         got = [c for c in calls if c[0] > 0 or c[2] > 0]
         assert got == expected, (kw, calls)
+    # without end-of-turn actions the calls' arguments agree as well
+    line.skip_end_turn_actions = True
+    calls.clear()
+    tr._track(P(), num_turns=3)
+    assert calls == [(3, 0, 10, False)], calls
+    calls.clear()
+    tr._track(P(), ele_start=4, num_turns=2)
+    assert calls == [(1, 4, 6, False), (1, 0, 10, False)], calls
 
 
 def _shard_worker(rank, world, port, n, out):

@@ -898,6 +898,9 @@ __global__ void compact_kernel(const int64_t* __restrict__ state, const int32_t*
     }
 }
 
+// threads of the one block of items_kernel
+static constexpr int kItemsThreads = 1024;
+
 // Cuts each lattice's list into items of at most `block` particles and
 // resets the queue counter. A list that needs more than `items_cap` items
 // writes none: the round tracks nothing and the error word says why.
@@ -915,16 +918,15 @@ __global__ void items_kernel(const int32_t* lat_count, const int64_t* lat_pbase,
     }
     __syncthreads();
     if (!s_fits) return;
-    // one thread per lattice writes that lattice's items
-    for (int32_t l = threadIdx.x; l < n_lat; l += blockDim.x) {
-        int32_t first = 0;
-        for (int32_t q = 0; q < l; q++) first += (lat_count[q] + block - 1) / block;
+    // lattice by lattice, the block's threads write that lattice's items
+    int32_t first = 0;
+    for (int32_t l = 0; l < n_lat; l++) {
         int32_t const c = lat_count[l];
         int32_t const ni = (c + block - 1) / block;
-        for (int32_t j = 0; j < ni; j++) {
-            int32_t const cnt = min(block, c - j * block);
-            items[first + j] = make_int4(l, (int32_t)(lat_pbase[l] + (int64_t)j * block), cnt, 0);
-        }
+        int64_t const pb = lat_pbase[l];
+        for (int32_t j = threadIdx.x; j < ni; j += blockDim.x)
+            items[first + j] = make_int4(l, (int32_t)(pb + (int64_t)j * block), min(block, c - j * block), 0);
+        first += ni;
     }
 }
 
@@ -1212,7 +1214,7 @@ static int32_t launch_round(ExecCtx* C, const TrackArgs& a, const int32_t* lat, 
     XTG_CUDA_CHECK(cudaMemsetAsync(W.lat_count, 0, n_lat * sizeof(int32_t), s));
     int64_t const cgrid = (cap + 255) / 256;
     compact_kernel<<<(unsigned)cgrid, 256, 0, s>>>(a.P.state, lat, cap, n_lat, W.lat_pbase, W.lat_count, W.idx);
-    items_kernel<<<1, 256, 0, s>>>(W.lat_count, W.lat_pbase, n_lat, block, W.items, W.items_cap, W.counters + 0,
+    items_kernel<<<1, kItemsThreads, 0, s>>>(W.lat_count, W.lat_pbase, n_lat, block, W.items, W.items_cap, W.counters + 0,
                                    W.counters + 1, W.counters + 2);
     track_kernel<kExact><<<grid, block, smem, s>>>(a);
     g_launch_count.fetch_add(3);
@@ -1474,7 +1476,7 @@ static int32_t run_rounds_noalloc(unsigned char* scratch, TrackArgs a, int64_t c
         XTG_CUDA_CHECK(cudaMemsetAsync(lat_count, 0, sizeof(int32_t), s));
         compact_kernel<<<(unsigned)((cap + 255) / 256), 256, 0, s>>>(a.P.state, nullptr, cap, 1, lat_pbase,
                                                                    lat_count, idx);
-        items_kernel<<<1, 256, 0, s>>>(lat_count, lat_pbase, 1, block, items, kNoAllocItems, counters + 0,
+        items_kernel<<<1, kItemsThreads, 0, s>>>(lat_count, lat_pbase, 1, block, items, kNoAllocItems, counters + 0,
                                        counters + 1, counters + 2);
         track_kernel<kExact><<<grid, block, 0, s>>>(a);
         g_launch_count.fetch_add(3);

@@ -274,11 +274,21 @@ class Tracker:
             if mem is not None:
                 self._set_multi_element_monitor(mem)
             try:
-                self._launch(pstruct, 1, ele_start, num_elements_first_turn, flag_end_first,
-                             flag_monitor, mstruct, flags, stream)
-                if num_middle_turns > 0:
-                    self._launch(pstruct, num_middle_turns, 0, L, flag_end_middle, flag_monitor,
+                if (ele_start == 0 and num_elements_first_turn == L and flag_end_first == flag_end_middle
+                        and num_middle_turns > 0):
+                    # the first turn is a whole turn with the middle turns'
+                    # arguments: one call, the same result (the reference's
+                    # split exists for a partial first turn), and a turn-by-
+                    # turn monitor's records of a particle are written in one
+                    # pass instead of two
+                    self._launch(pstruct, 1 + num_middle_turns, 0, L, flag_end_middle, flag_monitor,
                                  mstruct, flags, stream)
+                else:
+                    self._launch(pstruct, 1, ele_start, num_elements_first_turn, flag_end_first,
+                                 flag_monitor, mstruct, flags, stream)
+                    if num_middle_turns > 0:
+                        self._launch(pstruct, num_middle_turns, 0, L, flag_end_middle, flag_monitor,
+                                     mstruct, flags, stream)
                 if num_elements_last_turn > 0:
                     self._launch(pstruct, 1, 0, num_elements_last_turn, False, flag_monitor,
                                  mstruct, flags, stream)
