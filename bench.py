@@ -960,6 +960,93 @@ def run_real_lattice(args):
     print(json.dumps(out))
 
 
+def run_sliced_ring(args):
+    """The thick ring in its thin-sliced form: every magnet of the
+    6993-element thick ring sliced with Teapot(8) by
+    Line.slice_thick_elements (43,793 elements: thin kicks, drift slices,
+    entry and exit edges, apertures, the cavity), 10^6 protons, one turn
+    per step through the C-ABI (xtg_lattice_create / xtg_track) with CUDA
+    events, in the --arith arithmetic; the oracle's port of the reference
+    OpenMP path on the host cores as the CPU baseline."""
+    import ctypes
+
+    import torch
+    import xtrack_gb300 as xt
+    from xtrack_gb300 import _abi, workloads
+    import pyoracle
+
+    rank, world, local = _dist()
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    line = workloads.thick_ring()
+    line.slice_thick_elements([xt.Strategy(slicing=xt.Teapot(8))])
+    recs = np.ascontiguousarray(line._element_records())
+    n_el, L = len(recs), float(line.get_length())
+    lib = _abi.load_library()
+    cfg = _abi.XtgConfig()
+    cfg.has_global_xy_limit = 1
+    cfg.global_xy_limit = 1.0
+    cfg.arith = _abi.ARITH_FAST if args.arith == "fast" else _abi.ARITH_EXACT
+    h = ctypes.c_void_p()
+    _abi.check(lib.xtg_lattice_create(recs.ctypes.data_as(ctypes.c_void_p), n_el,
+                                      ctypes.byref(cfg), ctypes.byref(h)), lib)
+    nn, fl = ctypes.c_int64(), ctypes.c_double()
+    _abi.check(lib.xtg_lattice_info(h, ctypes.byref(nn), 0, n_el, ctypes.byref(fl)), lib)
+    flops_pt = fl.value
+    beam = workloads.gaussian_beam(args.particles, 7e12, device=dev, seed=7)
+    ps = beam._xtg_struct()
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        _abi.check(lib.xtg_track(h, ctypes.byref(ps), 1, 0, n_el, 1, 1, 0, n_el, L, None, 0,
+                                 ctypes.c_void_p(stream.cuda_stream)), lib)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize(dev)
+    alive0 = int((beam.state > 0).sum())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        e1.synchronize()
+    _abi.check(lib.xtg_device_status(h), lib)
+    ms = e0.elapsed_time(e1)
+    alive1 = int((beam.state > 0).sum())
+    value = alive1 * args.steps / (ms * 1e-3)
+    peak = ctypes.c_double()
+    _abi.check(lib.xtg_measure_fp64_peak(ctypes.byref(peak)), lib)
+    lib.xtg_lattice_destroy(h)
+    out = {"metric": "FP64 particle-turns/s on the thick ring sliced thin (Teapot(8))",
+           "value": value, "unit": "particle-turns/s", "higher_is_better": True, "n_gpus": 1,
+           "dtype": "f64", "data": "synthetic", "arith": args.arith,
+           "config": {"workload": f"thick LHC-like ring sliced with Teapot(8): {n_el} elements, "
+                                  f"{args.particles:g} protons 7 TeV, 1 turn per step",
+                      "particles": args.particles, "elements": n_el, "turns_per_step": 1},
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+           "alive_before": alive0, "alive_after": alive1,
+           "roofline": {"bound": "fp64", "achieved": value * flops_pt / 1e12,
+                        "peak": peak.value / 1e12, "unit": "TFLOP/s",
+                        "frac": value * flops_pt / peak.value, "flops_per_particle_turn": flops_pt},
+           "clocks": clk.summary()}
+    if not args.no_cpu_baseline:
+        pyoracle.ensure_built(with_ref=False)
+        n_cpu = 20000
+        arrs = pyoracle.host_arrays(workloads.gaussian_beam(n_cpu, 7e12, device="cpu", seed=8).to_numpy())
+        t0 = time.perf_counter()
+        pyoracle.track(recs, arrs, line_length=L, num_turns=1, mode=pyoracle.MODE_OPENMP)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": float(np.sum(arrs["state"] > 0)) / dt,
+                               "unit": "particle-turns/s", "cores": pyoracle.max_threads(),
+                               "kind": "port",
+                               "sample": f"{n_cpu} particles x 1 turn ({dt:.2f} s, OpenMP)"}
+    print(json.dumps(out))
+
+
 def run_turn_latency(args):
     """Milliseconds per turn of the thick ring for particle counts from a
     fraction of one resident wave (8 warps per SM) to four waves, for
@@ -1031,7 +1118,7 @@ def main():
                     help="record 6 coordinates per turn of the first N particles")
     ap.add_argument("--workload", default="thick_ring",
                     choices=["thick_ring", "da_screen", "turn_latency", "batch_scan", "toy_ring",
-                             "real_lattice", "monitor_hbm", "mlp"])
+                             "real_lattice", "monitor_hbm", "mlp", "sliced_ring"])
     ap.add_argument("--lattice", default="sps", choices=sorted(REAL_LATTICES),
                     help="real_lattice workload: which fixture's line")
     ap.add_argument("--toy-particles", dest="toy_particles", type=int, default=10000)
@@ -1086,6 +1173,8 @@ def main():
         run_batch_scan(args)
     elif args.workload == "mlp":
         run_mlp(args)
+    elif args.workload == "sliced_ring":
+        run_sliced_ring(args)
     elif args.workload == "monitor_hbm":
         run_monitor_hbm(args)
     elif args.workload == "toy_ring":
