@@ -343,7 +343,8 @@ def run_da_screen(args):
     fine window below the first coarse loss, brackets); (5) two passes with
     the fine window placed by the network around its predicted boundary;
     (6) the same two passes without the network (coarse sentinels, brackets
-    of one coarse step). value = plain time / time of (2). The DA error per
+    of one coarse step). value = plain time / time of (1), the
+    configuration's one-pass screening. The DA error per
     ray (sigma) judges each screened result against the plain one; the
     network's own DA per ray (its predicted boundary) is reported beside
     them."""
@@ -507,7 +508,7 @@ def run_da_screen(args):
     net_err = np.abs(da_net - da_plain)
 
     grid_step = float(np.max(np.diff(np.unique(s_test.r))))
-    out = {"metric": "DA-scan time, surrogate vs plain", "value": t_plain / t_net,
+    out = {"metric": "DA-scan time, surrogate vs plain", "value": t_plain / t_band,
            "unit": "x (plain time / screened time)", "higher_is_better": True, "n_gpus": 1,
            "dtype": "f64 tracking, bf16/f32 network", "data": "synthetic",
            "config": {"workload": "thick LHC-like ring seeds (6993 elements), polar grid "
@@ -520,10 +521,10 @@ def run_da_screen(args):
                       "train_particles": int(s_train.n), "test_particles": int(s_test.n),
                       "radial_step_sigma": grid_step, "arith": args.arith,
                       "features": args.da_features},
-           "plain_s": t_plain, "screened_s": t_net,
-           "da_error_sigma": two_pass["da_error_max_sigma"],
-           "da_error_mean_sigma": two_pass["da_error_mean_sigma"],
-           "tracked_fraction": two_pass["tracked_fraction"],
+           "plain_s": t_plain, "screened_s": t_band,
+           "da_error_sigma": band["da_error_max_sigma"],
+           "da_error_mean_sigma": band["da_error_mean_sigma"],
+           "tracked_fraction": band["tracked_fraction"],
            "methods": {"learned_band_one_pass": band, "sentinels_band_bracket": two_pass,
                        "sentinels_bracket_no_network": no_net,
                        "adaptive_three_pass_no_network": adaptive,
@@ -1131,7 +1132,7 @@ def main():
     ap.add_argument("--batch-tune-max", dest="batch_tune_max", type=int, default=500000,
                     help="largest particle count the batch autotuner times candidates on")
     ap.add_argument("--da-turns", dest="da_turns", type=int, default=100)
-    ap.add_argument("--da-train-particles", dest="da_train_particles", type=int, default=16000)
+    ap.add_argument("--da-train-particles", dest="da_train_particles", type=int, default=3200)
     ap.add_argument("--da-lo", dest="da_lo", type=float, default=0.02)
     ap.add_argument("--da-hi", dest="da_hi", type=float, default=0.98)
     ap.add_argument("--da-stride", dest="da_stride", type=int, default=34,
@@ -1143,7 +1144,9 @@ def main():
                          "keeps everything within 20 sigma, its DA lies near the aperture")
     ap.add_argument("--da-particles", dest="da_particles", type=int, default=100000,
                     help="mean particles per seed (uniform in [n/2, 3n/2])")
-    ap.add_argument("--da-train-seeds", dest="da_train_seeds", type=int, default=24)
+    ap.add_argument("--da-train-seeds", dest="da_train_seeds", type=int, default=120,
+                    help="seeds of the training scan: the network carries a seed's DA to "
+                         "unseen seeds only when it has seen many (24: 9.5 sigma off, 120: 0.94)")
     ap.add_argument("--da-test-seeds", dest="da_test_seeds", type=int, default=8)
     ap.add_argument("--da-epochs", dest="da_epochs", type=int, default=40)
     ap.add_argument("--da-features", dest="da_features", default="all",
