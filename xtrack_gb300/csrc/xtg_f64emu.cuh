@@ -109,12 +109,17 @@ XTG_EMU_HD double emul_split(const F64Split& a, const F64Split& b) {
     // 2047 gives the correctly rounded infinity)
     if ((ea1 > eb1 ? ea1 : eb1) < 2046u && (uint32_t)e < 2045u) {
         // the 106-bit product of the 53-bit significands (mh:lo) in four
-        // 32-bit words w3:w2:w1:w0
+        // 32-bit words w3:w2:w1:w0. The partial products are independent
+        // (a short dependency chain for the integer pipes); the two middle
+        // ones are below 2^53 (mh has 21 bits), so they and the carry out of
+        // the lowest word add up without overflowing 64 bits.
         uint64_t const p0 = (uint64_t)a.lo * b.lo;
-        uint64_t const t = (uint64_t)a.mh * b.lo + (p0 >> 32);
-        uint64_t const u = (uint64_t)a.lo * b.mh + (uint32_t)t;
-        uint64_t const w = (uint64_t)a.mh * b.mh + (t >> 32) + (u >> 32);
-        uint32_t const w0 = (uint32_t)p0, w1 = (uint32_t)u;
+        uint64_t const p1 = (uint64_t)a.mh * b.lo;
+        uint64_t const p2 = (uint64_t)a.lo * b.mh;
+        uint64_t const p3 = (uint64_t)a.mh * b.mh;
+        uint64_t const mid = p1 + p2 + (p0 >> 32);
+        uint64_t const w = p3 + (mid >> 32);
+        uint32_t const w0 = (uint32_t)p0, w1 = (uint32_t)mid;
         uint32_t const w2 = (uint32_t)w, w3 = (uint32_t)(w >> 32);
         // top = 1 when the product lies in [2^105, 2^106): its leading bit
         // is bit 9 of w3; shift the 53 leading bits to mh:ml (implicit bit
