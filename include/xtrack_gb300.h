@@ -496,6 +496,13 @@ int32_t xtg_mlp_to_bf16(const float* x, int64_t n, void* y, void* stream);
  * (that kernel's outputs were not written), else XTG_OK. */
 int32_t xtg_mlp_device_status(void);
 
+/* Diagnostic of the failure path of the contraction's bounded waits: one
+ * wait of its kind on a shared-memory barrier that nothing completes, given
+ * up after limit_cycles SM cycles (1 .. 2e9). Returns what
+ * xtg_mlp_device_status then reports: XTG_E_TIMEOUT when the wait gave up
+ * and the status was read and cleared; the context stays usable. */
+int32_t xtg_mlp_check_bounded_wait(int64_t limit_cycles);
+
 /* Message of the last failed xtg_mlp_* call of this thread. */
 int32_t xtg_mlp_get_last_error(char* buf, int64_t n);
 

@@ -110,6 +110,26 @@ def test_gemm_matches_torch(M, N, K, transpose):
 
 
 @pytest.mark.gpu
+def test_bounded_wait_of_the_contraction_times_out_and_the_context_survives():
+    """The contraction's mbarrier waits are bounded: one of them on a
+    barrier that nothing completes gives up after about 1 ms of SM clock;
+    the device status reports XTG_E_TIMEOUT once and is then clear, and a
+    contraction on the same context still matches torch."""
+    import torch
+    from xtrack_gb300 import _abi
+    lib = _abi.load_library()
+    assert lib.xtg_mlp_check_bounded_wait(2_000_000) == _abi.XTG_E_TIMEOUT
+    assert lib.xtg_mlp_device_status() == _abi.XTG_OK
+    g = torch.Generator().manual_seed(9)
+    A = _bf(torch.randn(300, 256, generator=g)).cuda()
+    B = _bf(torch.randn(256, 256, generator=g)).cuda()
+    bias = torch.zeros(256).cuda()
+    Z, _, _ = _gemm(A, 256, 1, B, 256, 1, 300, 256, 256, bias)
+    ref = A.float() @ B.float().t()
+    assert float((Z - ref).abs().max()) <= 1e-4 * 16 * float(ref.abs().max())
+
+
+@pytest.mark.gpu
 def test_colsum_and_adam():
     import torch
     from xtrack_gb300 import _abi

@@ -230,7 +230,8 @@ EXPORTED_SYMBOLS = (
     "xtg_track_batch", "xtg_sync", "xtg_launch_count", "xtg_measure_fp64_peak",
     "xtg_check_bounded_wait", "xtg_f64_mul_host", "xtg_f64_mul_device", "xtg_measure_emul_rate",
     "xtg_mlp_gemm", "xtg_mlp_act_backward", "xtg_mlp_colsum", "xtg_mlp_loss", "xtg_mlp_adam",
-    "xtg_mlp_to_bf16", "xtg_mlp_device_status", "xtg_mlp_get_last_error",
+    "xtg_mlp_to_bf16", "xtg_mlp_device_status", "xtg_mlp_check_bounded_wait",
+    "xtg_mlp_get_last_error",
 )
 
 MLP_ACT_NONE = 0
@@ -306,6 +307,8 @@ def load_library(path=None):
     lib.xtg_mlp_to_bf16.restype = i32
     lib.xtg_mlp_device_status.argtypes = []
     lib.xtg_mlp_device_status.restype = i32
+    lib.xtg_mlp_check_bounded_wait.argtypes = [i64]
+    lib.xtg_mlp_check_bounded_wait.restype = i32
     lib.xtg_mlp_get_last_error.argtypes = [c.c_char_p, i64]
     lib.xtg_mlp_get_last_error.restype = i32
     lib.xtg_sync.argtypes = [c.c_void_p]

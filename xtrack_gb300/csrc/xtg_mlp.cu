@@ -148,11 +148,11 @@ constexpr long long kMlpWaitLimit = 2000000000LL;
 
 // Bounded wait on the phase of `parity`; on time-out records the error word
 // and returns false.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long long limit = kMlpWaitLimit) {
     if (mbar_try_wait(bar, parity)) return true;
     long long const t0 = clock64();
     while (!mbar_try_wait(bar, parity)) {
-        if (clock64() - t0 > kMlpWaitLimit) {
+        if (clock64() - t0 > limit) {
             atomicExch(&g_mlp_dev_err, XTG_MLP_DEV_ERR_TIMEOUT);
             return false;
         }
@@ -480,6 +480,20 @@ __global__ void __launch_bounds__(GEMM_THREADS) gemm_tc_kernel(const __grid_cons
                      : "memory");
 }
 
+// One wait of the contraction's kind on a barrier that nothing completes:
+// thread 0 gives up after `limit` cycles and records the time-out in the
+// device error word.
+__global__ void mlp_wait_check_kernel(long long limit) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1u);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) (void)mbar_wait(&bar, 0u, limit);
+    __syncthreads();
+}
+
 // dZ = dY * act'(Z): fp32 and bf16 copies.
 __global__ void act_backward_kernel(const float* __restrict__ dY, const float* __restrict__ Z, int64_t n,
                                     int32_t act, float* __restrict__ dZ, __nv_bfloat16* __restrict__ dZ16) {
@@ -759,6 +773,16 @@ int32_t xtg_mlp_to_bf16(const float* x, int64_t n, void* y, void* stream) {
     to_bf16_kernel<<<blocks_for(n, 256), 256, 0, (cudaStream_t)stream>>>(x, n, (__nv_bfloat16*)y);
     xtg_internal_launch_add(1);
     return launched("to_bf16_kernel");
+}
+
+int32_t xtg_mlp_check_bounded_wait(int64_t limit_cycles) {
+    if (limit_cycles < 1 || limit_cycles > kMlpWaitLimit)
+        return fail(XTG_E_VALUE, "xtg_mlp_check_bounded_wait: limit must be in [1, 2e9] cycles");
+    mlp_wait_check_kernel<<<1, 32>>>((long long)limit_cycles);
+    xtg_internal_launch_add(1);
+    int32_t const st = launched("mlp_wait_check_kernel");
+    if (st != XTG_OK) return st;
+    return xtg_mlp_device_status();
 }
 
 int32_t xtg_mlp_device_status(void) {
