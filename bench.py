@@ -536,6 +536,7 @@ def run_da_screen(args):
            "da_plain_mean_sigma": float(da_plain.mean()),
            "misclassification_all": float(np.mean((p >= 0.5) != surv_plain)),
            "train_scan_s": t_train_scan, "fit_s": t_fit, "fit_loss": [hist[0], hist[-1]],
+           "fit_loss_curve": [float(h) for h in hist],
            "setup_s": t_setup}
     print(json.dumps(out))
 
