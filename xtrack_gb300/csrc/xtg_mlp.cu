@@ -82,6 +82,7 @@ struct GemmArgs {
     int32_t load;             // LOAD_*
     int32_t a_mn, b_mn;       // TMA path: the operand is stored MN-major
     int32_t vec_z, vec_y, vec_c;   // output base 16-byte aligned and pitch a multiple of 16 bytes
+    int32_t vec_bias;              // bias 16-byte aligned
 };
 
 // GELU in its tanh form (Hendrycks and Gimpel, 2016):
@@ -267,8 +268,20 @@ __device__ __forceinline__ void load_tile_sw128(unsigned char* S, int nrows, con
 __device__ __forceinline__ void store_row(const GemmArgs& g, int64_t row, int col0, const float (&v)[16]) {
     bool const full = col0 + 16 <= g.N;
     float z[16];
+    if (full && g.vec_bias) {
+        const float4* b4 = reinterpret_cast<const float4*>(g.bias + col0);
 #pragma unroll
-    for (int j = 0; j < 16; j++) z[j] = v[j] + ((g.bias && col0 + j < g.N) ? __ldg(g.bias + col0 + j) : 0.0f);
+        for (int q = 0; q < 4; q++) {
+            float4 const b = __ldg(b4 + q);
+            z[4 * q] = v[4 * q] + b.x;
+            z[4 * q + 1] = v[4 * q + 1] + b.y;
+            z[4 * q + 2] = v[4 * q + 2] + b.z;
+            z[4 * q + 3] = v[4 * q + 3] + b.w;
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < 16; j++) z[j] = v[j] + ((g.bias && col0 + j < g.N) ? __ldg(g.bias + col0 + j) : 0.0f);
+    }
     if (full) {
         if (g.Z && g.vec_z) {
             float4* p = reinterpret_cast<float4*>(g.Z + row * g.z_ld + col0);
@@ -320,7 +333,7 @@ __device__ __forceinline__ void store_row(const GemmArgs& g, int64_t row, int co
     }
 }
 
-__global__ void __launch_bounds__(GEMM_THREADS) gemm_tc_kernel(const __grid_constant__ CUtensorMap tmA,
+__global__ void __launch_bounds__(GEMM_THREADS, 2) gemm_tc_kernel(const __grid_constant__ CUtensorMap tmA,
                                                                const __grid_constant__ CUtensorMap tmB,
                                                                const GemmArgs g) {
     extern __shared__ unsigned char dsm_raw[];
@@ -478,6 +491,190 @@ __global__ void __launch_bounds__(GEMM_THREADS) gemm_tc_kernel(const __grid_cons
     if (warp == 0)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)g.bn)
                      : "memory");
+}
+
+// ---------------------------------------------------------------------------
+// Persistent variant for TMA-staged operands (K > 0). One CTA per SM walks
+// the output tiles (tile t = blockIdx.x + j * gridDim.x, row tile t / nN,
+// column tile t % nN): warp 0 loads the operand stages (TMA), warp 1 issues
+// the MMAs, warps 2-17 run the epilogue. Two accumulators in tensor memory
+// (2 x BN columns) let the epilogue of one tile run under the loads and
+// MMAs of the next, and four stages keep the loads ahead of the MMAs.
+// Warp 2 + w (w = 0..15) reads TMEM lane quarter (2 + w) % 4 and a quarter
+// of the tile's columns. Barriers: full / empty per stage (producer <-> MMA), acc_full / acc_empty
+// per accumulator (MMA <-> epilogue). Every wait is bounded; a role that
+// gives up raises the shared abort flag, the others leave their loops
+// (bounded themselves), the MMA thread waits for its MMAs in flight and the
+// producer for its copies before the tensor memory is freed.
+// ---------------------------------------------------------------------------
+constexpr int P_STAGES = 4;
+constexpr int P_EPI_WARPS = 16;
+constexpr int P_THREADS = 64 + 32 * P_EPI_WARPS;
+constexpr uint32_t P_MAX_DSMEM = P_STAGES * (A_STAGE_BYTES + MAX_BN * TK * 2) + 1024;
+
+__global__ void __launch_bounds__(P_THREADS, 1)
+    gemm_tc_persistent_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                              const GemmArgs g) {
+    extern __shared__ unsigned char dsm_raw[];
+    __shared__ __align__(8) uint64_t full_bar[P_STAGES];
+    __shared__ __align__(8) uint64_t empty_bar[P_STAGES];
+    __shared__ __align__(8) uint64_t acc_full[2];
+    __shared__ __align__(8) uint64_t acc_empty[2];
+    __shared__ __align__(8) uint64_t mma_done;
+    __shared__ uint32_t tmem_base_s;
+    __shared__ volatile int32_t abort_s;
+
+    unsigned char* const dsm = dsm_raw + ((1024u - (smem_u32(dsm_raw) & 1023u)) & 1023u);
+    int const tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    uint32_t const stage_bytes = A_STAGE_BYTES + (uint32_t)g.bn * TK * 2;
+    int const nk = (g.K + TK - 1) / TK;
+    int const n_tn = (g.N + g.bn - 1) / g.bn;
+    int64_t const n_total = (((int64_t)g.M + TM - 1) / TM) * n_tn;
+    uint32_t const ncols = 2u * (uint32_t)g.bn;
+
+    if (tid == 0) {
+        for (int s = 0; s < P_STAGES; s++) {
+            mbar_init(&full_bar[s], 1u);
+            mbar_init(&empty_bar[s], 1u);
+        }
+        for (int a = 0; a < 2; a++) {
+            mbar_init(&acc_full[a], 1u);
+            mbar_init(&acc_empty[a], (uint32_t)P_EPI_WARPS);
+        }
+        mbar_init(&mma_done, 1u);
+        abort_s = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(&tmem_base_s)),
+                     "r"(ncols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    uint32_t const tmem = tmem_base_s;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            // producer
+            int64_t it = 0;
+            for (int64_t t = blockIdx.x; t < n_total && !abort_s; t += gridDim.x) {
+                int32_t const m0 = (int32_t)((t / n_tn) * TM);
+                int32_t const n0 = (int32_t)(t % n_tn) * g.bn;
+                for (int kt = 0; kt < nk; kt++, it++) {
+                    int const s = (int)(it % P_STAGES);
+                    if (it >= P_STAGES && !mbar_wait(&empty_bar[s], (uint32_t)((it / P_STAGES - 1) & 1))) {
+                        abort_s = 1;
+                        break;
+                    }
+                    if (abort_s) break;
+                    unsigned char* const As = dsm + (size_t)s * stage_bytes;
+                    unsigned char* const Bs = As + A_STAGE_BYTES;
+                    int32_t const k0 = kt * TK;
+                    mbar_expect_tx(&full_bar[s], stage_bytes);
+                    if (!g.a_mn) {
+                        tma_load_2d(As, &tmA, k0, m0, &full_bar[s]);
+                    } else {
+                        tma_load_2d(As, &tmA, m0, k0, &full_bar[s]);
+                        tma_load_2d(As + MN_BOX_BYTES, &tmA, m0 + 64, k0, &full_bar[s]);
+                    }
+                    if (!g.b_mn) {
+                        tma_load_2d(Bs, &tmB, k0, n0, &full_bar[s]);
+                    } else {
+                        for (int j = 0; j < g.bn / 64; j++)
+                            tma_load_2d(Bs + j * MN_BOX_BYTES, &tmB, n0 + 64 * j, k0, &full_bar[s]);
+                    }
+                }
+            }
+            if (abort_s) {
+                // no copy may still write into shared memory when the CTA exits
+                for (int64_t j = it - P_STAGES < 0 ? 0 : it - P_STAGES; j < it; j++)
+                    (void)mbar_wait(&full_bar[j % P_STAGES], (uint32_t)((j / P_STAGES) & 1));
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            // MMA issuer
+            uint32_t const idesc = instr_desc(g.bn, g.a_mn, g.b_mn);
+            uint32_t const a_step = g.a_mn ? 16u * 128u : (uint32_t)UK * 2u;
+            uint32_t const b_step = g.b_mn ? 16u * 128u : (uint32_t)UK * 2u;
+            uint32_t const a_lbo = g.a_mn ? MN_BOX_BYTES : 16u, b_lbo = g.b_mn ? MN_BOX_BYTES : 16u;
+            int64_t it = 0, i = 0;
+            bool issued = false;
+            for (int64_t t = blockIdx.x; t < n_total && !abort_s; t += gridDim.x, i++) {
+                int const acc = (int)(i & 1);
+                if (i >= 2 && !mbar_wait(&acc_empty[acc], (uint32_t)(((i >> 1) - 1) & 1))) {
+                    abort_s = 1;
+                    break;
+                }
+                tc_fence_after();
+                uint32_t const d = tmem + (uint32_t)(acc * g.bn);
+                bool ok = true;
+                for (int kt = 0; kt < nk; kt++, it++) {
+                    int const s = (int)(it % P_STAGES);
+                    if (!mbar_wait(&full_bar[s], (uint32_t)((it / P_STAGES) & 1))) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    uint32_t const a0 = smem_u32(dsm + (size_t)s * stage_bytes);
+                    uint32_t const b0 = a0 + A_STAGE_BYTES;
+#pragma unroll
+                    for (int kk = 0; kk < TK / UK; kk++) {
+                        uint64_t const da = smem_desc(a0 + kk * a_step, a_lbo, 1024u);
+                        uint64_t const db = smem_desc(b0 + kk * b_step, b_lbo, 1024u);
+                        tc_mma(d, da, db, idesc, (kt | kk) != 0 ? 1u : 0u);
+                    }
+                    issued = true;
+                    tc_commit(&empty_bar[s]);
+                }
+                if (!ok) {
+                    abort_s = 1;
+                    break;
+                }
+                tc_commit(&acc_full[acc]);
+            }
+            // every MMA issued has completed before the tensor memory is freed
+            if (issued) tc_commit(&mma_done);
+            else mbar_arrive(&mma_done);
+            if (!mbar_wait(&mma_done, 0u)) abort_s = 1;
+        }
+    } else {
+        // epilogue: a warp reaches only the TMEM lanes of its quarter
+        // (warp % 4); the four warps of a quarter take a quarter of the
+        // columns each
+        int const lane_q = warp & 3, col_g = (warp - 2) >> 2;
+        int const span = g.bn / 4;
+        int64_t i = 0;
+        for (int64_t t = blockIdx.x; t < n_total; t += gridDim.x, i++) {
+            int const acc = (int)(i & 1);
+            bool const ok = mbar_wait(&acc_full[acc], (uint32_t)((i >> 1) & 1));
+            if (__any_sync(0xffffffffu, !ok || abort_s)) {
+                abort_s = 1;
+                break;
+            }
+            tc_fence_after();
+            int64_t const m0 = (t / n_tn) * TM;
+            int const n0 = (int)(t % n_tn) * g.bn;
+            int64_t const row = m0 + lane_q * 32 + lane;
+            uint32_t const taddr = tmem + ((uint32_t)(lane_q * 32) << 16) + (uint32_t)(acc * g.bn);
+            for (int c0 = col_g * span; c0 < (col_g + 1) * span && n0 + c0 < g.N; c0 += 16) {
+                float v[16];
+                tc_ld16(taddr + (uint32_t)c0, v);
+                if (row < g.M) store_row(g, row, n0 + c0, v);
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&acc_empty[acc]);
+        }
+    }
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 1)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols) : "memory");
 }
 
 // One wait of the contraction's kind on a barrier that nothing completes:
@@ -692,6 +889,7 @@ int32_t xtg_mlp_gemm(const void* A, int64_t a_sm, int64_t a_sk, const void* B, i
     g.vec_z = Z && ((uintptr_t)Z & 15u) == 0 && z_ld % 4 == 0;
     g.vec_y = Y && ((uintptr_t)Y & 15u) == 0 && y_ld % 8 == 0;
     g.vec_c = C && ((uintptr_t)C & 15u) == 0 && c_ld % 4 == 0;
+    g.vec_bias = bias && ((uintptr_t)bias & 15u) == 0;
 
     CUtensorMap ta, tb;
     memset(&ta, 0, sizeof(ta));
@@ -711,6 +909,25 @@ int32_t xtg_mlp_gemm(const void* A, int64_t a_sm, int64_t a_sk, const void* B, i
     int64_t const m_tiles = ((int64_t)M + TM - 1) / TM;
     int64_t const n_tiles = ((int64_t)N + g.bn - 1) / g.bn;
     if (m_tiles > 0x7FFFFFFFLL || n_tiles > 65535) return fail(XTG_E_CAPACITY, "xtg_mlp_gemm: grid too large");
+    if (g.load == LOAD_TMA) {
+        // persistent: one CTA per SM over the tiles
+        int dev = 0, sms = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(gemm_tc_persistent_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)P_MAX_DSMEM);
+        if (e != cudaSuccess) {
+            snprintf(g_mlp_err, sizeof(g_mlp_err), "xtg_mlp_gemm: %s", cudaGetErrorString(e));
+            return XTG_E_CUDA;
+        }
+        int64_t const total = m_tiles * n_tiles;
+        unsigned const grid = (unsigned)(total < (int64_t)sms ? total : (int64_t)sms);
+        uint32_t const dsmem = P_STAGES * (A_STAGE_BYTES + (uint32_t)g.bn * TK * 2) + 1024;
+        gemm_tc_persistent_kernel<<<grid, P_THREADS, dsmem, (cudaStream_t)stream>>>(ta, tb, g);
+        xtg_internal_launch_add(1);
+        return launched("gemm_tc_persistent_kernel");
+    }
     uint32_t const dsmem = STAGES * (A_STAGE_BYTES + (uint32_t)g.bn * TK * 2) + 1024;
     cudaError_t e = cudaFuncSetAttribute(gemm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)MAX_DSMEM);
     if (e != cudaSuccess) {
