@@ -385,11 +385,6 @@ __device__ __noinline__ void multi_element_monitor(const xtg_multi_element_monit
         }
     }
 }
-// Transverse shift and tilt of a record (F_SHIFTED, ApertureShift in
-// xtg_table.h: apertures, thin Multipoles, DipoleEdges): the entry
-// transform for the particle reaching the element, the exit transform only
-// if it survives; both also when local apertures are ignored. The block is found again from the header at the exit, so that
-// nothing stays live across the check.
 // limitpolygon.h:64-90: the crossing-number test with the inscribed-circle
 // shortcut of the CPU build; out of line (polygons are rare in a turn)
 __device__ __noinline__ bool polygon_alive(double x, double y, const unsigned char* __restrict__ rec) {
@@ -417,8 +412,13 @@ __device__ __forceinline__ void s_rotation(PState& p, double sin_z, double cos_z
     p.px = cos_z * px + sin_z * py;
     p.py = -sin_z * px + cos_z * py;
 }
-// Entry and exit of a transformed aperture; out of line, so that the
-// common untransformed aperture keeps a flag test only.
+// Transverse shift and tilt of a record (F_SHIFTED, ApertureShift in
+// xtg_table.h: apertures, thin Multipoles, DipoleEdges): the entry
+// transform for the particle reaching the element, the exit transform only
+// if it survives; both also when local apertures are ignored. The block is
+// found again from the header at the exit, so that nothing stays live
+// across the check. The transforms run out of line, so that the common
+// untransformed record keeps a flag test only.
 XTG_COLD PState aperture_transform_in(PState p, const ApertureShift* __restrict__ sh) {
     p.x = p.x + sh->in_x;
     p.y = p.y + sh->in_y;
