@@ -454,8 +454,8 @@ int32_t xtg_check_bounded_wait(int64_t limit_cycles);
  * A[m*a_sm + k*a_sk] and B(n, k) at B[n*b_sn + k*b_sk] (bf16, any strides),
  * FP32 accumulation in tensor memory (tcgen05). Operands with a unit stride
  * along k or along their rows, a 16-byte aligned base and a pitch that is a
- * multiple of 8 elements are staged by TMA; others by the threads (same
- * results). Epilogue: z = R + bias[n] (bias may be NULL);
+ * multiple of 8 elements are staged by TMA (a persistent kernel, one CTA per
+ * SM); others by the threads (same results). Epilogue: z = R + bias[n] (bias may be NULL);
  * Z[m*z_ld + n] = z (fp32, optional); Y[m*y_ld + n] = act(z) (bf16,
  * optional); C[m*c_ld + n] = z, or += z with c_accumulate (fp32, optional). */
 int32_t xtg_mlp_gemm(const void* A, int64_t a_sm, int64_t a_sk, const void* B,
