@@ -365,6 +365,39 @@ def test_guided_da_scan_places_the_window_by_the_network():
     assert res.tracked.sum() < 0.8 * res0.tracked.sum()
 
 
+def test_guided_and_adaptive_scans_edge_cases():
+    """Rays that survive everywhere: both scans track only their sentinels
+    (no loss, no bracket) and report the ray's largest amplitude as its DA;
+    a network that calls every amplitude lost places its window at the
+    ray's smallest amplitude; a ray lost from its first amplitude has DA
+    equal to it."""
+    from xtrack_gb300 import scan as sc
+    na = 500
+    s = sc.Scan()
+    s.r = np.tile(np.arange(1.0, na + 1.0), 3)
+    s.theta = np.repeat(np.array([0.1, 0.2, 0.3]), na)
+    s.lattice_index = np.zeros(3 * na, dtype=np.int32)
+    s.delta_index = np.zeros(3 * na, dtype=np.int64)
+    s.deltas = np.array([0.0])
+    ray = s.ray_index()
+    truth = np.ones(3 * na, dtype=bool)
+    truth[ray == 2] = False                      # ray 2 lost from its first amplitude
+    p_all_lost = np.zeros(3 * na)
+    assert np.all(sc.predicted_boundary(p_all_lost, s) == 1.0)
+    p_never = np.ones(3 * na)
+    assert np.all(sc.predicted_boundary(p_never, s) == float(na))
+    for fn in (lambda: sc.guided_da_scan(None, s, 10, p_never, coarse=50, fine=5, below=20.0,
+                                         above=5.0, track_fn=lambda m: truth[m]),
+               lambda: sc.adaptive_da_scan(None, s, 10, coarse=50, fine=5, window=20.0,
+                                           track_fn=lambda m: truth[m])):
+        res = fn()
+        assert res.da.ravel().tolist() == [float(na), float(na), 1.0]
+        assert np.array_equal(res.survive, truth | (ray != 2))
+        # the surviving rays are tracked at their sentinels (and window) only
+        for k in (0, 1):
+            assert res.tracked[ray == k].sum() <= na // 5 + 2
+
+
 @pytest.mark.gpu
 def test_screened_da_scan_equals_plain_scan_on_most_rays():
     """End to end on a short ring. The screened DA scan (sentinels every
